@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 tile-splat compositor.
+
+Headline: frames/s of the 760k-splat 1920x1080 hot-tile workload (seeded
+synthetic scene; see the package's workloads module), one full frame per
+step: projection, tile counting, scans, key emission, radix sort, per-tile
+sort with the hot-tile cascade, rasteriser.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value   frames/s with the scene resident in HBM; each step is timed with CUDA
+        events on the launching stream and a 256 MiB buffer is written between
+        steps to flush the 129 MB L2 (the flush is outside the timed events).
+e2e     the same frames/s through the C ABI with host buffers: every step
+        copies the scene from pinned host memory to the device, encodes the
+        frame and copies the four output images back.
+--impl reference  times the reference's CPU path restated in C (the oracle;
+        the reference itself is TypeScript/WGSL and cannot run here) on the
+        same workload with all host threads, one full frame per step.
+N > 1   runs N independent replicas (one per GPU); value = frames of all ranks
+        / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__  # noqa: E402
+
+METRIC = "760k-splat 1080p frames/s"
+UNIT = "frames/s"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in self.rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def setup_frame(pkg, wl, device_index=0):
+    """Packed scene, plan, uniforms, bound compositor sized to the frame."""
+    import torch
+
+    scene = wl.scene
+    cam = wl.cameras[0]
+    packed = pkg.splats.pack_splat_attributes(scene)
+    plan = pkg.plan_tile_splat_compositor(wl.width, wl.height, 16, scene.count)
+    u, fr = pkg.frame_uniforms_for(plan, cam, sh_degree=scene.sh_degree)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    bufs = pkg.splats.upload_splat_attribute_buffers(packed, order, device=f"cuda:{device_index}")
+    color, gb = pkg.create_output_textures(plan, device=f"cuda:{device_index}")
+    res = pkg.create_tile_splat_compositor(plan)
+    pkg.create_tile_splat_bind_groups(res, bufs, color, gb)
+    pkg.write_frame_uniform_buffer(res, u)
+    pkg.encode_full_compute_compositor_pipeline(None, res)
+    st = res.query_status()
+    if st["status"] == pkg._lib.HDSR_ERR_OVERFLOW:
+        # the reference grows its tile-entry budget from a readback of the
+        # frame's needs (gpuTileSplatCompositor.ts:123-126); size it exactly
+        need = int(st["total_pairs"])
+        res.destroy()
+        res = pkg.create_tile_splat_compositor(plan, pair_capacity=int(need * 1.02) + 1024)
+        pkg.create_tile_splat_bind_groups(res, bufs, color, gb)
+        pkg.write_frame_uniform_buffer(res, u)
+        pkg.encode_full_compute_compositor_pipeline(None, res)
+        st = res.check_frame()
+    torch.cuda.synchronize()
+    return dict(packed=packed, plan=plan, u=u, order=order, bufs=bufs, color=color, gb=gb, res=res, stats=st)
+
+
+def pass_bytes(name: str, N: int, P: int, px: int, sh_floats: int) -> float | None:
+    """Algorithmic HBM bytes of one launch of a pass (None: not HBM-bound)."""
+    if name == "project":
+        return N * (4 + 12 + 12 + 16 + 4 + 4 + 4 * sh_floats + 16 + 16 + 16 + 8 + 4 + 4)
+    if name == "count":
+        return N * (8 + 4 + 4)
+    if name == "scan_pairs":
+        return N * 8
+    if name == "emit_keys":
+        return N * 20 + P * 8
+    if name == "radix_hist":
+        return P * 8
+    if name.startswith("radix_pass"):
+        return P * 16
+    if name == "segment_sort":
+        return P * 12
+    return None
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    pkg = __graft_entry__.load_package()
+    pkg._build.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl = pkg.workloads.WORKLOADS[args.workload]()
+    F = setup_frame(pkg, wl, local)
+    res, plan = F["res"], F["plan"]
+    N, P = plan.splat_count, int(F["stats"]["total_pairs"])
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def frame():
+        pkg.encode_full_compute_compositor_pipeline(stream, res)
+
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    res.set_profiling(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = res.launch_count()
+    times, passes = [], {}
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            frame()
+            e.record(stream)
+            for name, ms in res.pass_times():
+                passes.setdefault(name, []).append(ms)
+            e.synchronize()
+            times.append(s.elapsed_time(e))
+        torch.cuda.synchronize()
+    launches = res.launch_count() - launches0
+    st = res.check_frame()
+    res.set_profiling(False)
+    total_s = sum(times) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = args.steps * world / total_s
+
+    # end to end through the C ABI with host buffers
+    e2e = run_e2e(pkg, F, args, stream, world, dev)
+
+    # roofline of the dominant HBM-bound pass
+    sh_floats = 6 + 3 * ((wl.scene.sh_degree + 1) ** 2 - 1)
+    mean_pass = {k: statistics.mean(v) for k, v in passes.items()}
+    frame_ms = statistics.mean(times)
+    hbm_passes = {k: v for k, v in mean_pass.items() if pass_bytes(k, N, P, plan.viewport_width * plan.viewport_height,
+                                                                  sh_floats)}
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom = max(hbm_passes, key=hbm_passes.get) if hbm_passes else None
+    roofline = None
+    if dom:
+        b = pass_bytes(dom, N, P, 0, sh_floats)
+        ach = b / (mean_pass[dom] / 1000.0) / 1e9
+        traffic = load_traffic(dom)
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(ach / peak, 4), "traffic": traffic,
+                    "algorithmic_bytes": int(b), "launch_ms": round(mean_pass[dom], 4),
+                    "peak_source": "measured" if peaks else "fallback"}
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {**wl.describe(), "pairs": P, "hot_tiles": int(st["hot_tiles"]), "chunks": int(st["chunks"]),
+                   "segments": int(st["segments"]), "l2": "256 MiB flush between timed steps",
+                   "parallelism": f"replicas{world}"},
+        "e2e": e2e, "gpu_launches": int(launches),
+        "passes_ms": {k: round(v, 4) for k, v in mean_pass.items()},
+        "pass_share": {k: round(v / frame_ms, 4) for k, v in mean_pass.items()},
+        "roofline": roofline, "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(pkg, wl, F)
+    if world > 1:
+        torch.distributed.barrier()
+    if rank == 0:
+        print(json.dumps(out))
+    res.destroy()
+
+
+def load_traffic(kernel: str):
+    """dram bytes per launch from the committed ncu summary, when present."""
+    f = ROOT / "profiles" / "traffic.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d.get(kernel)
+    return None
+
+
+def run_e2e(pkg, F, args, stream, world, dev):
+    import torch
+
+    bufs, res = F["bufs"], F["res"]
+    names = ["positions", "scales", "rotations", "opacities", "material", "sh_data", "sorted_indices"]
+    host = {k: bufs[k].cpu().pin_memory() for k in names}
+    outs = [F["color"], F["gb"]["depth"], F["gb"]["normal"], F["gb"]["material"]]
+    host_out = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs]
+    h2d = sum(h.numel() * h.element_size() for h in host.values())
+    d2h = sum(o.numel() * o.element_size() for o in outs)
+
+    def step():
+        for k in names:
+            bufs[k].copy_(host[k], non_blocking=True)
+        pkg.write_frame_uniform_buffer(res, F["u"])
+        pkg.encode_full_compute_compositor_pipeline(stream, res)
+        for o, h in zip(outs, host_out):
+            h.copy_(o, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(args.steps):
+        step()
+    e.record(stream)
+    e.synchronize()
+    total_s = s.elapsed_time(e) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    return {"value": round(args.steps * world / total_s, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h)}
+
+
+def cpu_baseline(pkg, wl, F=None, threads=None, frames=1) -> dict:
+    """The oracle (C restatement of the reference passes) on the host cores:
+    full frames of the same workload, plus the reference's CPU depth sort."""
+    import oracle
+
+    threads = threads or os.cpu_count() or 1
+    packed = F["packed"] if F else pkg.splats.pack_splat_attributes(wl.scene)
+    if F:
+        u, order = F["u"], F["order"]
+    else:
+        plan = pkg.plan_tile_splat_compositor(wl.width, wl.height, 16, wl.scene.count)
+        u, fr = pkg.frame_uniforms_for(plan, wl.cameras[0], sh_degree=wl.scene.sh_degree)
+        order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    cap = int(F["stats"]["total_pairs"]) + 16 if F else None
+    oracle.render_frame(u, packed, order, threads=threads, cap=cap)  # warm (page-in, allocation)
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        oracle.render_frame(u, packed, order, threads=threads, cap=cap)
+    dt = time.perf_counter() - t0
+    view = wl.cameras[0].view_matrix()
+    t1 = time.perf_counter()
+    oracle.sort_back_to_front(packed.positions, view, threads=1)
+    sort_ms = (time.perf_counter() - t1) * 1000.0
+    return {"value": round(frames / dt, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{frames} full frame(s) of {wl.name} through the oracle (C, OpenMP)",
+            "cpu_depth_sort_ms": round(sort_ms, 2), "cpu_depth_sort": "splatSort.ts sortSplatIdsBackToFront, "
+                                                                       "C restatement, 1 thread"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    pkg = __graft_entry__.load_package()
+    import oracle
+
+    oracle.build()
+    wl = pkg.workloads.WORKLOADS[args.workload]()
+    threads = os.cpu_count() or 1
+    packed = pkg.splats.pack_splat_attributes(wl.scene)
+    plan = pkg.plan_tile_splat_compositor(wl.width, wl.height, 16, wl.scene.count)
+    u, fr = pkg.frame_uniforms_for(plan, wl.cameras[0], sh_degree=wl.scene.sh_degree)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = oracle.render_frame(u, packed, order, threads=threads, composite=False)
+    cap = f["total_pairs"] + 16
+    for _ in range(args.warmup):
+        oracle.render_frame(u, packed, order, threads=threads, cap=cap)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.render_frame(u, packed, order, threads=threads, cap=cap)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    out = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(dt * 1000.0 / args.steps, 2), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "impl": "reference", "config": {**wl.describe(), "pairs": int(f["total_pairs"])},
+           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"one full frame of {wl.name} per step through the oracle (C restatement "
+                                      f"of the reference's WGSL passes; the TypeScript/WebGPU original cannot "
+                                      f"run on this machine)"},
+           "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hot760k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    try:
+        run_ours(args, rank, world, local)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,465 @@
+// hdsr_api.cu — the C ABI declared in include/hdsr.h.
+//
+// Host-side mirror of the reference operator API in
+// src/gpuTileSplatCompositor.ts: plan (:109-139), create (:141-728), bind
+// (:792-995), frame uniforms (:730-774), encode full (:1023-1179) and
+// composite-only (:1001-1014), destroy. The handle owns every internal
+// device buffer; scene and output buffers are borrowed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/hdsr.h"
+#include "hdsr_internal.cuh"
+
+using namespace hdsr;
+
+namespace {
+constexpr uint32_t kMaxProfiledPasses = 24;
+// names of the profiled passes, indexed by the ids recorded in encode()
+const char* const kPassNames[] = {"upload_uniforms", "frame_init", "project", "count", "scan_pairs",
+                                  "scan_tiles", "emit_keys", "radix_hist", "radix_pass_0", "radix_pass_1",
+                                  "radix_pass_2", "radix_pass_3", "radix_pass_4", "radix_pass_5",
+                                  "radix_pass_6", "radix_pass_7", "segment_sort", "raster"};
+constexpr uint32_t kNumPassNames = sizeof(kPassNames) / sizeof(kPassNames[0]);
+}  // namespace
+
+struct hdsr_compositor {
+  hdsr_plan plan{};
+  hdsr_config cfg{};
+  int device = 0;
+  FrameArgs args{};
+  std::vector<void*> allocs;
+  float uniforms[64] = {};
+  bool have_uniforms = false;
+  bool scene_bound = false;
+  bool outputs_bound = false;
+  bool sorted_valid = false;
+  cudaStream_t last_stream = nullptr;
+  bool has_last_stream = false;
+  uint64_t launches = 0;           // kernels queued by this handle
+  bool profiling = false;
+  cudaEvent_t ev[kMaxProfiledPasses + 1] = {};
+  uint32_t ev_used = 0;
+  uint32_t pass_id[kMaxProfiledPasses] = {};
+  char err[256] = {0};
+};
+
+namespace {
+
+char g_null_err[] = "null handle";
+
+hdsr_status fail(hdsr_compositor* h, hdsr_status s, const char* msg) {
+  if (h) std::snprintf(h->err, sizeof(h->err), "%s", msg);
+  return s;
+}
+
+hdsr_status cuda_fail(hdsr_compositor* h, cudaError_t e, const char* where) {
+  if (h) std::snprintf(h->err, sizeof(h->err), "%s: %s", where, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? HDSR_ERR_OOM : HDSR_ERR_CUDA;
+}
+
+uint32_t ceil_log2(uint64_t v) {
+  uint32_t b = 0;
+  while ((1ull << b) < v) ++b;
+  return b;
+}
+
+template <class T>
+hdsr_status dev_alloc(hdsr_compositor* h, T** p, uint64_t count, const char* what) {
+  uint64_t bytes = count * sizeof(T);
+  if (bytes == 0) bytes = 16;
+  void* ptr = nullptr;
+  cudaError_t e = cudaMalloc(&ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    char msg[128];
+    std::snprintf(msg, sizeof(msg), "cudaMalloc %s (%llu bytes)", what, (unsigned long long)bytes);
+    return cuda_fail(h, e, msg);
+  }
+  h->allocs.push_back(ptr);
+  *p = static_cast<T*>(ptr);
+  return HDSR_OK;
+}
+
+void free_all(hdsr_compositor* h) {
+  for (void* p : h->allocs) cudaFree(p);
+  h->allocs.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t hdsr_abi_version(void) { return HDSR_ABI_VERSION; }
+
+hdsr_status hdsr_plan_tile_splat_compositor(const hdsr_plan_input* in, hdsr_plan* out) {
+  if (!in || !out) return HDSR_ERR_INVALID_ARG;
+  if (in->viewport_width == 0 || in->viewport_height == 0 || in->tile_size_px == 0) return HDSR_ERR_INVALID_ARG;
+  const uint32_t t = in->tile_size_px;
+  out->viewport_width = in->viewport_width;
+  out->viewport_height = in->viewport_height;
+  out->tile_size_px = t;
+  out->tile_columns = (in->viewport_width + t - 1) / t;
+  out->tile_rows = (in->viewport_height + t - 1) / t;
+  out->tile_count = out->tile_columns * out->tile_rows;
+  out->morton_tile_count = morton(out->tile_columns - 1, out->tile_rows - 1) + 1;
+  out->splat_count = in->splat_count;
+  const double mult = in->tile_entry_multiplier > 0.0 ? in->tile_entry_multiplier : 16.0;
+  const double want = std::ceil((double)in->splat_count * mult);
+  const double cap = 65535.0 * 256.0;
+  out->max_total_tile_refs = (uint32_t)(want < cap ? want : cap);
+  return HDSR_OK;
+}
+
+hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_config* cfg,
+                                              hdsr_compositor** out) {
+  if (!plan || !out) return HDSR_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (plan->tile_size_px != kTilePx) return HDSR_ERR_UNSUPPORTED;
+  if (plan->tile_columns == 0 || plan->tile_rows == 0 || plan->tile_columns > 255 || plan->tile_rows > 255)
+    return HDSR_ERR_UNSUPPORTED;  // the u8x4 tile box packs <= 255 tiles per axis
+  hdsr_compositor* h = new (std::nothrow) hdsr_compositor();
+  if (!h) return HDSR_ERR_OOM;
+  h->plan = *plan;
+  if (cfg) h->cfg = *cfg;
+  if (h->cfg.color_format > HDSR_COLOR_RGBA32F) { delete h; return HDSR_ERR_INVALID_ARG; }
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) { hdsr_status s = cuda_fail(h, e, "cudaGetDevice"); delete h; return s; }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const uint32_t N = plan->splat_count, M = plan->morton_tile_count;
+  uint64_t cap = h->cfg.pair_capacity;
+  if (cap == 0) {
+    uint64_t want = (uint64_t)std::ceil((double)N * 16.0);
+    cap = want > plan->max_total_tile_refs ? want : plan->max_total_tile_refs;
+  }
+  if (cap < 16) cap = 16;
+  if (cap >= (1ull << 32)) { delete h; return HDSR_ERR_UNSUPPORTED; }
+  h->cfg.pair_capacity = cap;
+  FrameArgs& a = h->args;
+  a.N = N;
+  a.W = plan->viewport_width;
+  a.H = plan->viewport_height;
+  a.cols = plan->tile_columns;
+  a.rows = plan->tile_rows;
+  a.M = M;
+  a.tile_count = plan->tile_count;
+  a.rank_bits = ceil_log2(N > 1 ? N : 2);
+  a.key_bits = 20u + ceil_log2(M > 1 ? M : 2);
+  if (a.rank_bits + a.key_bits > 64u) { delete h; return HDSR_ERR_UNSUPPORTED; }
+  a.passes = (a.key_bits + 7u) / 8u;
+  a.cap = cap;
+  a.num_sms = sms > 0 ? sms : 1;
+  a.color_f32 = h->cfg.color_format == HDSR_COLOR_RGBA32F;
+  a.seg_cap = (uint32_t)(plan->tile_count + cap / kMaxTileEntries + 1);
+  a.radix_tiles_cap = (uint32_t)((cap + kRadixTile - 1) / kRadixTile);
+  const uint64_t scan_tiles_n = (N + kScanTile - 1) / kScanTile + 1;
+  const uint64_t scan_tiles_m = (M + kScanTile - 1) / kScanTile + 1;
+  hdsr_status s = HDSR_OK;
+  float* U = nullptr;
+#define ALLOC(ptr, n, what) \
+  if (s == HDSR_OK) s = dev_alloc(h, &(ptr), (n), (what))
+  ALLOC(U, 64, "uniforms");
+  ALLOC(a.geo, N, "cache_geo");
+  ALLOC(a.app, N, "cache_app");
+  ALLOC(a.gb, N, "cache_gb");
+  ALLOC(a.aux, N, "cache_aux");
+  ALLOC(a.depth, N, "depth");
+  ALLOC(a.ntiles, N, "ntiles");
+  ALLOC(a.pair_off, N, "pair_off");
+  ALLOC(a.tile_cnt, M, "tile_counts");
+  ALLOC(a.tile_dmin, M, "tile_dmin");
+  ALLOC(a.tile_dmax, M, "tile_dmax");
+  ALLOC(a.tile_off, M, "tile_offsets");
+  ALLOC(a.tile_log, M, "tile_log");
+  ALLOC(a.pairs_a, cap, "pairs_a");
+  ALLOC(a.pairs_b, cap, "pairs_b");
+  ALLOC(a.entries, cap, "tile_entries");
+  if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
+  ALLOC(a.segments, a.seg_cap, "segments");
+  ALLOC(a.digit_hist, (uint64_t)kMaxPasses * 256, "digit_hist");
+  ALLOC(a.radix_status, (uint64_t)a.passes * a.radix_tiles_cap * 256, "radix_status");
+  ALLOC(a.scan_status_n, scan_tiles_n, "scan_status_n");
+  ALLOC(a.scan_status_m, scan_tiles_m, "scan_status_m");
+  ALLOC(a.ctl, (uint64_t)kCtlWords, "ctl");
+#undef ALLOC
+  if (s != HDSR_OK) { free_all(h); delete h; return s; }
+  a.U = U;
+  // status words start at epoch 0, which no frame uses
+  e = cudaMemset(a.radix_status, 0, (size_t)a.passes * a.radix_tiles_cap * 256 * 8);
+  if (e == cudaSuccess) e = cudaMemset(a.scan_status_n, 0, scan_tiles_n * 8);
+  if (e == cudaSuccess) e = cudaMemset(a.scan_status_m, 0, scan_tiles_m * 8);
+  if (e == cudaSuccess) e = cudaMemset(a.ctl, 0, kCtlWords * 4);
+  if (e == cudaSuccess) e = cudaMemset(U, 0, 256);
+  if (e != cudaSuccess) { s = cuda_fail(h, e, "cudaMemset"); free_all(h); delete h; return s; }
+  *out = h;
+  return HDSR_OK;
+}
+
+void hdsr_destroy_tile_splat_compositor(hdsr_compositor* h) {
+  if (!h) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(h->device);
+  cudaDeviceSynchronize();
+  for (cudaEvent_t& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  free_all(h);
+  cudaSetDevice(prev);
+  delete h;
+}
+
+hdsr_status hdsr_bind_scene(hdsr_compositor* h, const hdsr_scene_views* sc) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (!sc) return fail(h, HDSR_ERR_INVALID_ARG, "scene views are NULL");
+  if (sc->splat_count != h->plan.splat_count)
+    return fail(h, HDSR_ERR_INVALID_ARG, "scene splat_count differs from the plan");
+  if (sc->sh_degree > 3) return fail(h, HDSR_ERR_INVALID_ARG, "sh_degree must be 0..3");
+  if (h->plan.splat_count > 0 &&
+      (!sc->positions || !sc->scales || !sc->rotations || !sc->opacities || !sc->material ||
+       !sc->sh_data || !sc->sorted_indices))
+    return fail(h, HDSR_ERR_INVALID_ARG, "a required scene buffer is NULL");
+  if (reinterpret_cast<uintptr_t>(sc->rotations) % 16 != 0)
+    return fail(h, HDSR_ERR_INVALID_ARG, "rotations must be 16-byte aligned");
+  if (sc->normals == nullptr && sc->normals_len != 0)
+    return fail(h, HDSR_ERR_INVALID_ARG, "normals_len without normals");
+  FrameArgs& a = h->args;
+  a.pos = sc->positions;
+  a.scl = sc->scales;
+  a.rot = sc->rotations;
+  a.opa = sc->opacities;
+  a.mat = sc->material;
+  a.nrm = sc->normals;
+  a.nrm_len = sc->normals ? sc->normals_len : 0;
+  a.sh = sc->sh_data;
+  a.sorted = sc->sorted_indices;
+  a.sh_degree = sc->sh_degree;
+  h->scene_bound = true;
+  h->sorted_valid = false;
+  return HDSR_OK;
+}
+
+hdsr_status hdsr_bind_outputs(hdsr_compositor* h, const hdsr_output_views* o) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (!o || !o->color || !o->depth || !o->normal || !o->material)
+    return fail(h, HDSR_ERR_INVALID_ARG, "an output buffer is NULL");
+  const uint64_t W = h->plan.viewport_width;
+  const uint64_t cbytes = h->args.color_f32 ? 16 : 8;
+  if (o->color_pitch < W * cbytes || o->depth_pitch < W * 4 || o->normal_pitch < W * 4 ||
+      o->material_pitch < W * 16)
+    return fail(h, HDSR_ERR_INVALID_ARG, "an output pitch is smaller than one row");
+  if (o->color_pitch % cbytes || o->depth_pitch % 4 || o->normal_pitch % 4 || o->material_pitch % 16 ||
+      reinterpret_cast<uintptr_t>(o->color) % cbytes || reinterpret_cast<uintptr_t>(o->material) % 16 ||
+      reinterpret_cast<uintptr_t>(o->depth) % 4 || reinterpret_cast<uintptr_t>(o->normal) % 4)
+    return fail(h, HDSR_ERR_INVALID_ARG, "output buffers or pitches are misaligned");
+  FrameArgs& a = h->args;
+  a.out_color = o->color;
+  a.color_pitch = o->color_pitch;
+  a.out_depth = o->depth;
+  a.depth_pitch = o->depth_pitch;
+  a.out_normal = o->normal;
+  a.normal_pitch = o->normal_pitch;
+  a.out_material = o->material;
+  a.material_pitch = o->material_pitch;
+  h->outputs_bound = true;
+  return HDSR_OK;
+}
+
+void hdsr_write_tile_splat_frame_uniforms(float* target, const float* view_proj, const hdsr_plan* plan,
+                                          float splat_scale, uint32_t sh_degree, const float* camera_pos,
+                                          const float* view_matrix, const float* proj_matrix,
+                                          const float* normal_matrix) {
+  if (!target || !view_proj || !plan) return;
+  auto put_u32 = [&](int i, uint32_t v) { std::memcpy(target + i, &v, 4); };
+  for (int i = 0; i < 16; ++i) target[i] = view_proj[i];
+  target[16] = (float)plan->viewport_width;
+  target[17] = (float)plan->viewport_height;
+  target[18] = (float)plan->tile_size_px;
+  target[19] = 0.0f;
+  put_u32(20, plan->tile_columns);
+  put_u32(21, plan->tile_rows);
+  put_u32(22, plan->splat_count);
+  put_u32(23, plan->max_total_tile_refs);
+  target[24] = splat_scale;
+  put_u32(25, sh_degree);
+  if (camera_pos) { target[28] = camera_pos[0]; target[29] = camera_pos[1]; target[30] = camera_pos[2]; }
+  if (view_matrix) for (int i = 0; i < 16; ++i) target[32 + i] = view_matrix[i];
+  if (proj_matrix) {
+    // JS evaluates viewport * proj * 0.5 in double, then stores to f32
+    target[48] = (float)((double)plan->viewport_width * (double)proj_matrix[0] * 0.5);
+    target[49] = (float)((double)plan->viewport_height * (double)proj_matrix[5] * 0.5);
+  }
+  static const float kIdentity[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  const float* n = normal_matrix ? normal_matrix : kIdentity;
+  target[52] = n[0]; target[53] = n[1]; target[54] = n[2]; target[55] = 0.0f;
+  target[56] = n[3]; target[57] = n[4]; target[58] = n[5]; target[59] = 0.0f;
+  target[60] = n[6]; target[61] = n[7]; target[62] = n[8]; target[63] = 0.0f;
+}
+
+hdsr_status hdsr_set_frame_uniforms(hdsr_compositor* h, const float* u) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (!u) return fail(h, HDSR_ERR_INVALID_ARG, "uniforms are NULL");
+  uint32_t n, gx, gy, deg;
+  std::memcpy(&gx, u + 20, 4);
+  std::memcpy(&gy, u + 21, 4);
+  std::memcpy(&n, u + 22, 4);
+  std::memcpy(&deg, u + 25, 4);
+  if (n != h->plan.splat_count || gx != h->plan.tile_columns || gy != h->plan.tile_rows)
+    return fail(h, HDSR_ERR_INVALID_ARG, "uniform block does not match the plan");
+  if (deg > 3) return fail(h, HDSR_ERR_INVALID_ARG, "uniform shDegree must be 0..3");
+  if (u[16] != (float)h->plan.viewport_width || u[17] != (float)h->plan.viewport_height || u[18] != (float)kTilePx)
+    return fail(h, HDSR_ERR_INVALID_ARG, "uniform viewport / tile size does not match the plan");
+  std::memcpy(h->uniforms, u, sizeof(h->uniforms));
+  h->have_uniforms = true;
+  return HDSR_OK;
+}
+
+// Records a profiling event after pass `id` (no-op unless profiling).
+static void mark(hdsr_compositor* h, cudaStream_t s, uint32_t id) {
+  if (!h->profiling || h->ev_used >= kMaxProfiledPasses) return;
+  h->pass_id[h->ev_used] = id;
+  cudaEventRecord(h->ev[++h->ev_used], s);
+}
+
+static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (!h->scene_bound || !h->outputs_bound) return fail(h, HDSR_ERR_NOT_BOUND, "bind scene and outputs first");
+  if (!h->have_uniforms) return fail(h, HDSR_ERR_NOT_BOUND, "set frame uniforms first");
+  if (!full && !h->sorted_valid) return fail(h, HDSR_ERR_NOT_BOUND, "no sorted entries: encode_full first");
+  uint32_t deg;
+  std::memcpy(&deg, h->uniforms + 25, 4);
+  if (deg != h->args.sh_degree) return fail(h, HDSR_ERR_INVALID_ARG, "uniform shDegree differs from the bound scene");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  FrameArgs& a = h->args;
+  h->ev_used = 0;
+  if (h->profiling) cudaEventRecord(h->ev[0], s);
+  cudaError_t e = cudaMemcpyAsync(const_cast<float*>(a.U), h->uniforms, 256, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "upload uniforms");
+  mark(h, s, 0);
+  const uint64_t n_splat_launch = a.N ? 1 : 0;
+  if (full) {
+    if ((e = launch_frame_init(a, s)) != cudaSuccess) return cuda_fail(h, e, "frame_init");
+    mark(h, s, 1);
+    if ((e = launch_project(a, s)) != cudaSuccess) return cuda_fail(h, e, "project");
+    mark(h, s, 2);
+    if ((e = launch_count(a, s)) != cudaSuccess) return cuda_fail(h, e, "count");
+    mark(h, s, 3);
+    if ((e = launch_scan_pairs(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_pairs");
+    mark(h, s, 4);
+    if ((e = launch_scan_tiles(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
+    mark(h, s, 5);
+    if ((e = launch_emit(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit");
+    mark(h, s, 6);
+    if ((e = launch_radix_hist(a, s)) != cudaSuccess) return cuda_fail(h, e, "radix_hist");
+    mark(h, s, 7);
+    for (uint32_t p = 0; p < a.passes; ++p) {
+      if ((e = launch_radix_pass(a, s, p)) != cudaSuccess) return cuda_fail(h, e, "radix_pass");
+      mark(h, s, 8 + p);
+    }
+    if ((e = launch_segment_sort(a, s)) != cudaSuccess) return cuda_fail(h, e, "segment_sort");
+    mark(h, s, 16);
+    h->launches += 1 + 3 * n_splat_launch + 2 + 2 + a.passes + 1;
+  }
+  if ((e = launch_raster(a, s)) != cudaSuccess) return cuda_fail(h, e, "raster");
+  mark(h, s, 17);
+  if (a.tile_count) h->launches += 1;
+  h->last_stream = s;
+  h->has_last_stream = true;
+  if (full) h->sorted_valid = true;
+  return HDSR_OK;
+}
+
+hdsr_status hdsr_encode_full(hdsr_compositor* h, void* stream) { return encode(h, stream, true); }
+
+hdsr_status hdsr_encode_composite_only(hdsr_compositor* h, void* stream) { return encode(h, stream, false); }
+
+hdsr_status hdsr_query_status(hdsr_compositor* h, hdsr_frame_stats* st) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  cudaError_t e = h->has_last_stream ? cudaStreamSynchronize(h->last_stream) : cudaSuccess;
+  if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+  uint32_t ctl[kCtlWords];
+  e = cudaMemcpy(ctl, h->args.ctl, sizeof(ctl), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(h, e, "read status");
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    st->total_pairs = (uint64_t)ctl[kCtlPairsLo] | ((uint64_t)ctl[kCtlPairsHi] << 32);
+    st->pair_capacity = h->args.cap;
+    st->visible_splats = ctl[kCtlVisible];
+    st->segments = ctl[kCtlSegments];
+    st->hot_tiles = ctl[kCtlHotTiles];
+    st->chunks = ctl[kCtlChunks];
+    st->device_flags = ctl[kCtlFlags];
+  }
+  if (ctl[kCtlFlags] & HDSR_DEV_OVERFLOW) {
+    h->sorted_valid = false;
+    return fail(h, HDSR_ERR_OVERFLOW, "frame needs more (tile, splat) pairs than pair_capacity");
+  }
+  if (ctl[kCtlFlags] & HDSR_DEV_TIMEOUT) return fail(h, HDSR_ERR_TIMEOUT, "a device-side wait gave up");
+  return HDSR_OK;
+}
+
+const char* hdsr_last_error(const hdsr_compositor* h) { return h ? h->err : g_null_err; }
+
+hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, uint64_t* bytes) {
+  if (!h || !ptr || !bytes) return HDSR_ERR_INVALID_ARG;
+  const FrameArgs& a = h->args;
+  const uint64_t N = a.N, M = a.M, cap = a.cap;
+  switch (id) {
+    case HDSR_BUF_CACHE_GEO: *ptr = a.geo; *bytes = N * 16; break;
+    case HDSR_BUF_CACHE_APP: *ptr = a.app; *bytes = N * 16; break;
+    case HDSR_BUF_CACHE_GB: *ptr = a.gb; *bytes = N * 16; break;
+    case HDSR_BUF_CACHE_AUX: *ptr = a.aux; *bytes = N * 8; break;
+    case HDSR_BUF_DEPTH: *ptr = a.depth; *bytes = N * 4; break;
+    case HDSR_BUF_TILE_COUNTS: *ptr = a.tile_cnt; *bytes = M * 4; break;
+    case HDSR_BUF_TILE_OFFSETS: *ptr = a.tile_off; *bytes = M * 4; break;
+    case HDSR_BUF_TILE_ENTRIES: *ptr = a.entries; *bytes = cap * 4; break;
+    case HDSR_BUF_SORTED_KEYS:
+      if (!a.sorted_keys) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_KEEP_SORTED_KEYS");
+      *ptr = a.sorted_keys; *bytes = cap * 8; break;
+    case HDSR_BUF_PAIR_OFFSETS: *ptr = a.pair_off; *bytes = N * 4; break;
+    case HDSR_BUF_SEGMENTS: *ptr = a.segments; *bytes = (uint64_t)a.seg_cap * 8; break;
+    default: return fail(h, HDSR_ERR_INVALID_ARG, "unknown buffer id");
+  }
+  return HDSR_OK;
+}
+
+uint32_t hdsr_rank_bits(const hdsr_compositor* h) { return h ? h->args.rank_bits : 0u; }
+
+hdsr_status hdsr_set_profiling(hdsr_compositor* h, int enable) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (enable) {
+    for (cudaEvent_t& ev : h->ev) {
+      if (ev) continue;
+      cudaError_t e = cudaEventCreate(&ev);
+      if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventCreate");
+    }
+  }
+  h->profiling = enable != 0;
+  return HDSR_OK;
+}
+
+hdsr_status hdsr_pass_times(hdsr_compositor* h, float* ms, uint32_t* ids, uint32_t max, uint32_t* count) {
+  if (!h || !count) return HDSR_ERR_INVALID_ARG;
+  *count = 0;
+  if (!h->profiling || h->ev_used == 0) return fail(h, HDSR_ERR_NOT_BOUND, "no profiled frame");
+  cudaError_t e = cudaEventSynchronize(h->ev[h->ev_used]);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventSynchronize");
+  uint32_t n = h->ev_used < max ? h->ev_used : max;
+  for (uint32_t i = 0; i < n; ++i) {
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, h->ev[i], h->ev[i + 1]);
+    if (ms) ms[i] = t;
+    if (ids) ids[i] = h->pass_id[i];
+  }
+  *count = n;
+  return HDSR_OK;
+}
+
+const char* hdsr_pass_name(uint32_t id) { return id < kNumPassNames ? kPassNames[id] : "unknown"; }
+
+uint64_t hdsr_launch_count(const hdsr_compositor* h) { return h ? h->launches : 0u; }
+
+}  // extern "C"

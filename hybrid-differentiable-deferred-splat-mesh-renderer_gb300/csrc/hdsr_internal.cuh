@@ -1,0 +1,122 @@
+// hdsr_internal.cuh — device buffer layout of one compositor handle and the
+// launchers each translation unit provides.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hdsr_math.cuh"
+
+namespace hdsr {
+
+// Control block (u32 words) in device memory, one per handle.
+enum Ctl : int {
+  kCtlEpoch = 0,       // frame counter: decoupled-lookback status words carry it
+  kCtlFlags = 1,       // HDSR_DEV_* bits
+  kCtlPairsLo = 2,     // P, total (tile, splat) pairs of the frame (u64)
+  kCtlPairsHi = 3,
+  kCtlSegments = 4,    // sort segments appended by the tile scan
+  kCtlHotTiles = 5,
+  kCtlChunks = 6,
+  kCtlVisible = 7,
+  kCtlScanNTile = 8,   // dynamic tile counters
+  kCtlScanMTile = 9,
+  kCtlRadixTile = 10,  // .. 10 + kMaxPasses - 1
+  kCtlSegTile = 18,
+  kCtlRasterTile = 19,
+  kCtlWords = 64
+};
+constexpr int kMaxPasses = 8;
+
+// Everything a kernel of the frame needs, passed by value.
+struct FrameArgs {
+  const float* U;                 // 64-float frame uniform block (device)
+  // scene (borrowed)
+  const float* pos;
+  const float* scl;
+  const float* rot;
+  const float* opa;
+  const uint32_t* mat;
+  const float* nrm;
+  uint64_t nrm_len;
+  const float* sh;
+  const uint32_t* sorted;
+  uint32_t N;
+  uint32_t sh_degree;
+  // plan
+  uint32_t W, H, cols, rows, M, tile_count;
+  uint32_t rank_bits;             // low key bits holding sortRank
+  uint32_t key_bits;              // 20 + Morton bits: radix-sorted bits above rank_bits
+  uint32_t passes;                // 8-bit digit passes
+  uint64_t cap;                   // pair capacity
+  // projection cache (SoA) and per-splat data
+  float4* geo;                    // centerPx.xy, invCov.xy
+  uint4* app;                     // invCov.z bits, f16(radius,opacity), f16 rg, f16 b|0
+  uint4* gb;                      // material, oct normal, f16 em rg, f16 em b|0
+  uint2* aux;                     // tile box u8x4, f16 normal confidence|0
+  uint32_t* depth;                // f32 NDC depth bits
+  uint32_t* ntiles;               // tiles touched per sortRank (0 if invisible)
+  uint32_t* pair_off;             // exclusive prefix of ntiles
+  // tiles
+  uint32_t* tile_cnt;
+  uint32_t* tile_dmin;
+  uint32_t* tile_dmax;
+  uint32_t* tile_off;
+  float2* tile_log;               // (logMin, keyScale)
+  // pairs and entries
+  unsigned long long* pairs_a;
+  unsigned long long* pairs_b;
+  unsigned long long* sorted_keys;  // optional copy of the radix output
+  uint32_t* entries;              // final per-tile order (sortRank)
+  uint2* segments;                // (start, count)
+  uint32_t seg_cap;
+  // radix
+  uint32_t* digit_hist;           // kMaxPasses * 256 counts, then exclusive bases
+  unsigned long long* radix_status;  // kMaxPasses * radix_tiles_cap * 256
+  uint32_t radix_tiles_cap;
+  unsigned long long* scan_status_n; // per 4096-element tile of the N scan
+  unsigned long long* scan_status_m;
+  uint32_t* ctl;
+  // outputs (borrowed)
+  void* out_color;
+  uint64_t color_pitch;
+  uint32_t color_f32;
+  float* out_depth;
+  uint64_t depth_pitch;
+  uint32_t* out_normal;
+  uint64_t normal_pitch;
+  uint32_t* out_material;
+  uint64_t material_pitch;
+  int num_sms;
+};
+
+// Bounded spin for decoupled-lookback waits (iterations of ~100 ns).
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Lookback status word: epoch (30 bits) | flag (2 bits) | value (32 bits).
+constexpr unsigned long long kFlagAgg = 1ull;
+constexpr unsigned long long kFlagInc = 2ull;
+HDSR_HD unsigned long long make_status(uint32_t epoch, unsigned long long flag, uint32_t v) {
+  return ((unsigned long long)(epoch & 0x3FFFFFFFu) << 34) | (flag << 32) | v;
+}
+
+// launchers (each returns cudaGetLastError() of its launches)
+cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_project(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_count(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_scan_pairs(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_emit(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_radix_hist(const FrameArgs& a, cudaStream_t s);    // 2 launches
+cudaError_t launch_radix_pass(const FrameArgs& a, cudaStream_t s, uint32_t pass);
+cudaError_t launch_segment_sort(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
+
+// sizing helpers shared with the API
+constexpr uint32_t kScanItems = 16;
+constexpr uint32_t kScanThreads = 256;
+constexpr uint32_t kScanTile = kScanItems * kScanThreads;
+constexpr uint32_t kRadixThreads = 256;
+constexpr uint32_t kRadixItems = 15;
+constexpr uint32_t kRadixTile = kRadixThreads * kRadixItems;
+
+}  // namespace hdsr

@@ -1,0 +1,216 @@
+// hdsr_raster.cu — front-to-back tile rasteriser with G-buffer voting.
+//
+// Follows composite in gpu_tile_splat_composite.wgsl:162-370: per pixel
+// (centre at +0.5) over the tile's entries in order, power = -0.5 a dx^2 -
+// 0.5 c dy^2 - b dx dy; skip the splat when all four powers of a 2x2 quad are
+// <= -4; alpha = min(0.99, opacity * exp(power)); a pixel takes the splat
+// only when power > -4, alpha > 1/255 and T >= 0.001; G-buffer votes are
+// gated at weight > 0.01; a quad stops once all four T < 0.001.
+//
+// GB300 layout: one warp owns a 16x16 tile, each lane two 2x2 quads
+// (rows 0-7 and 8-15 of the tile); splat batches of 32 entries are gathered
+// from the SoA projection cache (one entry per lane, 16-byte loads) into the
+// warp's shared-memory slab and then read as broadcasts. FP32 transmittance.
+// Arithmetic is the canonical form: power = fma(c' dy, dy, fma(b' dx, dy,
+// (a' dx) dx)) and every "acc += v * w" is fma(v, w, acc).
+#include "hdsr_internal.cuh"
+
+namespace hdsr {
+
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kFields = 19;
+enum Field { F_CX, F_CY, F_KA, F_KB, F_KC, F_OP, F_R, F_G, F_B, F_D, F_MR, F_MM, F_NX, F_NY, F_NZ, F_CF, F_ER, F_EG, F_EB };
+
+struct Quad {
+  float T[4];
+  float c[4][3];
+  float gd[4], gw[4], gc[4];
+  float m[4][2];
+  float n[4][3];
+  float e[4][3];
+  bool done;
+};
+
+__device__ __forceinline__ void quad_init(Quad& q) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    q.T[i] = 1.0f;
+    q.gd[i] = q.gw[i] = q.gc[i] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { q.c[i][k] = 0.0f; q.n[i][k] = 0.0f; q.e[i][k] = 0.0f; }
+    q.m[i][0] = q.m[i][1] = 0.0f;
+  }
+  q.done = false;
+}
+
+__device__ __forceinline__ void oct_decode(float ex, float ey, float& nx, float& ny, float& nz) {
+  float x = ex, y = ey, z = (1.0f - fabsf(ex)) - fabsf(ey);
+  if (z < 0.0f) {
+    float sx = x >= 0.0f ? 1.0f : -1.0f;
+    float sy = y >= 0.0f ? 1.0f : -1.0f;
+    float x2 = (1.0f - fabsf(y)) * sx;
+    float y2 = (1.0f - fabsf(x)) * sy;
+    x = x2;
+    y = y2;
+  }
+  float l = sqrtf(x * x + y * y + z * z);
+  nx = x / l;
+  ny = y / l;
+  nz = z / l;
+}
+
+__device__ __forceinline__ uint32_t oct_pack_norm(float x, float y, float z) {
+  float l = sqrtf(x * x + y * y + z * z);
+  x = x / l; y = y / l; z = z / l;
+  float sum = fabsf(x) + fabsf(y) + fabsf(z);
+  float px = x / sum, py = y / sum;
+  if (z < 0.0f) {
+    float sx = px >= 0.0f ? 1.0f : -1.0f;
+    float sy = py >= 0.0f ? 1.0f : -1.0f;
+    float nx = (1.0f - fabsf(py)) * sx;
+    float ny = (1.0f - fabsf(px)) * sy;
+    px = nx;
+    py = ny;
+  }
+  return pack2x16(px, py);
+}
+
+__device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, const float (*s)[32], int i) {
+  const float cx = s[F_CX][i], cy = s[F_CY][i];
+  const float ka = s[F_KA][i], kb = s[F_KB][i], kc = s[F_KC][i];
+  const float dx0 = p00x - cx, dy0 = p00y - cy;
+  const float dx1 = dx0 + 1.0f, dy1 = dy0 + 1.0f;
+  const float dxv[4] = {dx0, dx1, dx0, dx1};
+  const float dyv[4] = {dy0, dy0, dy1, dy1};
+  float pw[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) pw[k] = fmaf(kc * dyv[k], dyv[k], fmaf(kb * dxv[k], dyv[k], (ka * dxv[k]) * dxv[k]));
+  if (pw[0] <= -4.0f && pw[1] <= -4.0f && pw[2] <= -4.0f && pw[3] <= -4.0f) return;
+  const float op = s[F_OP][i];
+  const float sr = s[F_R][i], sg = s[F_G][i], sb = s[F_B][i];
+  const float sd = s[F_D][i], mr = s[F_MR][i], mm = s[F_MM][i];
+  const float nx = s[F_NX][i], ny = s[F_NY][i], nz = s[F_NZ][i];
+  const float sc = s[F_CF][i], er = s[F_ER][i], eg = s[F_EG][i], eb = s[F_EB][i];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float g = hx_expf(pw[k]);
+    const float al = mn(0.99f, op * g);
+    const float nT = q.T[k] * (1.0f - al);
+    const bool valid = (pw[k] > -4.0f) && (al > (1.0f / 255.0f)) && (q.T[k] >= 0.001f);
+    const float w = valid ? al * q.T[k] : 0.0f;
+    q.c[k][0] = fmaf(sr, w, q.c[k][0]);
+    q.c[k][1] = fmaf(sg, w, q.c[k][1]);
+    q.c[k][2] = fmaf(sb, w, q.c[k][2]);
+    if (valid) q.T[k] = nT;
+    const float gw = w > 0.01f ? w : 0.0f;
+    q.gd[k] = fmaf(gw, sd, q.gd[k]);
+    q.gw[k] = q.gw[k] + gw;
+    q.m[k][0] = fmaf(mr, gw, q.m[k][0]);
+    q.m[k][1] = fmaf(mm, gw, q.m[k][1]);
+    q.n[k][0] = fmaf(nx, gw, q.n[k][0]);
+    q.n[k][1] = fmaf(ny, gw, q.n[k][1]);
+    q.n[k][2] = fmaf(nz, gw, q.n[k][2]);
+    q.gc[k] = fmaf(sc, gw, q.gc[k]);
+    q.e[k][0] = fmaf(er, w, q.e[k][0]);
+    q.e[k][1] = fmaf(eg, w, q.e[k][1]);
+    q.e[k][2] = fmaf(eb, w, q.e[k][2]);
+  }
+  q.done = q.T[0] < 0.001f && q.T[1] < 0.001f && q.T[2] < 0.001f && q.T[3] < 0.001f;
+}
+
+__device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, uint32_t bx, uint32_t by) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t px = bx + (uint32_t)(k & 1), py = by + (uint32_t)(k >> 1);
+    if (px >= a.W || py >= a.H) continue;
+    const float sw = mx(q.gw[k], 0.0001f);
+    const float cr = fmaf(q.T[k], 0.02f, q.c[k][0]);
+    const float cg = fmaf(q.T[k], 0.02f, q.c[k][1]);
+    const float cb = fmaf(q.T[k], 0.04f, q.c[k][2]);
+    const float ca = 1.0f - q.T[k];
+    char* crow = static_cast<char*>(a.out_color) + (size_t)py * a.color_pitch;
+    if (a.color_f32) {
+      reinterpret_cast<float4*>(crow)[px] = make_float4(cr, cg, cb, ca);
+    } else {
+      reinterpret_cast<uint2*>(crow)[px] = make_uint2(pack2x16(cr, cg), pack2x16(cb, ca));
+    }
+    reinterpret_cast<float*>(reinterpret_cast<char*>(a.out_depth) + (size_t)py * a.depth_pitch)[px] = q.gd[k] / sw;
+    reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(a.out_normal) + (size_t)py * a.normal_pitch)[px] =
+        oct_pack_norm(q.n[k][0], q.n[k][1] + 0.0001f, q.n[k][2]);
+    reinterpret_cast<uint4*>(reinterpret_cast<char*>(a.out_material) + (size_t)py * a.material_pitch)[px] =
+        make_uint4(pack2x16(q.m[k][0] / sw, q.m[k][1] / sw), pack2x16(q.e[k][0], q.e[k][1]),
+                   pack2x16(q.e[k][2], 0.0f), pack2x16(q.gc[k] / sw, 0.0f));
+  }
+}
+
+__global__ void __launch_bounds__(kWarps * 32) k_raster(FrameArgs a) {
+  __shared__ float s_pay[kWarps][kFields][32];
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t tile_idx = blockIdx.x * kWarps + warp;
+  if (tile_idx >= a.tile_count) return;
+  const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
+  const uint32_t t = morton(tx, ty);
+  const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
+  const uint32_t qx = lane & 7u, qy = lane >> 3;
+  const uint32_t bx = tx * 16u + qx * 2u;
+  const uint32_t by0 = ty * 16u + qy * 2u, by1 = by0 + 8u;
+  const float p00x = (float)bx + 0.5f;
+  const float p00y0 = (float)by0 + 0.5f, p00y1 = (float)by1 + 0.5f;
+  Quad q0, q1;
+  quad_init(q0);
+  quad_init(q1);
+  float (*s)[32] = s_pay[warp];
+  for (uint32_t b = 0; b < count; b += 32u) {
+    const uint32_t n = count - b < 32u ? count - b : 32u;
+    if (lane < n) {
+      const uint32_t r = __ldg(a.entries + start + b + lane);
+      const float4 g = __ldg(a.geo + r);
+      const uint4 ap = __ldg(a.app + r);
+      const uint4 gb = __ldg(a.gb + r);
+      const uint2 ax = __ldg(a.aux + r);
+      s[F_CX][lane] = g.x;
+      s[F_CY][lane] = g.y;
+      s[F_KA][lane] = g.z * -0.5f;
+      s[F_KB][lane] = -g.w;
+      s[F_KC][lane] = u2f(ap.x) * -0.5f;
+      s[F_OP][lane] = hi16(ap.y);
+      s[F_R][lane] = lo16(ap.z);
+      s[F_G][lane] = hi16(ap.z);
+      s[F_B][lane] = lo16(ap.w);
+      s[F_D][lane] = u2f(__ldg(a.depth + r));
+      s[F_MR][lane] = lo16(gb.x);
+      s[F_MM][lane] = hi16(gb.x);
+      float nx, ny, nz;
+      oct_decode(lo16(gb.y), hi16(gb.y), nx, ny, nz);
+      s[F_NX][lane] = nx;
+      s[F_NY][lane] = ny;
+      s[F_NZ][lane] = nz;
+      s[F_CF][lane] = lo16(ax.y);
+      s[F_ER][lane] = lo16(gb.z);
+      s[F_EG][lane] = hi16(gb.z);
+      s[F_EB][lane] = lo16(gb.w);
+    }
+    __syncwarp();
+    for (uint32_t i = 0; i < n; ++i) {
+      if (!q0.done) quad_splat(q0, p00x, p00y0, s, (int)i);
+      if (!q1.done) quad_splat(q1, p00x, p00y1, s, (int)i);
+    }
+    __syncwarp();
+    if (__all_sync(0xFFFFFFFFu, q0.done && q1.done)) break;
+  }
+  quad_store(a, q0, bx, by0);
+  quad_store(a, q1, bx, by1);
+}
+
+}  // namespace
+
+cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s) {
+  const uint32_t blocks = (a.tile_count + kWarps - 1) / kWarps;
+  if (blocks) k_raster<<<blocks, kWarps * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace hdsr

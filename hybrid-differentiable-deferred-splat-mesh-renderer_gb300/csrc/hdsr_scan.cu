@@ -1,0 +1,196 @@
+// hdsr_scan.cu — single-pass exclusive scans with decoupled lookback.
+//
+// Replaces the reference's three-pass Hillis-Steele scan (scan,
+// scan_block_sums, add_block_sums in gpu_prefix_sum.wgsl:169-240, driven by
+// gpuTileSplatCompositor.ts:1063-1088) with one launch per array:
+//   - per-splat tile counts (N) -> pair offsets and P, the frame's pair total;
+//   - per-tile counts (M) -> tile offsets (bit-identical to the reference's
+//     tileOffsets), plus per-tile log-depth parameters and the sort segment
+//     list that replaces classify_tiles (gpu_tile_classify.wgsl:44-86).
+// Tiles of 4096 elements are claimed through an atomic counter, so a tile
+// only waits on tiles already claimed by running blocks; every wait is
+// bounded and sets HDSR_DEV_TIMEOUT when it gives up.
+#include "hdsr_internal.cuh"
+
+namespace hdsr {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
+  return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+__device__ __forceinline__ void st_volatile(unsigned long long* p, unsigned long long v) {
+  *reinterpret_cast<volatile unsigned long long*>(p) = v;
+}
+
+// Exclusive prefix of all tiles before `tile`, walking back through their
+// status words (single thread).
+__device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t epoch, uint32_t* ctl) {
+  uint32_t prefix = 0;
+  int t = (int)tile - 1;
+  while (t >= 0) {
+    unsigned long long st;
+    uint32_t spins = 0;
+    for (;;) {
+      st = ld_volatile(status + t);
+      if ((uint32_t)(st >> 34) == (epoch & 0x3FFFFFFFu) && ((st >> 32) & 3ull) != 0ull) break;
+      if (++spins > kSpinLimit) {
+        atomicOr(ctl + kCtlFlags, 0x2u);
+        st = make_status(epoch, kFlagInc, 0u);
+        break;
+      }
+      __nanosleep(64);
+    }
+    prefix += (uint32_t)st;
+    if (((st >> 32) & 3ull) == kFlagInc) break;
+    --t;
+  }
+  return prefix;
+}
+
+struct PairScan {
+  static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
+  static __device__ uint32_t counter() { return kCtlScanNTile; }
+  static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
+  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.ntiles[i]; }
+  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) { a.pair_off[i] = excl; }
+  static __device__ void finish(const FrameArgs& a, uint32_t total) {
+    a.ctl[kCtlPairsLo] = total;
+    a.ctl[kCtlPairsHi] = 0u;
+    if ((uint64_t)total > a.cap) atomicOr(a.ctl + kCtlFlags, 0x1u);
+  }
+};
+
+struct TileScan {
+  static __device__ uint32_t size(const FrameArgs& a) { return a.M; }
+  static __device__ uint32_t counter() { return kCtlScanMTile; }
+  static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_m; }
+  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.tile_cnt[i]; }
+  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) {
+    a.tile_off[i] = excl;
+    const uint32_t c = a.tile_cnt[i];
+    if (c == 0u) return;
+    a.tile_log[i] = tile_log_params(a.tile_dmin[i], a.tile_dmax[i]);
+    if (c < 2u) return;
+    if (c <= kMaxTileEntries) {
+      uint32_t slot = atomicAdd(a.ctl + kCtlSegments, 1u);
+      if (slot < a.seg_cap) a.segments[slot] = make_uint2(excl, c);
+    } else {
+      // hot tile: greedy chunk pack of the bucket-ordered entries yields
+      // consecutive 4096-entry chunks (gpu_tile_bucket_sort.wgsl:276-307)
+      const uint32_t nch = (c + kMaxTileEntries - 1u) / kMaxTileEntries;
+      atomicAdd(a.ctl + kCtlHotTiles, 1u);
+      atomicAdd(a.ctl + kCtlChunks, nch);
+      uint32_t slot = atomicAdd(a.ctl + kCtlSegments, nch);
+      for (uint32_t k = 0; k < nch; ++k) {
+        uint32_t st = k * kMaxTileEntries;
+        uint32_t cnt = c - st < kMaxTileEntries ? c - st : kMaxTileEntries;
+        if (slot + k < a.seg_cap) a.segments[slot + k] = make_uint2(excl + st, cnt);
+      }
+    }
+  }
+  static __device__ void finish(const FrameArgs&, uint32_t) {}
+};
+
+template <class Policy>
+__global__ void __launch_bounds__(kScanThreads) k_scan(FrameArgs a) {
+  constexpr uint32_t PAD = kScanTile / 32;
+  __shared__ uint32_t s_data[kScanTile + PAD];
+  __shared__ uint32_t s_warp[kScanThreads / 32];
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_prefix;
+  const uint32_t n = Policy::size(a);
+  const uint32_t num_tiles = (n + kScanTile - 1) / kScanTile;
+  const uint32_t epoch = a.ctl[kCtlEpoch];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  unsigned long long* status = Policy::status(a);
+  for (;;) {
+    if (tid == 0) s_tile = atomicAdd(a.ctl + Policy::counter(), 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= num_tiles) break;
+    const uint32_t base = tile * kScanTile;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+      uint32_t i = k * kScanThreads + tid;
+      uint32_t g = base + i;
+      s_data[i + i / 32] = g < n ? Policy::load(a, g) : 0u;
+    }
+    __syncthreads();
+    uint32_t vals[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+      uint32_t i = tid * kScanItems + k;
+      vals[k] = s_data[i + i / 32];
+      sum += vals[k];
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += v;
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+      uint32_t wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+        if (lane >= (uint32_t)o) wi += v;
+      }
+      if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+      if (lane == kScanThreads / 32 - 1) {
+        const uint32_t total = wi;
+        if (tile == 0) {
+          st_volatile(status + tile, make_status(epoch, kFlagInc, total));
+          s_prefix = 0u;
+        } else {
+          st_volatile(status + tile, make_status(epoch, kFlagAgg, total));
+          uint32_t prefix = lookback(status, tile, epoch, a.ctl);
+          st_volatile(status + tile, make_status(epoch, kFlagInc, prefix + total));
+          s_prefix = prefix;
+        }
+        if (tile == num_tiles - 1) Policy::finish(a, s_prefix + total);
+      }
+    }
+    __syncthreads();
+    uint32_t running = s_prefix + s_warp[warp] + (inc - sum);
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+      uint32_t i = tid * kScanItems + k;
+      s_data[i + i / 32] = running;
+      running += vals[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+      uint32_t i = k * kScanThreads + tid;
+      uint32_t g = base + i;
+      if (g < n) Policy::store(a, g, s_data[i + i / 32]);
+    }
+    __syncthreads();
+  }
+}
+
+int scan_grid(const FrameArgs& a, uint32_t n) {
+  uint32_t tiles = (n + kScanTile - 1) / kScanTile;
+  uint32_t cap = (uint32_t)a.num_sms * 4u;
+  return (int)(tiles < cap ? (tiles ? tiles : 1u) : cap);
+}
+
+}  // namespace
+
+cudaError_t launch_scan_pairs(const FrameArgs& a, cudaStream_t s) {
+  k_scan<PairScan><<<scan_grid(a, a.N), kScanThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s) {
+  k_scan<TileScan><<<scan_grid(a, a.M), kScanThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace hdsr

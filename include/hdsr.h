@@ -1,0 +1,212 @@
+/*
+ * hdsr.h — C ABI of the GB300 tile-splat compositor.
+ *
+ * Drop-in for the reference's compute compositor operator API
+ * (lyonsno/hybrid-differentiable-deferred-splat-mesh-renderer,
+ * src/gpuTileSplatCompositor.ts). Each entry point names the reference
+ * function it replaces. Plain pointers and sizes only; device pointers are
+ * CUDA device addresses owned by the caller unless stated otherwise; a
+ * "stream" is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *
+ * Error model: every call returns hdsr_status; no C++ exception crosses this
+ * boundary, nothing traps or aborts. Work queued on a stream reports device-
+ * side conditions (pair-capacity overflow, a bounded wait that gave up) in a
+ * status word read by hdsr_query_status(). A handle is externally
+ * synchronised (one host thread at a time); distinct handles are independent.
+ */
+#ifndef HDSR_H
+#define HDSR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HDSR_ABI_VERSION 1
+
+typedef enum hdsr_status {
+  HDSR_OK = 0,
+  HDSR_ERR_INVALID_ARG = 1,
+  HDSR_ERR_OOM = 2,
+  HDSR_ERR_CUDA = 3,
+  HDSR_ERR_OVERFLOW = 4,     /* more (tile, splat) pairs than the handle holds */
+  HDSR_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up           */
+  HDSR_ERR_UNSUPPORTED = 6,
+  HDSR_ERR_NOT_BOUND = 7     /* encode before bind_scene / bind_outputs      */
+} hdsr_status;
+
+/* Device status flags (hdsr_frame_stats.device_flags). */
+#define HDSR_DEV_OVERFLOW   0x1u  /* pairs > pair_capacity: frame skipped       */
+#define HDSR_DEV_TIMEOUT    0x2u  /* a lookback wait exceeded its spin limit    */
+#define HDSR_DEV_BAD_INDEX  0x4u  /* sortedIndices held an id >= splatCount     */
+
+/* planTileSplatCompositor input — gpuTileSplatCompositor.ts:109-116. */
+typedef struct hdsr_plan_input {
+  uint32_t viewport_width;
+  uint32_t viewport_height;
+  uint32_t tile_size_px;          /* the reference always uses 16; only 16 is supported */
+  uint32_t splat_count;
+  double tile_entry_multiplier;   /* <= 0 selects the reference default, 16 */
+} hdsr_plan_input;
+
+/* TileSplatCompositorPlan — gpuTileSplatCompositor.ts:39-49. */
+typedef struct hdsr_plan {
+  uint32_t viewport_width;
+  uint32_t viewport_height;
+  uint32_t tile_size_px;
+  uint32_t tile_columns;
+  uint32_t tile_rows;
+  uint32_t tile_count;
+  uint32_t morton_tile_count;     /* M = morton(cols-1, rows-1) + 1 */
+  uint32_t splat_count;
+  uint32_t max_total_tile_refs;   /* reference budget min(ceil(N*mult), 65535*256) */
+} hdsr_plan;
+
+#define HDSR_COLOR_RGBA16F 0u     /* reference output texture format */
+#define HDSR_COLOR_RGBA32F 1u
+
+#define HDSR_CFG_KEEP_SORTED_KEYS 0x1u  /* keep the radix output keys for readback */
+#define HDSR_CFG_NO_GRAPH         0x2u  /* launch kernels directly, no CUDA graph  */
+
+/* Options of createTileSplatCompositor — gpuTileSplatCompositor.ts:141-145
+ * ({f16?}); the f16 composite variant is not rebuilt (FP32 transmittance). */
+typedef struct hdsr_config {
+  uint64_t pair_capacity;         /* (tile, splat) pairs held; 0 = max(budget, ceil(N*16)) */
+  uint32_t color_format;          /* HDSR_COLOR_* */
+  uint32_t flags;                 /* HDSR_CFG_* */
+} hdsr_config;
+
+/* Splat buffers of createTileSplatBindGroups — gpuTileSplatCompositor.ts:
+ * 792-803 and the upload layout of src/splats.ts:376-500. Device pointers,
+ * borrowed: the handle never frees them. */
+typedef struct hdsr_scene_views {
+  uint32_t splat_count;
+  uint32_t sh_degree;             /* 0..3 */
+  const float* positions;         /* N*3 */
+  const float* scales;            /* N*3 log scales */
+  const float* rotations;         /* N*4 wxyz */
+  const float* opacities;         /* N activated opacities in [0,1] */
+  const uint32_t* material;       /* N pack2x16float(roughness, metalness) */
+  const float* normals;           /* NULL (covariance normals), N*3 or N*6 floats */
+  uint64_t normals_len;           /* float count of normals */
+  const float* sh_data;           /* N*(6+3K): dc3 | sh 3K | emissive3, K=(d+1)^2-1 */
+  const uint32_t* sorted_indices; /* N back-to-front splat ids (gpuSortPrototype) */
+} hdsr_scene_views;
+
+/* Output textures of createTileSplatBindGroups, as headless device buffers.
+ * Pitches are bytes per row. */
+typedef struct hdsr_output_views {
+  void* color;        uint64_t color_pitch;     /* rgba16f (8 B/px) or rgba32f (16 B/px) */
+  float* depth;       uint64_t depth_pitch;     /* r32f */
+  uint32_t* normal;   uint64_t normal_pitch;    /* r32u: pack2x16float(oct normal) */
+  uint32_t* material; uint64_t material_pitch;  /* rgba32u */
+} hdsr_output_views;
+
+typedef struct hdsr_frame_stats {
+  uint64_t total_pairs;           /* P of the last encoded frame */
+  uint64_t pair_capacity;
+  uint32_t visible_splats;
+  uint32_t segments;              /* per-tile / per-chunk sort segments */
+  uint32_t hot_tiles;             /* tiles with > 4096 entries */
+  uint32_t chunks;                /* 4096-entry chunks of hot tiles */
+  uint32_t device_flags;          /* HDSR_DEV_* */
+  uint32_t _reserved;
+} hdsr_frame_stats;
+
+typedef struct hdsr_compositor hdsr_compositor;
+
+/* ABI version of the loaded library. */
+uint32_t hdsr_abi_version(void);
+
+/* planTileSplatCompositor — gpuTileSplatCompositor.ts:109-139. Pure. */
+hdsr_status hdsr_plan_tile_splat_compositor(const hdsr_plan_input* in, hdsr_plan* out);
+
+/* createTileSplatCompositor — gpuTileSplatCompositor.ts:141-728. Allocates
+ * every internal device buffer on the current CUDA device. */
+hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_config* cfg,
+                                              hdsr_compositor** out);
+
+/* resources.destroy() — gpuTileSplatCompositor.ts:710-727. NULL is a no-op. */
+void hdsr_destroy_tile_splat_compositor(hdsr_compositor* h);
+
+/* createTileSplatBindGroups, splat half — gpuTileSplatCompositor.ts:792-995. */
+hdsr_status hdsr_bind_scene(hdsr_compositor* h, const hdsr_scene_views* scene);
+
+/* createTileSplatBindGroups, output half (outputTexture, gbufferTextures). */
+hdsr_status hdsr_bind_outputs(hdsr_compositor* h, const hdsr_output_views* out);
+
+/* writeTileSplatFrameUniforms — gpuTileSplatCompositor.ts:730-774. Pure
+ * host; same 64-float layout. cameraPos (3), viewMatrix (16), projMatrix (16)
+ * may be NULL (left untouched, as in the reference); normalMatrix (9, column
+ * major) NULL = identity. */
+void hdsr_write_tile_splat_frame_uniforms(float target[64], const float view_proj[16],
+                                          const hdsr_plan* plan, float splat_scale,
+                                          uint32_t sh_degree, const float* camera_pos,
+                                          const float* view_matrix, const float* proj_matrix,
+                                          const float* normal_matrix);
+
+/* device.queue.writeBuffer(frameUniformBuffer, ...) — splatRenderer.ts:
+ * 1029-1030. The block is copied into the handle; the next encode uploads it
+ * on its stream. */
+hdsr_status hdsr_set_frame_uniforms(hdsr_compositor* h, const float uniforms[64]);
+
+/* encodeFullComputeCompositorPipeline — gpuTileSplatCompositor.ts:
+ * 1023-1179. Queues the whole frame (project, count, scans, key emission,
+ * radix sort, per-tile sort + hot-tile cascade, rasteriser) on `stream`.
+ * Returns launch errors; device-side conditions go to hdsr_query_status. */
+hdsr_status hdsr_encode_full(hdsr_compositor* h, void* stream);
+
+/* encodeCompositeOnly — gpuTileSplatCompositor.ts:1001-1014. Rasterises the
+ * entries sorted by the last encode_full again (same camera). */
+hdsr_status hdsr_encode_composite_only(hdsr_compositor* h, void* stream);
+
+/* Synchronises the stream of the last encode and reports its frame. Returns
+ * HDSR_ERR_OVERFLOW / HDSR_ERR_TIMEOUT when the device flagged one. */
+hdsr_status hdsr_query_status(hdsr_compositor* h, hdsr_frame_stats* stats);
+
+/* Last error message of this handle (static storage, never NULL). */
+const char* hdsr_last_error(const hdsr_compositor* h);
+
+/* Internal buffers, for parity tests and zero-copy consumers. */
+typedef enum hdsr_buffer_id {
+  HDSR_BUF_CACHE_GEO = 0,     /* float4[N]: centerPx.xy, invCov.xy (reference words 0-3) */
+  HDSR_BUF_CACHE_APP = 1,     /* uint4[N]: invCov.z, f16(radius,opacity), f16 rgb (words 4,6,9,10) */
+  HDSR_BUF_CACHE_GB = 2,      /* uint4[N]: material, oct normal, f16 emissive (words 5,8,11,12) */
+  HDSR_BUF_CACHE_AUX = 3,     /* uint2[N]: tile box u8x4, f16 normal confidence (words 7,13) */
+  HDSR_BUF_DEPTH = 4,         /* u32[N]: f32 NDC depth bits */
+  HDSR_BUF_TILE_COUNTS = 5,   /* u32[M] */
+  HDSR_BUF_TILE_OFFSETS = 6,  /* u32[M] exclusive prefix of tile counts */
+  HDSR_BUF_TILE_ENTRIES = 7,  /* u32[P] sortRank per entry, final per-tile order */
+  HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] radix output: tile<<(20+R) | k20<<R | sortRank */
+  HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat tile counts */
+  HDSR_BUF_SEGMENTS = 10      /* uint2[S] (start, count) sort segments, unordered */
+} hdsr_buffer_id;
+
+/* Device address and byte size of an internal buffer (valid until destroy). */
+hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** device_ptr,
+                            uint64_t* bytes);
+
+/* Number of low key bits that hold the sortRank in HDSR_BUF_SORTED_KEYS. */
+uint32_t hdsr_rank_bits(const hdsr_compositor* h);
+
+/* Per-pass timing of the next encodes: CUDA events recorded on the encode
+ * stream between passes (the reference times only its present pass with
+ * timestamp queries, src/timestamps.ts:10-76). */
+hdsr_status hdsr_set_profiling(hdsr_compositor* h, int enable);
+
+/* Durations (ms) of the passes of the last profiled encode, with their pass
+ * ids (see hdsr_pass_name). Synchronises on the last event. */
+hdsr_status hdsr_pass_times(hdsr_compositor* h, float* ms, uint32_t* ids, uint32_t max, uint32_t* count);
+
+/* Name of a profiled pass id ("project", "radix_pass_0", "raster", ...). */
+const char* hdsr_pass_name(uint32_t id);
+
+/* Number of kernels this handle has queued since creation. */
+uint64_t hdsr_launch_count(const hdsr_compositor* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HDSR_H */

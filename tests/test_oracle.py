@@ -1,0 +1,305 @@
+"""The oracle, pinned: the reference's own known-answer vectors, the
+arithmetic it defines, and the frame-level invariants of the canonical order."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "reference_kats.json").read_text())
+
+
+# --- splatSort.ts known answers (tests/cpuDepthSort.test.ts) ---------------
+
+@pytest.mark.parametrize("case", GOLDEN["cpu_depth_sort"], ids=lambda c: c["name"])
+@pytest.mark.parametrize("threads", [1, 4])
+def test_cpu_depth_sort_known_answers(orc, case, threads):
+    order = orc.sort_back_to_front(case["positions"], case["view"], threads=threads)
+    assert order.tolist() == case["order"]
+
+
+@pytest.mark.parametrize("case", GOLDEN["cpu_depth_sort"], ids=lambda c: c["name"])
+def test_gpu_sort_prototype_order_matches_known_answers(orc, pkg, case):
+    """sortedIndices producer (gpuSortPrototype) gives the same order on the
+    reference's cases, in the oracle and in the host-side numpy form."""
+    assert orc.gpu_sort_prototype_order(case["positions"], case["view"]).tolist() == case["order"]
+    assert pkg.splats.back_to_front_order(case["positions"], case["view"]).tolist() == case["order"]
+
+
+def test_view_space_depth_known_answers():
+    case = next(c for c in GOLDEN["cpu_depth_sort"] if c["name"] == "translated_view")
+    p = np.array(case["positions"], np.float64).reshape(-1, 3)
+    v = np.array(case["view"], np.float64)
+    z = v[2] * p[:, 0] + v[6] * p[:, 1] + v[10] * p[:, 2] + v[14]
+    assert z.tolist() == case["depths"]
+
+
+@pytest.mark.parametrize("case", GOLDEN["cpu_depth_sort_errors"], ids=lambda c: c["message"][:20])
+def test_cpu_depth_sort_rejects_malformed_input(orc, case):
+    with pytest.raises(ValueError, match=case["message"]):
+        orc.sort_back_to_front(case["positions"], case["view"])
+
+
+def test_cpu_depth_sort_rejects_non_finite(orc):
+    with pytest.raises(ValueError, match="non-finite"):
+        orc.sort_back_to_front([0, 0, np.inf], np.eye(4, dtype=np.float32).reshape(-1))
+
+
+def test_cpu_depth_sort_parallel_equals_serial(orc):
+    rng = np.random.default_rng(3)
+    pos = rng.integers(-50, 50, (20000, 3)).astype(np.float32)  # many exact ties
+    view = np.eye(4, dtype=np.float32).reshape(-1)
+    a = orc.sort_back_to_front(pos, view, threads=1)
+    b = orc.sort_back_to_front(pos, view, threads=8)
+    assert np.array_equal(a, b)
+    z = pos[:, 2].astype(np.float64)
+    assert np.array_equal(a, np.lexsort((np.arange(len(z)), z)))
+
+
+# --- compositor constants (computeCompositorLifecycle.test.mjs) -----------
+
+def test_plan_budget_cap(orc):
+    c = GOLDEN["compositor_constants"]
+    assert orc.plan(1920, 1080, 16, 2_000_000)[8] == c["max_dispatch_safe_refs"]
+    assert orc.plan(1920, 1080, 16, 760_000)[8] == 760_000 * 16
+    p = orc.plan(1920, 1080, 16, 1)
+    assert p[3:7].tolist() == [120, 68, 8160, 13600]
+    assert orc.plan(3840, 2160, 16, 1)[6] == 54398
+    assert orc.plan(800, 600, 16, 1)[6] == 3364
+
+
+def _one_splat_scene(pkg, pos, log_scale, opacity=0.8, color=(1.0, 0.5, 0.25)):
+    scene = pkg.splats.SplatAttributes(
+        positions=np.array([pos], np.float32), scales=np.array([[log_scale] * 3], np.float32),
+        rotations=np.array([[1, 0, 0, 0]], np.float32), opacities=np.array([opacity], np.float32),
+        colors=np.array([color], np.float32))
+    return scene
+
+
+def _uniforms(pkg, W, H, N, cam, sh_degree=0):
+    fr = cam.frame(W, H)
+    import ctypes  # noqa: F401
+
+    plan = _plan(pkg, W, H, N)
+    return pkg.write_tile_splat_frame_uniforms(None, fr["view_proj"], plan, 1.0, sh_degree, fr["camera_pos"],
+                                               fr["view"], fr["proj"]), fr
+
+
+def _plan(pkg, W, H, N):
+    return pkg.plan_tile_splat_compositor(W, H, 16, N)
+
+
+def test_footprint_clamped_to_eight_tiles(orc, pkg, hdsr_lib):
+    clamp = GOLDEN["compositor_constants"]["footprint_clamp_tiles"]
+    scene = _one_splat_scene(pkg, (0.0, 0.0, 0.0), 2.0)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    u, _ = _uniforms(pkg, 1024, 1024, 1, pkg.camera.look_from((0, 0, 5)))
+    fr = orc.render_frame(u, packed, np.zeros(1, np.uint32), composite=False)
+    box = int(fr["proj_cache"][0, 7])
+    x0, y0, x1, y1 = box & 255, (box >> 8) & 255, (box >> 16) & 255, box >> 24
+    assert x1 - x0 + 1 == 2 * clamp + 1 and y1 - y0 + 1 == 2 * clamp + 1
+    assert fr["proj_cache"].shape[1] == GOLDEN["compositor_constants"]["proj_stride_u32"]
+
+
+# --- arithmetic the canonical frame is defined with ------------------------
+
+def test_exp_accuracy(orc):
+    x = np.concatenate([np.linspace(-103.0, 88.0, 200001), np.linspace(-4.0, 0.0, 100001),
+                        np.random.default_rng(0).normal(-3, 2, 100000)]).astype(np.float32)
+    got = orc.expf(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    normal = ref > 1.2e-38
+    rel = np.abs(got[normal] - ref[normal]) / ref[normal]
+    assert rel.max() < 3.0e-7  # within ~2.5 ulp
+    assert orc.expf([np.float32(-104.0)])[0] == 0.0
+    assert np.isinf(orc.expf([np.float32(89.0)])[0])
+    assert orc.expf([0.0])[0] == 1.0
+
+
+def test_log_accuracy(orc):
+    x = np.concatenate([np.geomspace(1e-30, 1e30, 200001), np.linspace(0.5, 2.0, 100001),
+                        np.array([1e-6, 1.0, 2.0, 0.5], np.float64)]).astype(np.float32)
+    got = orc.logf(x).astype(np.float64)
+    ref = np.log(x.astype(np.float64))
+    err = np.abs(got - ref)
+    tol = np.maximum(np.abs(ref), 1e-30) * 2.5e-7 + 1e-9
+    assert np.all(err <= tol)
+    assert orc.logf([1.0])[0] == 0.0
+    assert np.isneginf(orc.logf([0.0])[0])
+
+
+def test_f16_round_to_nearest_even_matches_ieee(orc):
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.normal(0, 1, 200000), rng.normal(0, 1e-5, 50000), rng.uniform(-70000, 70000, 50000),
+                        [0.0, -0.0, 65504.0, 65519.0, 65520.0, 1e-8, 6.0e-8, 2.0 ** -24, 2.0 ** -25,
+                         3 * 2.0 ** -26, np.inf, -np.inf]]).astype(np.float32)
+    got = orc.f16_rne(x)
+    with np.errstate(over="ignore"):
+        ref = x.astype(np.float16).view(np.uint16)
+    assert np.array_equal(got, ref)
+    assert orc.f16_rne([np.nan])[0] == 0x7E00
+    h = np.arange(65536, dtype=np.uint16)
+    finite = (h & 0x7C00) != 0x7C00
+    assert np.array_equal(orc.f16_to_f32(h)[finite], h.view(np.float16).astype(np.float32)[finite])
+
+
+def test_f16_truncation_of_host_packer(orc, pkg):
+    """f32ToF16 (splats.ts:431-442): restated in C and in numpy, same bits."""
+    rng = np.random.default_rng(2)
+    x = np.concatenate([rng.normal(0, 1, 100000), rng.uniform(-1e6, 1e6, 1000),
+                        [0.75, 0.0, 1.0, 6.1e-5, 6.0e-5, 65504.0, 70000.0]]).astype(np.float32)
+    assert np.array_equal(orc.f16_trunc(x), pkg.splats.f32_to_f16_trunc(x))
+    # truncation, not rounding: 0.75 is exact, 1/3 truncates below RNE
+    assert pkg.splats.f32_to_f16_trunc([0.75])[0] == 0x3A00
+    assert pkg.splats.f32_to_f16_trunc([1.0 / 3.0])[0] == 0x3555
+    assert pkg.splats.pack_material_buffer(1)[0] == 0x3A00
+
+
+def test_morton_interleave(orc):
+    x = np.arange(256, dtype=np.uint32).repeat(256)
+    y = np.tile(np.arange(256, dtype=np.uint32), 256)
+    ref = np.zeros_like(x)
+    for b in range(8):
+        ref |= ((x >> b) & 1) << (2 * b)
+        ref |= ((y >> b) & 1) << (2 * b + 1)
+    assert np.array_equal(orc.morton(x, y), ref)
+
+
+def test_bucket_is_top_bits_of_key20(orc):
+    """The 128 log buckets of the hot-tile cascade are k20 >> 13, so sorting
+    by the 20-bit key refines the bucket order."""
+    rng = np.random.default_rng(5)
+    for _ in range(200):
+        d = rng.uniform(0.0, 1.0, 4000).astype(np.float32)
+        d[rng.integers(0, 4000, 40)] = rng.uniform(-0.01, 0.0, 40).astype(np.float32)
+        bits = d.view(np.uint32)
+        b, k = orc.bucket_key20(bits, int(bits.min()), int(bits.max()))
+        assert np.array_equal(b, k >> 13)
+    b, k = orc.bucket_key20(np.full(10, 0x3F000000, np.uint32), 0x3F000000, 0x3F000000)
+    assert not b.any() and not k.any()
+
+
+# --- frame invariants of the canonical order -------------------------------
+
+@pytest.fixture(scope="module")
+def small_frame(orc, pkg, hdsr_lib):
+    scene = pkg.workloads.plain_scene(6000, seed=4)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    cam = pkg.camera.look_from((0.5, 0.2, 4.5))
+    u, fr = _uniforms(pkg, 320, 240, scene.count, cam)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    return dict(u=u, packed=packed, order=order, frame=orc.render_frame(u, packed, order, threads=4))
+
+
+def test_counts_offsets_entries_consistent(small_frame, orc):
+    f = small_frame["frame"]
+    assert f["tile_counts"].sum() == f["total_pairs"]
+    assert np.array_equal(f["tile_offsets"], np.concatenate([[0], np.cumsum(f["tile_counts"])[:-1]]))
+    depth = f["depth"]
+    for t in np.nonzero(f["tile_counts"])[0]:
+        e = f["tile_entries"][f["tile_offsets"][t]: f["tile_offsets"][t] + f["tile_counts"][t]]
+        key = depth[e].astype(np.uint64) << np.uint64(32) | e.astype(np.uint64)
+        if f["tile_counts"][t] <= 4096:
+            assert np.all(key[1:] > key[:-1])
+
+
+def test_keys20_order_matches_frame_tiles(small_frame, orc):
+    f = small_frame["frame"]
+    keys, vals = orc.sorted_keys20(small_frame["u"], f["proj_cache"], f["depth"])
+    assert len(keys) == f["total_pairs"]
+    assert np.all(keys[1:] >= keys[:-1])
+    tiles = (keys >> np.uint64(20)).astype(np.int64)
+    assert np.array_equal(np.bincount(tiles, minlength=f["M"])[: f["M"]], f["tile_counts"])
+    # same multiset of entries per tile as the canonical frame
+    for t in np.nonzero(f["tile_counts"])[0][:50]:
+        a = np.sort(vals[tiles == t])
+        b = np.sort(f["tile_entries"][f["tile_offsets"][t]: f["tile_offsets"][t] + f["tile_counts"][t]])
+        assert np.array_equal(a, b)
+
+
+def test_composite_close_to_fp64(small_frame, orc):
+    f = small_frame["frame"]
+    img = orc.f16_to_f32(f["color"].reshape(-1)).reshape(f["H"], f["W"], 4).astype(np.float64)
+    ref = orc.render_frame_f64(small_frame["u"], small_frame["packed"], small_frame["order"], f, threads=4)
+    err = np.abs(img - ref)
+    assert err.mean() < 2e-3
+    mse = np.mean((img[..., :3] - ref[..., :3]) ** 2)
+    assert 10 * np.log10(1.0 / max(mse, 1e-20)) > 40.0
+
+
+def test_oracle_deterministic_across_threads(pkg, orc, small_frame):
+    a = orc.render_frame(small_frame["u"], small_frame["packed"], small_frame["order"], threads=1)
+    b = small_frame["frame"]
+    for k in ("proj_cache", "depth", "tile_counts", "tile_offsets", "tile_entries", "color", "material"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def _stack_scene(pkg, n, pos=(0.0, 0.0, 0.0), log_scale=-6.0, depth_jitter=0.0, seed=0):
+    rng = np.random.default_rng(seed)
+    p = np.tile(np.array(pos, np.float32), (n, 1))
+    p[:, 2] += rng.uniform(-depth_jitter, depth_jitter, n).astype(np.float32)
+    return pkg.splats.SplatAttributes(
+        positions=p, scales=np.full((n, 3), log_scale, np.float32),
+        rotations=np.tile(np.array([1, 0, 0, 0], np.float32), (n, 1)),
+        opacities=np.full(n, 0.5, np.float32), colors=rng.uniform(0, 1, (n, 3)).astype(np.float32))
+
+
+@pytest.mark.parametrize("n,hot", [(4096, 0), (4097, 1), (9000, 1)])
+def test_hot_tile_threshold_and_chunks(orc, pkg, hdsr_lib, n, hot):
+    """A tile with exactly 4096 entries stays small; 4097 makes it hot and
+    splits it into 4096-entry chunks in bucket order."""
+    scene = _stack_scene(pkg, n, pos=(0.72, -0.72, 0.0), depth_jitter=0.5, seed=n)  # tile (2, 2)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    cam = pkg.camera.look_from((0, 0, 5))
+    u, fr = _uniforms(pkg, 64, 64, n, cam)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order, composite=False)
+    assert f["hot_tiles"] == hot
+    busiest = int(np.argmax(f["tile_counts"]))
+    assert f["tile_counts"][busiest] == n
+    if hot:
+        assert f["total_chunks"] == (n + 4095) // 4096
+        sizes = f["chunk_ranges"][:, 1].tolist()
+        assert sizes[:-1] == [4096] * (len(sizes) - 1)
+        assert not (f["flags"] & orc.FLAG_BUCKET_KEY_MISMATCH)
+        # chunks are in bucket (k20) order: every entry of chunk c has k20
+        # <= every entry of chunk c+1
+        keys, vals = orc.sorted_keys20(u, f["proj_cache"], f["depth"])
+        tile_keys = keys[(keys >> np.uint64(20)) == busiest] & np.uint64(0xFFFFF)
+        k_of = dict(zip(vals[(keys >> np.uint64(20)) == busiest].tolist(), tile_keys.tolist()))
+        start = f["tile_offsets"][busiest]
+        for c in range(len(sizes) - 1):
+            a = f["tile_entries"][start + 4096 * c: start + 4096 * (c + 1)]
+            b = f["tile_entries"][start + 4096 * (c + 1): start + 4096 * (c + 2)]
+            assert max(k_of[x] for x in a.tolist()) <= min(k_of[x] for x in b.tolist())
+
+
+def test_equal_depth_ties_break_by_sort_rank(orc, pkg, hdsr_lib):
+    scene = _stack_scene(pkg, 300, pos=(0.72, -0.72, 0.0), depth_jitter=0.0)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    u, fr = _uniforms(pkg, 64, 64, 300, pkg.camera.look_from((0, 0, 5)))
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order, composite=False)
+    t = int(np.argmax(f["tile_counts"]))
+    e = f["tile_entries"][f["tile_offsets"][t]: f["tile_offsets"][t] + f["tile_counts"][t]]
+    assert np.array_equal(e, np.arange(300))
+
+
+def test_two_overlapping_splats_front_to_back(orc, pkg, hdsr_lib):
+    """Hand-computed front-to-back blend at a splat centre pixel."""
+    scene = pkg.splats.SplatAttributes(
+        positions=np.array([[0, 0, 0], [0, 0, -1.0]], np.float32),
+        scales=np.full((2, 3), -1.0, np.float32), rotations=np.array([[1, 0, 0, 0]] * 2, np.float32),
+        opacities=np.array([0.5, 0.9], np.float32), colors=np.array([[1, 0, 0], [0, 0, 1]], np.float32))
+    packed = pkg.splats.pack_splat_attributes(scene)
+    u, fr = _uniforms(pkg, 64, 64, 2, pkg.camera.look_from((0, 0, 5)))
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order)
+    img = orc.f16_to_f32(f["color"].reshape(-1)).reshape(64, 64, 4)
+    # near splat (red, the one at z=0) is first after the per-tile depth sort
+    a0 = orc.f16_to_f32(np.array([f["proj_cache"][order.tolist().index(0), 6] >> 16], np.uint16))[0]
+    a1 = orc.f16_to_f32(np.array([f["proj_cache"][order.tolist().index(1), 6] >> 16], np.uint16))[0]
+    px = img[31, 31]
+    # pixel (31,31) centre is 0.5 px from the projected centre (32,32) in x and y
+    assert px[0] > px[2] > 0
+    assert abs((1 - px[3]) - (1 - a0 * np.exp(-0.5 * 0)) * (1 - a1)) < 0.2
