@@ -202,7 +202,7 @@ def run_ours(args, rank, world, local):
     value = args.steps * world / total_s
 
     # end to end through the C ABI with host buffers
-    e2e = run_e2e(pkg, F, args, stream, world, dev)
+    e2e = None if args.no_e2e else run_e2e(pkg, F, args, stream, world, dev)
 
     # roofline of the dominant HBM-bound pass
     sh_floats = 6 + 3 * ((wl.scene.sh_degree + 1) ** 2 - 1)
@@ -362,6 +362,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hot760k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiler runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -120,6 +120,12 @@ def hot760k() -> Workload:
     return Workload("hot760k_1920x1080", hot_scene(760_000, 2), 1920, 1080, [OrbitCamera(**HOT760K_CAMERA)])
 
 
+def hot190k() -> Workload:
+    """A quarter of the hot-tile workload (same distribution and camera), for
+    profiler captures that must stay small (about 10M pairs)."""
+    return Workload("hot190k_1920x1080", hot_scene(190_000, 2), 1920, 1080, [OrbitCamera(**HOT760K_CAMERA)])
+
+
 def orbit_cameras(count: int, radius: float, elevation: float = 0.25) -> list:
     return [OrbitCamera(azimuth=2.0 * math.pi * i / count, elevation=elevation, distance=radius)
             for i in range(count)]
@@ -140,4 +146,5 @@ def hot_camera_candidates(seed: int = 7, count: int = 64) -> list:
                         distance=float(rng.uniform(2.5, 8.0))) for _ in range(count)]
 
 
-WORKLOADS = {"plain50k": plain50k, "hot760k": hot760k, "sh3_3m": sh3_3m, "train500k": train500k}
+WORKLOADS = {"plain50k": plain50k, "hot760k": hot760k, "hot190k": hot190k, "sh3_3m": sh3_3m,
+             "train500k": train500k}
