@@ -180,6 +180,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.entries, cap, "tile_entries");
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
   ALLOC(a.segments, a.seg_cap, "segments");
+  ALLOC(a.dirty, a.seg_cap, "dirty_segments");
   ALLOC(a.digit_hist, (uint64_t)kMaxPasses * 256, "digit_hist");
   ALLOC(a.radix_status, (uint64_t)a.passes * a.radix_tiles_cap * 256, "radix_status");
   ALLOC(a.scan_status_n, scan_tiles_n, "scan_status_n");
@@ -361,7 +362,7 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
     }
     if ((e = launch_segment_sort(a, s)) != cudaSuccess) return cuda_fail(h, e, "segment_sort");
     mark(h, s, 16);
-    h->launches += 1 + 3 * n_splat_launch + 2 + 2 + a.passes + 1;
+    h->launches += 1 + 3 * n_splat_launch + 2 + 2 + a.passes + 2;
   }
   if ((e = launch_raster(a, s)) != cudaSuccess) return cuda_fail(h, e, "raster");
   mark(h, s, 17);

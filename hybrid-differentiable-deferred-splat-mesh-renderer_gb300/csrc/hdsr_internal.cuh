@@ -23,6 +23,7 @@ enum Ctl : int {
   kCtlRadixTile = 10,  // .. 10 + kMaxPasses - 1
   kCtlSegTile = 18,
   kCtlRasterTile = 19,
+  kCtlDirty = 20,      // segments the check pass found out of order
   kCtlWords = 64
 };
 constexpr int kMaxPasses = 8;
@@ -68,6 +69,7 @@ struct FrameArgs {
   unsigned long long* sorted_keys;  // optional copy of the radix output
   uint32_t* entries;              // final per-tile order (sortRank)
   uint2* segments;                // (start, count)
+  uint32_t* dirty;                // indices of segments that need the full sort
   uint32_t seg_cap;
   // radix
   uint32_t* digit_hist;           // kMaxPasses * 256 counts, then exclusive bases
@@ -108,7 +110,7 @@ cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_emit(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_radix_hist(const FrameArgs& a, cudaStream_t s);    // 2 launches
 cudaError_t launch_radix_pass(const FrameArgs& a, cudaStream_t s, uint32_t pass);
-cudaError_t launch_segment_sort(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_segment_sort(const FrameArgs& a, cudaStream_t s);  // 2 launches
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 
 // sizing helpers shared with the API

@@ -250,31 +250,36 @@ __global__ void __launch_bounds__(256) k_project(FrameArgs a) {
   a.ntiles[r] = (t1x - t0x + 1u) * (t1y - t0y + 1u);
 }
 
-// count_tile_refs + per-tile depth min/max. One thread per sortRank; splats
-// above the reference's large-splat threshold (16 tiles) are spread over the
-// warp so one lane does not serialise up to 17x17 tiles.
-__global__ void __launch_bounds__(256) k_count(FrameArgs a) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+// count_tile_refs + per-tile depth min/max. Splats above the reference's
+// large-splat threshold (16 tiles) are spread over the warp so one lane does
+// not serialise up to 17x17 tiles. Templated on the table the atomics go to:
+// global memory, or a per-block copy in shared memory (privatised tables,
+// flushed once per block) when the M-tile tables fit there.
+struct GlobalTables {
+  uint32_t *cnt, *dmin, *dmax;
+  __device__ void add(uint32_t t, uint32_t d) const {
+    atomicAdd(cnt + t, 1u);
+    atomicMin(dmin + t, d);
+    atomicMax(dmax + t, d);
+  }
+};
+
+template <class Tables>
+__device__ __forceinline__ void count_splats(const FrameArgs& a, const Tables& tb, uint32_t r) {
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t box = kSentinel, d = 0u, n = 0u;
   if (r < a.N) {
     box = a.aux[r].x;
     if (box != kSentinel) { d = a.depth[r]; n = a.ntiles[r]; }
   }
-  const bool small = box != kSentinel && n <= kLargeSplatTiles;
-  if (small) {
+  if (box != kSentinel && n <= kLargeSplatTiles) {
     uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
     for (uint32_t ty = y0; ty <= y1; ++ty)
       for (uint32_t tx = x0; tx <= x1; ++tx) {
         uint32_t t = morton(tx, ty);
-        if (t < a.M) {
-          atomicAdd(a.tile_cnt + t, 1u);
-          atomicMin(a.tile_dmin + t, d);
-          atomicMax(a.tile_dmax + t, d);
-        }
+        if (t < a.M) tb.add(t, d);
       }
   }
-  // cooperative pass over the warp's large splats
   uint32_t large = __ballot_sync(0xFFFFFFFFu, box != kSentinel && n > kLargeSplatTiles);
   while (large) {
     const int src = __ffs(large) - 1;
@@ -286,11 +291,36 @@ __global__ void __launch_bounds__(256) k_count(FrameArgs a) {
     const uint32_t spanX = x1 - x0 + 1u;
     for (uint32_t i = lane; i < ln; i += 32u) {
       uint32_t t = morton(x0 + i % spanX, y0 + i / spanX);
-      if (t < a.M) {
-        atomicAdd(a.tile_cnt + t, 1u);
-        atomicMin(a.tile_dmin + t, ld);
-        atomicMax(a.tile_dmax + t, ld);
-      }
+      if (t < a.M) tb.add(t, ld);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_count(FrameArgs a) {
+  count_splats(a, GlobalTables{a.tile_cnt, a.tile_dmin, a.tile_dmax}, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+constexpr uint32_t kCountSmemThreads = 1024;
+
+__global__ void __launch_bounds__(kCountSmemThreads, 1) k_count_smem(FrameArgs a) {
+  extern __shared__ uint32_t s_tab[];
+  const uint32_t M = a.M;
+  GlobalTables tb{s_tab, s_tab + M, s_tab + 2 * M};
+  for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
+    tb.cnt[i] = 0u;
+    tb.dmin[i] = 0xFFFFFFFFu;
+    tb.dmax[i] = 0u;
+  }
+  __syncthreads();
+  for (uint32_t base = blockIdx.x * blockDim.x; base < a.N; base += gridDim.x * blockDim.x)
+    count_splats(a, tb, base + threadIdx.x);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
+    const uint32_t c = tb.cnt[i];
+    if (c) {
+      atomicAdd(a.tile_cnt + i, c);
+      atomicMin(a.tile_dmin + i, tb.dmin[i]);
+      atomicMax(a.tile_dmax + i, tb.dmax[i]);
     }
   }
 }
@@ -355,8 +385,24 @@ cudaError_t launch_project(const FrameArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Largest M whose three privatised u32 tables fit one block's shared memory.
+uint32_t count_smem_max_tiles() { return (200u * 1024u) / 12u; }
+
 cudaError_t launch_count(const FrameArgs& a, cudaStream_t s) {
-  if (a.N) k_count<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  if (!a.N) return cudaSuccess;
+  if (a.M <= count_smem_max_tiles()) {
+    const size_t smem = (size_t)a.M * 12u;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(k_count_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(count_smem_max_tiles() * 12u));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    k_count_smem<<<a.num_sms, kCountSmemThreads, smem, s>>>(a);
+  } else {
+    k_count<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
