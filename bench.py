@@ -142,14 +142,12 @@ def pass_bytes(name: str, N: int, P: int, px: int, sh_floats: int) -> float | No
         return N * (8 + 4 + 4)
     if name == "scan_pairs":
         return N * 8
+    if name == "depth_sort":
+        return 4 * (N * 8 + N * 16)  # 4 passes: upsweep read + downsweep read/write
     if name == "emit_keys":
         return N * 20 + P * 8
-    if name == "radix_hist":
-        return P * 8
-    if name.startswith("radix_pass"):
-        return P * 16
-    if name == "segment_sort":
-        return P * 12
+    if name.startswith("tile_sort"):
+        return P * 8 + P * 16  # upsweep read + downsweep read/write (last pass writes 4 B)
     return None
 
 
@@ -227,7 +225,7 @@ def run_ours(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {**wl.describe(), "pairs": P, "hot_tiles": int(st["hot_tiles"]), "chunks": int(st["chunks"]),
-                   "segments": int(st["segments"]), "l2": "256 MiB flush between timed steps",
+                   "l2": "256 MiB flush between timed steps",
                    "parallelism": f"replicas{world}"},
         "e2e": e2e, "gpu_launches": int(launches),
         "passes_ms": {k: round(v, 4) for k, v in mean_pass.items()},

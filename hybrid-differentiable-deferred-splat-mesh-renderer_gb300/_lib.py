@@ -45,7 +45,7 @@ BUFFER_IDS = {
     "tile_entries": 7,
     "sorted_keys": 8,
     "pair_offsets": 9,
-    "segments": 10,
+    "depth_order": 10,
 }
 
 
@@ -79,8 +79,8 @@ class OutputViews(ctypes.Structure):
 
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_pairs", c_uint64), ("pair_capacity", c_uint64), ("visible_splats", c_uint32),
-                ("segments", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
-                ("device_flags", c_uint32), ("_reserved", c_uint32)]
+                ("_reserved0", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
+                ("device_flags", c_uint32), ("_reserved1", c_uint32)]
 
 
 class HdsrError(RuntimeError):

@@ -20,9 +20,9 @@ namespace {
 constexpr uint32_t kMaxProfiledPasses = 24;
 // names of the profiled passes, indexed by the ids recorded in encode()
 const char* const kPassNames[] = {"upload_uniforms", "frame_init", "project", "count", "scan_pairs",
-                                  "scan_tiles", "emit_keys", "radix_hist", "radix_pass_0", "radix_pass_1",
-                                  "radix_pass_2", "radix_pass_3", "radix_pass_4", "radix_pass_5",
-                                  "radix_pass_6", "radix_pass_7", "segment_sort", "raster"};
+                                  "scan_tiles", "depth_sort", "emit_keys", "tile_sort_0", "tile_sort_1",
+                                  "unused_10", "unused_11", "unused_12", "unused_13", "unused_14",
+                                  "unused_15", "unused_16", "raster"};
 constexpr uint32_t kNumPassNames = sizeof(kPassNames) / sizeof(kPassNames[0]);
 }  // namespace
 
@@ -148,14 +148,24 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   a.M = M;
   a.tile_count = plan->tile_count;
   a.rank_bits = ceil_log2(N > 1 ? N : 2);
-  a.key_bits = 20u + ceil_log2(M > 1 ? M : 2);
-  if (a.rank_bits + a.key_bits > 64u) { delete h; return HDSR_ERR_UNSUPPORTED; }
-  a.passes = (a.key_bits + 7u) / 8u;
+  a.morton_bits = ceil_log2(M > 1 ? M : 2);
+  if (a.rank_bits + a.morton_bits > 64u || a.rank_bits > 32u) { delete h; return HDSR_ERR_UNSUPPORTED; }
+  a.tile_passes = (a.morton_bits + kRadixBits - 1u) / kRadixBits;
+  for (uint32_t p = 0, sh = a.rank_bits, left = a.morton_bits; p < a.tile_passes; ++p) {
+    const uint32_t w = (left + (a.tile_passes - p) - 1u) / (a.tile_passes - p);  // widest digits first
+    a.tile_shift[p] = sh;
+    a.tile_bits[p] = w;
+    sh += w;
+    left -= w;
+  }
   a.cap = cap;
   a.num_sms = sms > 0 ? sms : 1;
   a.color_f32 = h->cfg.color_format == HDSR_COLOR_RGBA32F;
-  a.seg_cap = (uint32_t)(plan->tile_count + cap / kMaxTileEntries + 1);
-  a.radix_tiles_cap = (uint32_t)((cap + kRadixTile - 1) / kRadixTile);
+  a.log_keys = (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) ? 1u : 0u;
+  {
+    const uint64_t most = cap > N ? cap : N;
+    a.radix_tiles_cap = (uint32_t)((most + kRadixTile - 1) / kRadixTile);
+  }
   const uint64_t scan_tiles_n = (N + kScanTile - 1) / kScanTile + 1;
   const uint64_t scan_tiles_m = (M + kScanTile - 1) / kScanTile + 1;
   hdsr_status s = HDSR_OK;
@@ -169,6 +179,9 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.aux, N, "cache_aux");
   ALLOC(a.depth, N, "depth");
   ALLOC(a.ntiles, N, "ntiles");
+  ALLOC(a.dkeys_a, N, "depth_keys_a");
+  ALLOC(a.dkeys_b, N, "depth_keys_b");
+  ALLOC(a.order, N, "depth_order");
   ALLOC(a.pair_off, N, "pair_off");
   ALLOC(a.tile_cnt, M, "tile_counts");
   ALLOC(a.tile_dmin, M, "tile_dmin");
@@ -179,10 +192,8 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.pairs_b, cap, "pairs_b");
   ALLOC(a.entries, cap, "tile_entries");
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
-  ALLOC(a.segments, a.seg_cap, "segments");
-  ALLOC(a.dirty, a.seg_cap, "dirty_segments");
-  ALLOC(a.digit_hist, (uint64_t)kMaxPasses * 256, "digit_hist");
-  ALLOC(a.radix_status, (uint64_t)a.passes * a.radix_tiles_cap * 256, "radix_status");
+  ALLOC(a.tile_digits, (uint64_t)a.radix_tiles_cap * kRadixBins, "tile_digits");
+  ALLOC(a.bin_base, (uint64_t)kRadixBins, "bin_base");
   ALLOC(a.scan_status_n, scan_tiles_n, "scan_status_n");
   ALLOC(a.scan_status_m, scan_tiles_m, "scan_status_m");
   ALLOC(a.ctl, (uint64_t)kCtlWords, "ctl");
@@ -190,8 +201,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   if (s != HDSR_OK) { free_all(h); delete h; return s; }
   a.U = U;
   // status words start at epoch 0, which no frame uses
-  e = cudaMemset(a.radix_status, 0, (size_t)a.passes * a.radix_tiles_cap * 256 * 8);
-  if (e == cudaSuccess) e = cudaMemset(a.scan_status_n, 0, scan_tiles_n * 8);
+  e = cudaMemset(a.scan_status_n, 0, scan_tiles_n * 8);
   if (e == cudaSuccess) e = cudaMemset(a.scan_status_m, 0, scan_tiles_m * 8);
   if (e == cudaSuccess) e = cudaMemset(a.ctl, 0, kCtlWords * 4);
   if (e == cudaSuccess) e = cudaMemset(U, 0, 256);
@@ -348,21 +358,55 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
     mark(h, s, 2);
     if ((e = launch_count(a, s)) != cudaSuccess) return cuda_fail(h, e, "count");
     mark(h, s, 3);
-    if ((e = launch_scan_pairs(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_pairs");
-    mark(h, s, 4);
     if ((e = launch_scan_tiles(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
     mark(h, s, 5);
-    if ((e = launch_emit(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit");
+    // splats: 4 passes over the 32 depth bits -> order (sortRanks by depth)
+    RadixJob dj{};
+    dj.count = a.ctl + kCtlSplats;
+    dj.flags = a.ctl + kCtlFlags;
+    dj.tile_digits = a.tile_digits;
+    dj.bin_base = a.bin_base;
+    dj.tiles_cap = a.radix_tiles_cap;
+    dj.out_low = a.order;
+    dj.low_mask = 0xFFFFFFFFull;
+    for (uint32_t p = 0; p < kDepthPasses; ++p) {
+      dj.in = (p & 1u) ? a.dkeys_b : a.dkeys_a;
+      dj.out = (p & 1u) ? a.dkeys_a : a.dkeys_b;
+      dj.shift = 32u + 8u * p;
+      dj.bits = 8u;
+      if ((e = launch_radix_pass(dj, p + 1 == kDepthPasses, a.num_sms, s)) != cudaSuccess)
+        return cuda_fail(h, e, "depth_sort");
+    }
     mark(h, s, 6);
-    if ((e = launch_radix_hist(a, s)) != cudaSuccess) return cuda_fail(h, e, "radix_hist");
+    if ((e = launch_scan_pairs(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_pairs");
+    mark(h, s, 4);
+    if ((e = launch_emit(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit");
     mark(h, s, 7);
-    for (uint32_t p = 0; p < a.passes; ++p) {
-      if ((e = launch_radix_pass(a, s, p)) != cudaSuccess) return cuda_fail(h, e, "radix_pass");
+    // pairs: stable passes over the Morton tile bits -> tile entries
+    RadixJob tj = dj;
+    tj.count = a.ctl + kCtlPairsLo;
+    tj.out_low = a.entries;
+    tj.low_mask = (1ull << a.rank_bits) - 1ull;
+    for (uint32_t p = 0; p < a.tile_passes; ++p) {
+      tj.in = (p & 1u) ? a.pairs_b : a.pairs_a;
+      tj.out = (p & 1u) ? a.pairs_a : a.pairs_b;
+      tj.shift = a.tile_shift[p];
+      tj.bits = a.tile_bits[p];
+      if ((e = launch_radix_pass(tj, p + 1 == a.tile_passes, a.num_sms, s)) != cudaSuccess)
+        return cuda_fail(h, e, "tile_sort");
       mark(h, s, 8 + p);
     }
-    if ((e = launch_segment_sort(a, s)) != cudaSuccess) return cuda_fail(h, e, "segment_sort");
-    mark(h, s, 16);
-    h->launches += 1 + 3 * n_splat_launch + 2 + 2 + a.passes + 2;
+    if (a.log_keys) {
+      if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
+      h->launches += 1;
+    }
+    h->launches += 1 + 3 * n_splat_launch + 2 + 4 * (kDepthPasses + a.tile_passes);
+  }
+  if (!full) {
+    // composite-only reuses the frame's entries; the raster's tile counter
+    // is the one control word it must start from zero
+    e = cudaMemsetAsync(a.ctl + kCtlRasterTile, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "reset raster counter");
   }
   if ((e = launch_raster(a, s)) != cudaSuccess) return cuda_fail(h, e, "raster");
   mark(h, s, 17);
@@ -389,7 +433,6 @@ hdsr_status hdsr_query_status(hdsr_compositor* h, hdsr_frame_stats* st) {
     st->total_pairs = (uint64_t)ctl[kCtlPairsLo] | ((uint64_t)ctl[kCtlPairsHi] << 32);
     st->pair_capacity = h->args.cap;
     st->visible_splats = ctl[kCtlVisible];
-    st->segments = ctl[kCtlSegments];
     st->hot_tiles = ctl[kCtlHotTiles];
     st->chunks = ctl[kCtlChunks];
     st->device_flags = ctl[kCtlFlags];
@@ -421,7 +464,7 @@ hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, u
       if (!a.sorted_keys) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_KEEP_SORTED_KEYS");
       *ptr = a.sorted_keys; *bytes = cap * 8; break;
     case HDSR_BUF_PAIR_OFFSETS: *ptr = a.pair_off; *bytes = N * 4; break;
-    case HDSR_BUF_SEGMENTS: *ptr = a.segments; *bytes = (uint64_t)a.seg_cap * 8; break;
+    case HDSR_BUF_DEPTH_ORDER: *ptr = a.order; *bytes = N * 4; break;
     default: return fail(h, HDSR_ERR_INVALID_ARG, "unknown buffer id");
   }
   return HDSR_OK;

@@ -12,21 +12,38 @@ namespace hdsr {
 enum Ctl : int {
   kCtlEpoch = 0,       // frame counter: decoupled-lookback status words carry it
   kCtlFlags = 1,       // HDSR_DEV_* bits
-  kCtlPairsLo = 2,     // P, total (tile, splat) pairs of the frame (u64)
+  kCtlPairsLo = 2,     // P, total (tile, splat) pairs of the frame
   kCtlPairsHi = 3,
-  kCtlSegments = 4,    // sort segments appended by the tile scan
+  kCtlSplats = 4,      // N, the depth sort's key count (constant per handle)
   kCtlHotTiles = 5,
   kCtlChunks = 6,
   kCtlVisible = 7,
-  kCtlScanNTile = 8,   // dynamic tile counters
+  kCtlScanNTile = 8,   // dynamic tile counters of the scans
   kCtlScanMTile = 9,
-  kCtlRadixTile = 10,  // .. 10 + kMaxPasses - 1
-  kCtlSegTile = 18,
-  kCtlRasterTile = 19,
-  kCtlDirty = 20,      // segments the check pass found out of order
+  kCtlRasterTile = 19, // dynamic tile counter of the rasteriser
   kCtlWords = 64
 };
-constexpr int kMaxPasses = 8;
+
+constexpr uint32_t kRadixBits = 8;               // widest digit
+constexpr uint32_t kRadixBins = 1u << kRadixBits;
+constexpr uint32_t kDepthPasses = 4;             // 32 depth bits
+constexpr uint32_t kMaxTilePasses = 2;           // <= 16 Morton bits
+
+// One LSD radix pass over u64 keys: digit = (key >> shift) & (2^bits - 1).
+struct RadixJob {
+  const unsigned long long* in;
+  unsigned long long* out;          // non-final passes
+  uint32_t* out_low;                // final pass: key & low_mask
+  unsigned long long* out_keys;     // final pass, optional: the keys themselves
+  unsigned long long low_mask;
+  const uint32_t* count;            // number of keys (device)
+  const uint32_t* flags;            // frame flags: skip the pass on overflow
+  uint32_t* tile_digits;            // kRadixBins * tiles_cap counts -> offsets
+  uint32_t* bin_base;               // kRadixBins totals -> bases
+  uint32_t tiles_cap;
+  uint32_t shift;
+  uint32_t bits;
+};
 
 // Everything a kernel of the frame needs, passed by value.
 struct FrameArgs {
@@ -46,9 +63,12 @@ struct FrameArgs {
   // plan
   uint32_t W, H, cols, rows, M, tile_count;
   uint32_t rank_bits;             // low key bits holding sortRank
-  uint32_t key_bits;              // 20 + Morton bits: radix-sorted bits above rank_bits
-  uint32_t passes;                // 8-bit digit passes
+  uint32_t morton_bits;           // tile bits of the pair keys
+  uint32_t tile_passes;           // radix passes over the tile bits
+  uint32_t tile_shift[kMaxTilePasses];
+  uint32_t tile_bits[kMaxTilePasses];
   uint64_t cap;                   // pair capacity
+  uint32_t log_keys;              // compute per-tile depth range + 20-bit keys
   // projection cache (SoA) and per-splat data
   float4* geo;                    // centerPx.xy, invCov.xy
   uint4* app;                     // invCov.z bits, f16(radius,opacity), f16 rg, f16 b|0
@@ -56,7 +76,10 @@ struct FrameArgs {
   uint2* aux;                     // tile box u8x4, f16 normal confidence|0
   uint32_t* depth;                // f32 NDC depth bits
   uint32_t* ntiles;               // tiles touched per sortRank (0 if invisible)
-  uint32_t* pair_off;             // exclusive prefix of ntiles
+  unsigned long long* dkeys_a;    // depth << 32 | sortRank, per sortRank
+  unsigned long long* dkeys_b;
+  uint32_t* order;                // sortRanks in ascending (depth, sortRank)
+  uint32_t* pair_off;             // exclusive prefix of ntiles in that order
   // tiles
   uint32_t* tile_cnt;
   uint32_t* tile_dmin;
@@ -66,14 +89,11 @@ struct FrameArgs {
   // pairs and entries
   unsigned long long* pairs_a;
   unsigned long long* pairs_b;
-  unsigned long long* sorted_keys;  // optional copy of the radix output
+  unsigned long long* sorted_keys;  // optional: tile, 20-bit log-depth key, sortRank per entry
   uint32_t* entries;              // final per-tile order (sortRank)
-  uint2* segments;                // (start, count)
-  uint32_t* dirty;                // indices of segments that need the full sort
-  uint32_t seg_cap;
-  // radix
-  uint32_t* digit_hist;           // kMaxPasses * 256 counts, then exclusive bases
-  unsigned long long* radix_status;  // kMaxPasses * radix_tiles_cap * 256
+  // radix scratch (shared by every pass, passes run in stream order)
+  uint32_t* tile_digits;
+  uint32_t* bin_base;
   uint32_t radix_tiles_cap;
   unsigned long long* scan_status_n; // per 4096-element tile of the N scan
   unsigned long long* scan_status_m;
@@ -108,9 +128,8 @@ cudaError_t launch_count(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_pairs(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_emit(const FrameArgs& a, cudaStream_t s);
-cudaError_t launch_radix_hist(const FrameArgs& a, cudaStream_t s);    // 2 launches
-cudaError_t launch_radix_pass(const FrameArgs& a, cudaStream_t s, uint32_t pass);
-cudaError_t launch_segment_sort(const FrameArgs& a, cudaStream_t s);  // 2 launches
+cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 4 launches
+cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 
 // sizing helpers shared with the API

@@ -2,12 +2,13 @@
 //
 // k_project follows gpu_project_splats.wgsl:112-358 step by step (one thread
 // per sortRank) and writes the reference's 14-word projection cache as four
-// SoA streams plus the f32 depth word. k_count is count_tile_refs
-// (gpu_tile_splat_composite.wgsl:65-84) extended with the per-tile depth
-// min/max that the hot-tile bucket mapping needs (gpu_tile_bucket_sort.wgsl:
-// 232-237). k_emit writes one 64-bit (tile, 20-bit log depth, sortRank) key
-// per pair at the per-splat prefix offsets; it replaces scatter_tile_refs and
-// the cooperative large-splat scatter (gpu_large_splat_scatter.wgsl).
+// SoA streams plus the f32 depth word, and the splat's depth sort key. k_count
+// is count_tile_refs (gpu_tile_splat_composite.wgsl:65-84); when the 20-bit
+// log-depth keys are requested it also keeps the per-tile depth min/max of
+// the hot-tile bucket mapping (gpu_tile_bucket_sort.wgsl:232-237). k_emit
+// writes one 64-bit (tile, sortRank) key per pair, visiting the splats in
+// ascending (depth, sortRank) order; it replaces scatter_tile_refs and the
+// cooperative large-splat scatter (gpu_large_splat_scatter.wgsl).
 #include "hdsr_internal.cuh"
 
 namespace hdsr {
@@ -60,19 +61,20 @@ __global__ void k_frame_init(FrameArgs a) {
   if (i == 0) {
     a.ctl[kCtlEpoch] += 1u;
     for (int k = 1; k < kCtlWords; ++k) a.ctl[k] = 0u;
+    a.ctl[kCtlSplats] = a.N;
   }
   if (i < a.M) {
     a.tile_cnt[i] = 0u;
     a.tile_dmin[i] = 0xFFFFFFFFu;
     a.tile_dmax[i] = 0u;
   }
-  if (i < kMaxPasses * 256) a.digit_hist[i] = 0u;
 }
 
 __device__ __forceinline__ void write_invisible(const FrameArgs& a, uint32_t r) {
   a.aux[r] = make_uint2(kSentinel, 0u);
   a.depth[r] = kSentinel;
   a.ntiles[r] = 0u;
+  a.dkeys_a[r] = ((unsigned long long)kSentinel << 32) | r;
 }
 
 __global__ void __launch_bounds__(256) k_project(FrameArgs a) {
@@ -248,6 +250,7 @@ __global__ void __launch_bounds__(256) k_project(FrameArgs a) {
   a.aux[r] = make_uint2(box, pack2x16(conf, 0.0f));
   a.depth[r] = f2u(depthNdc);
   a.ntiles[r] = (t1x - t0x + 1u) * (t1y - t0y + 1u);
+  a.dkeys_a[r] = ((unsigned long long)f2u(depthNdc) << 32) | r;
 }
 
 // count_tile_refs + per-tile depth min/max. Splats above the reference's
@@ -255,12 +258,15 @@ __global__ void __launch_bounds__(256) k_project(FrameArgs a) {
 // not serialise up to 17x17 tiles. Templated on the table the atomics go to:
 // global memory, or a per-block copy in shared memory (privatised tables,
 // flushed once per block) when the M-tile tables fit there.
+template <bool MINMAX>
 struct GlobalTables {
   uint32_t *cnt, *dmin, *dmax;
   __device__ void add(uint32_t t, uint32_t d) const {
     atomicAdd(cnt + t, 1u);
-    atomicMin(dmin + t, d);
-    atomicMax(dmax + t, d);
+    if (MINMAX) {
+      atomicMin(dmin + t, d);
+      atomicMax(dmax + t, d);
+    }
   }
 };
 
@@ -296,20 +302,24 @@ __device__ __forceinline__ void count_splats(const FrameArgs& a, const Tables& t
   }
 }
 
+template <bool MINMAX>
 __global__ void __launch_bounds__(256) k_count(FrameArgs a) {
-  count_splats(a, GlobalTables{a.tile_cnt, a.tile_dmin, a.tile_dmax}, blockIdx.x * blockDim.x + threadIdx.x);
+  count_splats(a, GlobalTables<MINMAX>{a.tile_cnt, a.tile_dmin, a.tile_dmax}, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 constexpr uint32_t kCountSmemThreads = 1024;
 
+template <bool MINMAX>
 __global__ void __launch_bounds__(kCountSmemThreads, 1) k_count_smem(FrameArgs a) {
   extern __shared__ uint32_t s_tab[];
   const uint32_t M = a.M;
-  GlobalTables tb{s_tab, s_tab + M, s_tab + 2 * M};
+  GlobalTables<MINMAX> tb{s_tab, s_tab + M, s_tab + 2 * M};
   for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
     tb.cnt[i] = 0u;
-    tb.dmin[i] = 0xFFFFFFFFu;
-    tb.dmax[i] = 0u;
+    if (MINMAX) {
+      tb.dmin[i] = 0xFFFFFFFFu;
+      tb.dmax[i] = 0u;
+    }
   }
   __syncthreads();
   for (uint32_t base = blockIdx.x * blockDim.x; base < a.N; base += gridDim.x * blockDim.x)
@@ -319,55 +329,54 @@ __global__ void __launch_bounds__(kCountSmemThreads, 1) k_count_smem(FrameArgs a
     const uint32_t c = tb.cnt[i];
     if (c) {
       atomicAdd(a.tile_cnt + i, c);
-      atomicMin(a.tile_dmin + i, tb.dmin[i]);
-      atomicMax(a.tile_dmax + i, tb.dmax[i]);
+      if (MINMAX) {
+        atomicMin(a.tile_dmin + i, tb.dmin[i]);
+        atomicMax(a.tile_dmax + i, tb.dmax[i]);
+      }
     }
   }
 }
 
-// Key emission at per-splat offsets: key = tile << (20+R) | k20 << R | sortRank.
+// Key emission: key = tile << R | sortRank, splats visited in ascending
+// (depth, sortRank) order (`order`, from the depth sort) at the prefix
+// offsets of their tile counts in that order. A warp emits the pairs of its
+// 32 consecutive splats as one contiguous range, lane l writing pair
+// begin + l + 32k (coalesced stores); each lane finds the splat owning its
+// pair by a binary search over the warp's prefix offsets.
 __global__ void __launch_bounds__(256) k_emit(FrameArgs a) {
-  if (a.ctl[kCtlFlags] & 0x1u) return;  // overflow: frame skipped
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t P = a.ctl[kCtlPairsLo];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
-  uint32_t box = kSentinel, n = 0u, base = 0u;
-  float logd = 0.0f;
-  if (r < a.N) {
+  uint32_t box = kSentinel, n = 0u, base = P, r = 0u;
+  if (i < a.N) {
+    r = a.order[i];
+    base = a.pair_off[i];
     box = a.aux[r].x;
-    if (box != kSentinel) {
-      n = a.ntiles[r];
-      base = a.pair_off[r];
-      logd = log_depth(a.depth[r]);
-    }
+    if (box != kSentinel) n = a.ntiles[r];
   }
   const uint32_t R = a.rank_bits;
-  const uint32_t KS = 20u + R;
-  if (box != kSentinel && n <= kLargeSplatTiles) {
-    uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
-    uint32_t j = 0;
-    for (uint32_t ty = y0; ty <= y1; ++ty)
-      for (uint32_t tx = x0; tx <= x1; ++tx) {
-        uint32_t t = morton(tx, ty);
-        uint32_t k = key20(logd, a.tile_log[t]);
-        a.pairs_a[base + j] = ((unsigned long long)t << KS) | ((unsigned long long)k << R) | r;
-        ++j;
-      }
-  }
-  uint32_t large = __ballot_sync(0xFFFFFFFFu, box != kSentinel && n > kLargeSplatTiles);
-  while (large) {
-    const int src = __ffs(large) - 1;
-    large &= large - 1u;
-    const uint32_t lb = __shfl_sync(0xFFFFFFFFu, box, src);
-    const uint32_t ln = __shfl_sync(0xFFFFFFFFu, n, src);
-    const uint32_t lbase = __shfl_sync(0xFFFFFFFFu, base, src);
-    const float llog = __shfl_sync(0xFFFFFFFFu, logd, src);
-    const uint32_t lr = __shfl_sync(0xFFFFFFFFu, r, src);
-    const uint32_t x0 = lb & 0xFFu, y0 = (lb >> 8) & 0xFFu, x1 = (lb >> 16) & 0xFFu;
-    const uint32_t spanX = x1 - x0 + 1u;
-    for (uint32_t i = lane; i < ln; i += 32u) {
-      uint32_t t = morton(x0 + i % spanX, y0 + i / spanX);
-      uint32_t k = key20(llog, a.tile_log[t]);
-      a.pairs_a[lbase + i] = ((unsigned long long)t << KS) | ((unsigned long long)k << R) | lr;
+  const uint32_t begin = __shfl_sync(0xFFFFFFFFu, base, 0);
+  const uint32_t end = __shfl_sync(0xFFFFFFFFu, base + n, 31);
+  for (uint32_t p0 = begin; p0 < end; p0 += 32u) {
+    const uint32_t p = p0 + lane;
+    // owner: the largest lane whose base <= p (empty splats share the base of
+    // the next splat, so they are never chosen for a pair they do not own)
+    uint32_t lo = 0;
+#pragma unroll
+    for (uint32_t step = 16; step > 0; step >>= 1) {
+      const uint32_t b = __shfl_sync(0xFFFFFFFFu, base, lo + step);
+      if (b <= p) lo += step;
+    }
+    const uint32_t ob = __shfl_sync(0xFFFFFFFFu, base, lo);
+    const uint32_t obox = __shfl_sync(0xFFFFFFFFu, box, lo);
+    const uint32_t orank = __shfl_sync(0xFFFFFFFFu, r, lo);
+    if (p < end) {
+      const uint32_t j = p - ob;
+      const uint32_t x0 = obox & 0xFFu, y0 = (obox >> 8) & 0xFFu, x1 = (obox >> 16) & 0xFFu;
+      const uint32_t spanX = x1 - x0 + 1u;
+      const uint32_t t = morton(x0 + j % spanX, y0 + j / spanX);
+      a.pairs_a[p] = ((unsigned long long)t << R) | orank;
     }
   }
 }
@@ -375,7 +384,7 @@ __global__ void __launch_bounds__(256) k_emit(FrameArgs a) {
 }  // namespace
 
 cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s) {
-  uint32_t n = a.M > kMaxPasses * 256 ? a.M : kMaxPasses * 256;
+  uint32_t n = a.M > 1u ? a.M : 1u;
   k_frame_init<<<(n + 255) / 256, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
@@ -391,17 +400,22 @@ uint32_t count_smem_max_tiles() { return (200u * 1024u) / 12u; }
 cudaError_t launch_count(const FrameArgs& a, cudaStream_t s) {
   if (!a.N) return cudaSuccess;
   if (a.M <= count_smem_max_tiles()) {
-    const size_t smem = (size_t)a.M * 12u;
+    const size_t smem = (size_t)a.M * (a.log_keys ? 12u : 4u);
     static bool attr_set = false;
     if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(k_count_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      cudaError_t e = cudaFuncSetAttribute(k_count_smem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(count_smem_max_tiles() * 12u));
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_count_smem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(count_smem_max_tiles() * 12u));
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    k_count_smem<<<a.num_sms, kCountSmemThreads, smem, s>>>(a);
+    if (a.log_keys) k_count_smem<true><<<a.num_sms, kCountSmemThreads, smem, s>>>(a);
+    else k_count_smem<false><<<a.num_sms, kCountSmemThreads, smem, s>>>(a);
   } else {
-    k_count<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+    if (a.log_keys) k_count<true><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+    else k_count<false><<<(a.N + 255) / 256, 256, 0, s>>>(a);
   }
   return cudaGetLastError();
 }

@@ -8,9 +8,12 @@
 // gated at weight > 0.01; a quad stops once all four T < 0.001.
 //
 // GB300 layout: one warp owns a 16x16 tile, each lane two 2x2 quads
-// (rows 0-7 and 8-15 of the tile); splat batches of 32 entries are gathered
-// from the SoA projection cache (one entry per lane, 16-byte loads) into the
-// warp's shared-memory slab and then read as broadcasts. FP32 transmittance.
+// (rows 0-7 and 8-15 of the tile), composited in two passes over the tile's
+// entries so that only one quad's accumulators are live (about half the
+// registers, twice the resident warps) and each half stops on its own. Splat
+// batches of 32 entries are gathered from the SoA projection cache (one entry
+// per lane, 16-byte loads) into the warp's shared-memory slab and read as
+// broadcasts. Warps take tiles from an atomic counter. FP32 transmittance.
 // Arithmetic is the canonical form: power = fma(c' dy, dy, fma(b' dx, dy,
 // (a' dx) dx)) and every "acc += v * w" is fma(v, w, acc).
 #include "hdsr_internal.cuh"
@@ -93,6 +96,9 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
   const float sd = s[F_D][i], mr = s[F_MR][i], mm = s[F_MM][i];
   const float nx = s[F_NX][i], ny = s[F_NY][i], nz = s[F_NZ][i];
   const float sc = s[F_CF][i], er = s[F_ER][i], eg = s[F_EG][i], eb = s[F_EB][i];
+  // a splat without emission adds exactly +0 to the emissive sums: skip it
+  // (uniform across the warp, all lanes read the same splat)
+  const bool emits = er != 0.0f || eg != 0.0f || eb != 0.0f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const float g = hx_expf(pw[k]);
@@ -113,9 +119,11 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
     q.n[k][1] = fmaf(ny, gw, q.n[k][1]);
     q.n[k][2] = fmaf(nz, gw, q.n[k][2]);
     q.gc[k] = fmaf(sc, gw, q.gc[k]);
-    q.e[k][0] = fmaf(er, w, q.e[k][0]);
-    q.e[k][1] = fmaf(eg, w, q.e[k][1]);
-    q.e[k][2] = fmaf(eb, w, q.e[k][2]);
+    if (emits) {
+      q.e[k][0] = fmaf(er, w, q.e[k][0]);
+      q.e[k][1] = fmaf(eg, w, q.e[k][1]);
+      q.e[k][2] = fmaf(eb, w, q.e[k][2]);
+    }
   }
   q.done = q.T[0] < 0.001f && q.T[1] < 0.001f && q.T[2] < 0.001f && q.T[3] < 0.001f;
 }
@@ -145,70 +153,77 @@ __device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, ui
   }
 }
 
-__global__ void __launch_bounds__(kWarps * 32) k_raster(FrameArgs a) {
+__device__ __forceinline__ void load_batch(const FrameArgs& a, float (*s)[32], uint32_t e, uint32_t lane) {
+  const uint32_t r = __ldg(a.entries + e);
+  const float4 g = __ldg(a.geo + r);
+  const uint4 ap = __ldg(a.app + r);
+  const uint4 gb = __ldg(a.gb + r);
+  const uint2 ax = __ldg(a.aux + r);
+  s[F_CX][lane] = g.x;
+  s[F_CY][lane] = g.y;
+  s[F_KA][lane] = g.z * -0.5f;
+  s[F_KB][lane] = -g.w;
+  s[F_KC][lane] = u2f(ap.x) * -0.5f;
+  s[F_OP][lane] = hi16(ap.y);
+  s[F_R][lane] = lo16(ap.z);
+  s[F_G][lane] = hi16(ap.z);
+  s[F_B][lane] = lo16(ap.w);
+  s[F_D][lane] = u2f(__ldg(a.depth + r));
+  s[F_MR][lane] = lo16(gb.x);
+  s[F_MM][lane] = hi16(gb.x);
+  float nx, ny, nz;
+  oct_decode(lo16(gb.y), hi16(gb.y), nx, ny, nz);
+  s[F_NX][lane] = nx;
+  s[F_NY][lane] = ny;
+  s[F_NZ][lane] = nz;
+  s[F_CF][lane] = lo16(ax.y);
+  s[F_ER][lane] = lo16(gb.z);
+  s[F_EG][lane] = hi16(gb.z);
+  s[F_EB][lane] = lo16(gb.w);
+}
+
+__global__ void __launch_bounds__(kWarps * 32, 5) k_raster(FrameArgs a) {
   __shared__ float s_pay[kWarps][kFields][32];
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t tile_idx = blockIdx.x * kWarps + warp;
-  if (tile_idx >= a.tile_count) return;
-  const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
-  const uint32_t t = morton(tx, ty);
-  const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
-  const uint32_t qx = lane & 7u, qy = lane >> 3;
-  const uint32_t bx = tx * 16u + qx * 2u;
-  const uint32_t by0 = ty * 16u + qy * 2u, by1 = by0 + 8u;
-  const float p00x = (float)bx + 0.5f;
-  const float p00y0 = (float)by0 + 0.5f, p00y1 = (float)by1 + 0.5f;
-  Quad q0, q1;
-  quad_init(q0);
-  quad_init(q1);
   float (*s)[32] = s_pay[warp];
-  for (uint32_t b = 0; b < count; b += 32u) {
-    const uint32_t n = count - b < 32u ? count - b : 32u;
-    if (lane < n) {
-      const uint32_t r = __ldg(a.entries + start + b + lane);
-      const float4 g = __ldg(a.geo + r);
-      const uint4 ap = __ldg(a.app + r);
-      const uint4 gb = __ldg(a.gb + r);
-      const uint2 ax = __ldg(a.aux + r);
-      s[F_CX][lane] = g.x;
-      s[F_CY][lane] = g.y;
-      s[F_KA][lane] = g.z * -0.5f;
-      s[F_KB][lane] = -g.w;
-      s[F_KC][lane] = u2f(ap.x) * -0.5f;
-      s[F_OP][lane] = hi16(ap.y);
-      s[F_R][lane] = lo16(ap.z);
-      s[F_G][lane] = hi16(ap.z);
-      s[F_B][lane] = lo16(ap.w);
-      s[F_D][lane] = u2f(__ldg(a.depth + r));
-      s[F_MR][lane] = lo16(gb.x);
-      s[F_MM][lane] = hi16(gb.x);
-      float nx, ny, nz;
-      oct_decode(lo16(gb.y), hi16(gb.y), nx, ny, nz);
-      s[F_NX][lane] = nx;
-      s[F_NY][lane] = ny;
-      s[F_NZ][lane] = nz;
-      s[F_CF][lane] = lo16(ax.y);
-      s[F_ER][lane] = lo16(gb.z);
-      s[F_EG][lane] = hi16(gb.z);
-      s[F_EB][lane] = lo16(gb.w);
+  for (;;) {
+    uint32_t tile_idx = 0;
+    if (lane == 0) tile_idx = atomicAdd(a.ctl + kCtlRasterTile, 1u);
+    tile_idx = __shfl_sync(0xFFFFFFFFu, tile_idx, 0);
+    if (tile_idx >= a.tile_count) break;
+    const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
+    const uint32_t t = morton(tx, ty);
+    const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
+    const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
+    const float p00x = (float)bx + 0.5f;
+#pragma unroll 1
+    for (uint32_t half = 0; half < 2; ++half) {
+      const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
+      const float p00y = (float)by + 0.5f;
+      Quad q;
+      quad_init(q);
+      for (uint32_t b = 0; b < count; b += 32u) {
+        const uint32_t n = count - b < 32u ? count - b : 32u;
+        if (lane < n) load_batch(a, s, start + b + lane, lane);
+        __syncwarp();
+        for (uint32_t i = 0; i < n; ++i)
+          if (!q.done) quad_splat(q, p00x, p00y, s, (int)i);
+        __syncwarp();
+        if (__all_sync(0xFFFFFFFFu, q.done)) break;
+      }
+      quad_store(a, q, bx, by);
     }
-    __syncwarp();
-    for (uint32_t i = 0; i < n; ++i) {
-      if (!q0.done) quad_splat(q0, p00x, p00y0, s, (int)i);
-      if (!q1.done) quad_splat(q1, p00x, p00y1, s, (int)i);
-    }
-    __syncwarp();
-    if (__all_sync(0xFFFFFFFFu, q0.done && q1.done)) break;
   }
-  quad_store(a, q0, bx, by0);
-  quad_store(a, q1, bx, by1);
 }
 
 }  // namespace
 
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s) {
-  const uint32_t blocks = (a.tile_count + kWarps - 1) / kWarps;
+  // persistent warps: enough blocks to fill every SM, tiles from a counter
+  const uint32_t want = (a.tile_count + kWarps - 1) / kWarps;
+  const uint32_t cap = (uint32_t)a.num_sms * 8u;
+  const uint32_t blocks = want < cap ? want : cap;
   if (blocks) k_raster<<<blocks, kWarps * 32, 0, s>>>(a);
   return cudaGetLastError();
 }

@@ -3,10 +3,12 @@
 // Replaces the reference's three-pass Hillis-Steele scan (scan,
 // scan_block_sums, add_block_sums in gpu_prefix_sum.wgsl:169-240, driven by
 // gpuTileSplatCompositor.ts:1063-1088) with one launch per array:
-//   - per-splat tile counts (N) -> pair offsets and P, the frame's pair total;
+//   - per-splat tile counts, taken in ascending (depth, sortRank) order (N)
+//     -> pair offsets of the emission and P, the frame's pair total;
 //   - per-tile counts (M) -> tile offsets (bit-identical to the reference's
-//     tileOffsets), plus per-tile log-depth parameters and the sort segment
-//     list that replaces classify_tiles (gpu_tile_classify.wgsl:44-86).
+//     tileOffsets), the hot-tile statistics of classify_tiles
+//     (gpu_tile_classify.wgsl:44-86) and, when requested, the per-tile
+//     log-depth parameters of the 20-bit keys.
 // Tiles of 4096 elements are claimed through an atomic counter, so a tile
 // only waits on tiles already claimed by running blocks; every wait is
 // bounded and sets HDSR_DEV_TIMEOUT when it gives up.
@@ -52,7 +54,7 @@ struct PairScan {
   static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
-  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.ntiles[i]; }
+  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.ntiles[a.order[i]]; }
   static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) { a.pair_off[i] = excl; }
   static __device__ void finish(const FrameArgs& a, uint32_t total) {
     a.ctl[kCtlPairsLo] = total;
@@ -70,23 +72,12 @@ struct TileScan {
     a.tile_off[i] = excl;
     const uint32_t c = a.tile_cnt[i];
     if (c == 0u) return;
-    a.tile_log[i] = tile_log_params(a.tile_dmin[i], a.tile_dmax[i]);
-    if (c < 2u) return;
-    if (c <= kMaxTileEntries) {
-      uint32_t slot = atomicAdd(a.ctl + kCtlSegments, 1u);
-      if (slot < a.seg_cap) a.segments[slot] = make_uint2(excl, c);
-    } else {
-      // hot tile: greedy chunk pack of the bucket-ordered entries yields
-      // consecutive 4096-entry chunks (gpu_tile_bucket_sort.wgsl:276-307)
-      const uint32_t nch = (c + kMaxTileEntries - 1u) / kMaxTileEntries;
+    if (a.log_keys) a.tile_log[i] = tile_log_params(a.tile_dmin[i], a.tile_dmax[i]);
+    if (c > kMaxTileEntries) {
+      // hot tile: the reference's bucket cascade splits it into 4096-entry
+      // chunks (gpu_tile_bucket_sort.wgsl:276-307)
       atomicAdd(a.ctl + kCtlHotTiles, 1u);
-      atomicAdd(a.ctl + kCtlChunks, nch);
-      uint32_t slot = atomicAdd(a.ctl + kCtlSegments, nch);
-      for (uint32_t k = 0; k < nch; ++k) {
-        uint32_t st = k * kMaxTileEntries;
-        uint32_t cnt = c - st < kMaxTileEntries ? c - st : kMaxTileEntries;
-        if (slot + k < a.seg_cap) a.segments[slot + k] = make_uint2(excl + st, cnt);
-      }
+      atomicAdd(a.ctl + kCtlChunks, (c + kMaxTileEntries - 1u) / kMaxTileEntries);
     }
   }
   static __device__ void finish(const FrameArgs&, uint32_t) {}

@@ -1,323 +1,289 @@
-// hdsr_sort.cu — one-sweep LSD radix sort of the (tile, log-depth) pair keys
-// and the per-segment depth sort.
+// hdsr_sort.cu — the stable LSD radix sort of the frame and the optional
+// 20-bit log-depth key readback.
 //
-// Keys are u64: tile << (20+R) | k20 << R | sortRank, where R = rank bits.
-// The radix sorts only the 20 + Morton bits above R, 8 bits per pass; the
-// sortRank bits need no pass because the sort is stable and keys are emitted
-// in ascending sortRank. This is the (Morton tile, log-depth) radix order the
-// reference documents (README.md:77-80, gpuRadixSort.ts:1-354, never
-// dispatched there) with its 16-bucket / 4-bit digits replaced by 256-way
-// digits, warp match ranking, shared-memory staging and decoupled lookback
-// on the digit offsets (one launch per digit, no separate scan passes).
-//
-// The segment check + sort replace tile_depth_sort (gpu_tile_depth_sort.wgsl:
-// 114-165) and chunk_sort (gpu_tile_chunk_sort.wgsl:345-395): every segment
-// (a tile of 2..4096 entries, or a 4096-entry chunk of a hot tile) ends up in
-// ascending 64-bit (depth bits, sortRank) order, a total order, so the result
-// is the canonical per-tile order whatever the input order.
+// Per-tile order. Every tile's entries end in ascending (depth bits,
+// sortRank) order: the order of tile_depth_sort (gpu_tile_depth_sort.wgsl:
+// 114-165) and chunk_sort (gpu_tile_chunk_sort.wgsl:345-395) with sortRank
+// breaking their ties, and — because the 128 log-depth buckets of the
+// hot-tile cascade (gpu_tile_bucket_sort.wgsl:240-307) are monotone in the
+// depth — also the cascade's order when a bucket keeps (depth, sortRank)
+// order. So the frame's sort is one stable LSD radix over the composite key
+// (Morton tile, depth bits, sortRank), done in two stages:
+//   1. the depth digits on the N splats (depth is per splat): 4 passes of 8
+//      bits over u64 keys depth << 32 | sortRank; the pairs are then emitted
+//      in that depth order (hdsr_project.cu);
+//   2. the tile digits on the P pairs: 2 passes over u64 keys
+//      tile << R | sortRank (R = rank bits); the last pass writes the 1-u32
+//      tile entries (sortRank).
+// Each pass is reduce-then-scan: an upsweep counts the digits of every block
+// tile of keys, a column scan turns the counts into per-tile digit offsets,
+// a bin scan gives the digits' global bases, and a downsweep ranks the keys
+// per warp with __match_any_sync (stable: warp-striped items keep input
+// order), stages them in shared memory in digit order and writes consecutive
+// addresses of each digit bucket from consecutive threads.
 #include "hdsr_internal.cuh"
 
 namespace hdsr {
 
 namespace {
 
-__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
-  return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
-__device__ __forceinline__ void st_volatile(unsigned long long* p, unsigned long long v) {
-  *reinterpret_cast<volatile unsigned long long*>(p) = v;
-}
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
-__device__ __forceinline__ uint32_t frame_pairs(const FrameArgs& a) {
-  return a.ctl[kCtlPairsLo];
-}
 
-__global__ void __launch_bounds__(256) k_radix_hist(FrameArgs a) {
-  __shared__ uint32_t s_hist[kMaxPasses * 256];
-  if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t P = frame_pairs(a);
-  for (uint32_t i = threadIdx.x; i < a.passes * 256u; i += blockDim.x) s_hist[i] = 0u;
-  __syncthreads();
-  const uint32_t R = a.rank_bits;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
-    const unsigned long long k = a.pairs_a[i];
-    for (uint32_t p = 0; p < a.passes; ++p) atomicAdd(&s_hist[p * 256u + (uint32_t)((k >> (R + 8u * p)) & 0xFFull)], 1u);
+__device__ __forceinline__ bool skipped(const RadixJob& j) { return (*j.flags & 0x1u) != 0u; }
+
+// Upsweep: per block-tile digit counts, bin-major (tile_digits[bin*cap+tile]).
+__global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
+  __shared__ uint32_t s_hist[kRadixBins];
+  if (skipped(j)) return;
+  const uint32_t P = *j.count;
+  const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
+  const uint32_t dmask = (1u << j.bits) - 1u;
+  for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+    for (uint32_t i = threadIdx.x; i < kRadixBins; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    const uint32_t base = tile * kRadixTile;
+    uint32_t dig[kRadixItems];
+#pragma unroll
+    for (uint32_t i = 0; i < kRadixItems; ++i) {
+      const uint32_t g = base + i * kRadixThreads + threadIdx.x;
+      dig[i] = g < P ? (uint32_t)(j.in[g] >> j.shift) & dmask : kRadixBins;
+    }
+#pragma unroll
+    for (uint32_t i = 0; i < kRadixItems; ++i)
+      if (dig[i] < kRadixBins) atomicAdd(&s_hist[dig[i]], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b <= dmask; b += blockDim.x)
+      j.tile_digits[(size_t)b * j.tiles_cap + tile] = s_hist[b];
+    __syncthreads();
   }
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < a.passes * 256u; i += blockDim.x)
-    if (s_hist[i]) atomicAdd(a.digit_hist + i, s_hist[i]);
 }
 
-// Exclusive scan of each pass's 256 digit counts (one block per pass).
-__global__ void __launch_bounds__(256) k_radix_hist_scan(FrameArgs a) {
+// Column scan: for every bin, exclusive prefix of its per-tile counts; the
+// bin's total goes to bin_base. One block per bin, 16 tiles per thread.
+__global__ void __launch_bounds__(256) k_radix_colscan(RadixJob j) {
+  constexpr uint32_t IT = 16;
   __shared__ uint32_t s_w[8];
-  if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t p = blockIdx.x, d = threadIdx.x, lane = d & 31u, w = d >> 5;
-  uint32_t v = a.digit_hist[p * 256u + d];
+  __shared__ uint32_t s_carry;
+  if (skipped(j)) return;
+  const uint32_t P = *j.count;
+  const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
+  const uint32_t bin = blockIdx.x, tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
+  uint32_t* col = j.tile_digits + (size_t)bin * j.tiles_cap;
+  if (tid == 0) s_carry = 0u;
+  __syncthreads();
+  for (uint32_t t0 = 0; t0 < num_tiles; t0 += 256u * IT) {
+    const uint32_t tb = t0 + tid * IT;
+    uint32_t v[IT];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < IT; ++k) {
+      v[k] = tb + k < num_tiles ? col[tb + k] : 0u;
+      sum += v[k];
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t x = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += x;
+    }
+    if (lane == 31) s_w[w] = inc;
+    __syncthreads();
+    uint32_t run = s_carry;
+    for (uint32_t k = 0; k < w; ++k) run += s_w[k];
+    run += inc - sum;
+#pragma unroll
+    for (uint32_t k = 0; k < IT; ++k) {
+      if (tb + k < num_tiles) col[tb + k] = run;
+      run += v[k];
+    }
+    __syncthreads();
+    if (tid == 255) s_carry = run;
+    __syncthreads();
+  }
+  if (tid == 0) j.bin_base[bin] = s_carry;
+}
+
+// Bin scan: bin totals -> exclusive global bases (256 threads, 2 bins each).
+__global__ void __launch_bounds__(256) k_radix_binscan(RadixJob j) {
+  __shared__ uint32_t s_w[8];
+  if (skipped(j)) return;
+  const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+  const uint32_t nb = 1u << j.bits;
+  uint32_t* h = j.bin_base;
+  const uint32_t v0 = 2 * t < nb ? h[2 * t] : 0u, v1 = 2 * t + 1 < nb ? h[2 * t + 1] : 0u;
+  const uint32_t v = v0 + v1;
   uint32_t inc = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-    if (lane >= (uint32_t)o) inc += t;
+    uint32_t x = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= (uint32_t)o) inc += x;
   }
   if (lane == 31) s_w[w] = inc;
   __syncthreads();
   uint32_t off = 0;
   for (uint32_t k = 0; k < w; ++k) off += s_w[k];
-  a.digit_hist[p * 256u + d] = off + inc - v;
+  const uint32_t ex = off + inc - v;
+  if (2 * t < nb) h[2 * t] = ex;
+  if (2 * t + 1 < nb) h[2 * t + 1] = ex + v0;
 }
 
+// Shared memory of one downsweep block (dynamic).
+struct SweepSmem {
+  unsigned long long keys[kRadixTile];
+  uint32_t whist[kRadixThreads / 32][kRadixBins];
+  uint32_t excl[kRadixBins];  // per digit: global offset minus tile-local bucket start
+  uint32_t wsum[kRadixThreads / 32];
+};
+
+// Downsweep: rank (warp match, leader atomic + shuffle), fold per-warp
+// offsets into one table, scatter to shared memory in digit order, write out.
 template <bool LAST>
-__global__ void __launch_bounds__(kRadixThreads) k_onesweep(FrameArgs a, uint32_t pass,
-                                                            const unsigned long long* __restrict__ in,
-                                                            unsigned long long* __restrict__ out) {
+__global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j) {
   constexpr uint32_t W = kRadixThreads / 32;
-  __shared__ unsigned long long s_keys[kRadixTile];
-  __shared__ uint32_t s_whist[W][256];
-  __shared__ uint32_t s_excl[256];
-  __shared__ uint32_t s_gbase[256];
-  __shared__ uint32_t s_wsum[W];
-  __shared__ uint32_t s_tile;
-  if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t P = frame_pairs(a);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SweepSmem& S = *reinterpret_cast<SweepSmem*>(smem_raw);
+  if (skipped(j)) return;
+  const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
-  const uint32_t shift = a.rank_bits + 8u * pass;
-  const uint32_t epoch = a.ctl[kCtlEpoch];
+  const uint32_t shift = j.shift;
+  const uint32_t dmask = (1u << j.bits) - 1u;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  unsigned long long* status = a.radix_status + (size_t)pass * a.radix_tiles_cap * 256u;
-  const unsigned long long rank_mask = (1ull << a.rank_bits) - 1ull;
   const uint32_t lt = lanemask_lt();
-  for (;;) {
-    if (tid == 0) s_tile = atomicAdd(a.ctl + kCtlRadixTile + pass, 1u);
-    for (uint32_t i = tid; i < W * 256u; i += kRadixThreads) (&s_whist[0][0])[i] = 0u;
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    if (tile >= num_tiles) break;
-    const uint32_t base = tile * kRadixTile;
-    unsigned long long key[kRadixItems];
-    uint32_t dig[kRadixItems];
-    uint32_t rank[kRadixItems];
-#pragma unroll
-    for (uint32_t i = 0; i < kRadixItems; ++i) {
-      const uint32_t g = base + warp * (32u * kRadixItems) + i * 32u + lane;
-      if (g < P) {
-        key[i] = in[g];
-        dig[i] = (uint32_t)((key[i] >> shift) & 0xFFull);
-      } else {
-        key[i] = 0ull;
-        dig[i] = 256u;
-      }
-    }
-#pragma unroll
-    for (uint32_t i = 0; i < kRadixItems; ++i) {
-      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig[i]);
-      const uint32_t lower = __popc(peers & lt);
-      const bool valid = dig[i] < 256u;
-      const uint32_t prior = valid ? s_whist[warp][dig[i]] : 0u;
-      __syncwarp();
-      if (valid && lower == 0u) s_whist[warp][dig[i]] = prior + __popc(peers);
-      __syncwarp();
-      rank[i] = prior + lower;
-    }
-    __syncthreads();
-    // per digit: exclusive over warps, tile total, tile-local exclusive prefix
+  static_assert(kRadixBins == kRadixThreads, "one digit per thread in the bookkeeping");
+  for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+    for (uint32_t i = tid; i < W * kRadixBins; i += kRadixThreads) (&S.whist[0][0])[i] = 0u;
     const uint32_t d = tid;
-    uint32_t run = 0;
+    __syncthreads();
+    const uint32_t base = tile * kRadixTile;
+    {
+      unsigned long long key[kRadixItems];
+      uint32_t rank[kRadixItems];
 #pragma unroll
-    for (uint32_t w = 0; w < W; ++w) {
-      uint32_t c = s_whist[w][d];
-      s_whist[w][d] = run;
-      run += c;
-    }
-    if (tile == 0) st_volatile(status + d, make_status(epoch, kFlagInc, run));
-    else st_volatile(status + (size_t)tile * 256u + d, make_status(epoch, kFlagAgg, run));
-    uint32_t inc = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-      if (lane >= (uint32_t)o) inc += t;
-    }
-    if (lane == 31) s_wsum[warp] = inc;
-    // lookback over previous tiles for digit d
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      int t = (int)tile - 1;
-      while (t >= 0) {
-        unsigned long long st;
-        uint32_t spins = 0;
-        for (;;) {
-          st = ld_volatile(status + (size_t)t * 256u + d);
-          if ((uint32_t)(st >> 34) == (epoch & 0x3FFFFFFFu) && ((st >> 32) & 3ull) != 0ull) break;
-          if (++spins > kSpinLimit) {
-            atomicOr(a.ctl + kCtlFlags, 0x2u);
-            st = make_status(epoch, kFlagInc, 0u);
-            break;
-          }
-          __nanosleep(32);
-        }
-        prefix += (uint32_t)st;
-        if (((st >> 32) & 3ull) == kFlagInc) break;
-        --t;
+      for (uint32_t i = 0; i < kRadixItems; ++i) {
+        const uint32_t g = base + warp * (32u * kRadixItems) + i * 32u + lane;
+        key[i] = g < P ? j.in[g] : ~0ull;
       }
-      st_volatile(status + (size_t)tile * 256u + d, make_status(epoch, kFlagInc, prefix + run));
-    }
-    s_gbase[d] = a.digit_hist[pass * 256u + d] + prefix;
-    __syncthreads();
-    uint32_t woff = 0;
-    for (uint32_t w = 0; w < warp; ++w) woff += s_wsum[w];
-    s_excl[d] = woff + inc - run;
-    __syncthreads();
 #pragma unroll
-    for (uint32_t i = 0; i < kRadixItems; ++i) {
-      if (dig[i] < 256u) s_keys[s_excl[dig[i]] + s_whist[warp][dig[i]] + rank[i]] = key[i];
+      for (uint32_t i = 0; i < kRadixItems; ++i) {
+        const uint32_t g = base + warp * (32u * kRadixItems) + i * 32u + lane;
+        const uint32_t dig = g < P ? (uint32_t)(key[i] >> shift) & dmask : kRadixBins;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig);
+        const uint32_t lower = __popc(peers & lt);
+        const uint32_t leader = __ffs(peers) - 1u;
+        uint32_t prior = 0u;
+        if (lower == 0u && dig < kRadixBins) prior = atomicAdd(&S.whist[warp][dig], (uint32_t)__popc(peers));
+        prior = __shfl_sync(0xFFFFFFFFu, prior, leader);  // every lane reads its group's leader
+        rank[i] = prior + lower;
+      }
+      __syncthreads();
+      // digit d: count over warps, tile-local bucket start, per-warp offsets
+      uint32_t run = 0;
+#pragma unroll
+      for (uint32_t w = 0; w < W; ++w) run += S.whist[w][d];
+      uint32_t inc = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= (uint32_t)o) inc += t;
+      }
+      if (lane == 31) S.wsum[warp] = inc;
+      __syncthreads();
+      uint32_t woff = 0;
+      for (uint32_t w = 0; w < warp; ++w) woff += S.wsum[w];
+      uint32_t e = woff + inc - run;
+      if (d <= dmask) S.excl[d] = j.bin_base[d] + j.tile_digits[(size_t)d * j.tiles_cap + tile] - e;
+#pragma unroll
+      for (uint32_t w = 0; w < W; ++w) {
+        const uint32_t c = S.whist[w][d];
+        S.whist[w][d] = e;
+        e += c;
+      }
+      __syncthreads();
+#pragma unroll
+      for (uint32_t i = 0; i < kRadixItems; ++i) {
+        const uint32_t g = base + warp * (32u * kRadixItems) + i * 32u + lane;
+        if (g < P) {
+          const uint32_t dig = (uint32_t)(key[i] >> shift) & dmask;
+          S.keys[S.whist[warp][dig] + rank[i]] = key[i];
+        }
+      }
     }
     __syncthreads();
     const uint32_t count = P - base < kRadixTile ? P - base : kRadixTile;
-    for (uint32_t j = tid; j < count; j += kRadixThreads) {
-      const unsigned long long k = s_keys[j];
-      const uint32_t dj = (uint32_t)((k >> shift) & 0xFFull);
-      const uint32_t o = s_gbase[dj] + (j - s_excl[dj]);
+    for (uint32_t jj = tid; jj < count; jj += kRadixThreads) {
+      const unsigned long long k = S.keys[jj];
+      const uint32_t o = S.excl[(uint32_t)(k >> shift) & dmask] + jj;
       if (LAST) {
-        a.entries[o] = (uint32_t)(k & rank_mask);
-        if (a.sorted_keys) a.sorted_keys[o] = k;
+        j.out_low[o] = (uint32_t)(k & j.low_mask);
+        if (j.out_keys) j.out_keys[o] = k;
       } else {
-        out[o] = k;
+        j.out[o] = k;
       }
     }
     __syncthreads();
   }
 }
 
-
-// Check pass: one warp per segment compares every adjacent pair of entries
-// under the (depth bits, sortRank) order. The radix output is ordered by the
-// 20-bit log-depth key with sortRank ties, and the key is monotone in the
-// depth, so a segment can only be out of order inside a run of equal keys;
-// on the scenes measured here no segment is. Segments with an inversion are
-// appended to the dirty list for the full sort below.
-__global__ void __launch_bounds__(256) k_segcheck(FrameArgs a) {
+// Verification readback of the 20-bit log-depth keys: for every final entry
+// i of tile t, sorted_keys[i] = t << (20+R) | k20 << R | sortRank (k20: the
+// tile's log-depth mapping, gpu_tile_bucket_sort.wgsl:240-250, scaled to
+// 2^20). One warp per tile.
+__global__ void __launch_bounds__(256) k_log_depth_keys(FrameArgs a) {
   if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t nseg = min(a.ctl[kCtlSegments], a.seg_cap);
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  constexpr uint32_t U = 4;  // 128 entries per warp step
-  for (uint32_t sidx = wid; sidx < nseg; sidx += nw) {
-    const uint2 sg = a.segments[sidx];
-    const uint32_t start = sg.x;
-    const uint32_t count = (sg.y <= kMaxTileEntries && (uint64_t)start + sg.y <= a.cap) ? sg.y : 0u;
-    bool bad = false;
-    unsigned long long carry = 0ull;  // last key of the previous step (lane-uniform)
-    for (uint32_t base = 0; base < count; base += 32u * U) {
-      uint32_t r[U];
-      unsigned long long k[U];
-#pragma unroll
-      for (uint32_t u = 0; u < U; ++u) {
-        const uint32_t i = base + u * 32u + lane;
-        r[u] = i < count ? __ldg(a.entries + start + i) : 0u;
-      }
-#pragma unroll
-      for (uint32_t u = 0; u < U; ++u) {
-        const uint32_t i = base + u * 32u + lane;
-        k[u] = i < count ? (((unsigned long long)__ldg(a.depth + r[u]) << 32) | r[u]) : ~0ull;
-      }
-#pragma unroll
-      for (uint32_t u = 0; u < U; ++u) {
-        const uint32_t i = base + u * 32u + lane;
-        const unsigned long long next = __shfl_down_sync(0xFFFFFFFFu, k[u], 1);
-        const unsigned long long first = __shfl_sync(0xFFFFFFFFu, k[u], 0);
-        if (lane < 31u && i + 1u < count && k[u] > next) bad = true;
-        if ((base > 0u || u > 0u) && lane == 0u && carry > first) bad = true;
-        carry = __shfl_sync(0xFFFFFFFFu, k[u], 31);
-      }
-    }
-    if (__any_sync(0xFFFFFFFFu, bad) && lane == 0u) {
-      const uint32_t slot = atomicAdd(a.ctl + kCtlDirty, 1u);
-      a.dirty[slot] = sidx;
+  const uint32_t R = a.rank_bits;
+  for (uint32_t t = w; t < a.M; t += nw) {
+    const uint32_t c = a.tile_cnt[t];
+    if (!c) continue;
+    const uint32_t off = a.tile_off[t];
+    const float2 tl = a.tile_log[t];
+    for (uint32_t i = lane; i < c; i += 32u) {
+      const uint32_t r = a.entries[off + i];
+      const uint32_t k = key20(log_depth(a.depth[r]), tl);
+      a.sorted_keys[off + i] = ((unsigned long long)t << (20u + R)) | ((unsigned long long)k << R) | r;
     }
   }
 }
 
-__device__ __forceinline__ uint32_t insert_zero_bit(uint32_t v, uint32_t bit) {
-  uint32_t mask = (1u << bit) - 1u;
-  return ((v >> bit) << (bit + 1u)) | (v & mask);
-}
-
-// Full sort of the dirty segments: bitonic network over the 64-bit
-// (depth bits, sortRank) keys in shared memory, sized to the next power of
-// two of the segment. The keys are unique, so the result is the canonical
-// order whatever the input order.
-__global__ void __launch_bounds__(256) k_segsort(FrameArgs a) {
-  __shared__ unsigned long long s[kMaxTileEntries];
-  __shared__ uint32_t s_seg;
-  if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t ndirty = min(a.ctl[kCtlDirty], a.seg_cap);
-  const uint32_t tid = threadIdx.x;
-  for (;;) {
-    if (tid == 0) s_seg = atomicAdd(a.ctl + kCtlSegTile, 1u);
-    __syncthreads();
-    const uint32_t didx = s_seg;
-    if (didx >= ndirty) break;
-    const uint2 sg = a.segments[a.dirty[didx]];
-    const uint32_t start = sg.x;
-    const uint32_t count = (sg.y <= kMaxTileEntries && (uint64_t)start + sg.y <= a.cap) ? sg.y : 0u;
-    uint32_t npad = 1;
-    while (npad < count) npad <<= 1;
-    for (uint32_t i = tid; i < npad; i += blockDim.x) {
-      if (i < count) {
-        uint32_t r = a.entries[start + i];
-        s[i] = ((unsigned long long)a.depth[r] << 32) | r;
-      } else {
-        s[i] = ~0ull;
-      }
-    }
-    __syncthreads();
-    for (uint32_t k = 2; k <= npad; k <<= 1) {
-      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-        const uint32_t bit = __ffs(j) - 1;
-        for (uint32_t c = tid; c < npad / 2; c += blockDim.x) {
-          uint32_t l = insert_zero_bit(c, bit);
-          uint32_t r = l | j;
-          bool asc = (l & k) == 0u;
-          unsigned long long x = s[l], y = s[r];
-          if ((x > y) == asc) { s[l] = y; s[r] = x; }
-        }
-        __syncthreads();
-      }
-    }
-    for (uint32_t i = tid; i < count; i += blockDim.x) a.entries[start + i] = (uint32_t)s[i];
-    __syncthreads();
-  }
+// Persistent grid: as many blocks as can be resident at once.
+template <class K>
+int resident_blocks(K kernel, int threads, int sms, size_t smem) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  return per_sm * sms;
 }
 
 }  // namespace
 
-cudaError_t launch_radix_hist(const FrameArgs& a, cudaStream_t s) {
-  k_radix_hist<<<a.num_sms * 4, 256, 0, s>>>(a);
-  k_radix_hist_scan<<<a.passes, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-// Pass p reads pairs_a (even p) or pairs_b (odd p); the last pass writes the
-// sortRank entries instead of keys.
-cudaError_t launch_radix_pass(const FrameArgs& a, cudaStream_t s, uint32_t p) {
-  const unsigned long long* in = (p & 1u) ? a.pairs_b : a.pairs_a;
-  unsigned long long* out = (p & 1u) ? a.pairs_a : a.pairs_b;
-  if (p + 1 == a.passes) {
-    k_onesweep<true><<<a.num_sms * 4, kRadixThreads, 0, s>>>(a, p, in, out);
-  } else {
-    k_onesweep<false><<<a.num_sms * 4, kRadixThreads, 0, s>>>(a, p, in, out);
+cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s) {
+  static int grid_mid = 0, grid_last = 0;
+  const size_t smem = sizeof(SweepSmem);
+  if (!grid_mid) {
+    cudaError_t e = cudaFuncSetAttribute(k_radix_downsweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_radix_downsweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    grid_mid = resident_blocks(k_radix_downsweep<false>, kRadixThreads, num_sms, smem);
+    grid_last = resident_blocks(k_radix_downsweep<true>, kRadixThreads, num_sms, smem);
   }
+  k_radix_upsweep<<<num_sms * 8, kRadixThreads, 0, s>>>(j);
+  k_radix_colscan<<<1u << j.bits, 256, 0, s>>>(j);
+  k_radix_binscan<<<1, 256, 0, s>>>(j);
+  if (last) k_radix_downsweep<true><<<grid_last, kRadixThreads, smem, s>>>(j);
+  else k_radix_downsweep<false><<<grid_mid, kRadixThreads, smem, s>>>(j);
   return cudaGetLastError();
 }
 
-cudaError_t launch_segment_sort(const FrameArgs& a, cudaStream_t s) {
-  k_segcheck<<<a.num_sms * 8, 256, 0, s>>>(a);
-  k_segsort<<<a.num_sms * 4, 256, 0, s>>>(a);
+cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s) {
+  if (a.sorted_keys) k_log_depth_keys<<<a.num_sms * 4, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

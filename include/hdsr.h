@@ -67,7 +67,7 @@ typedef struct hdsr_plan {
 #define HDSR_COLOR_RGBA16F 0u     /* reference output texture format */
 #define HDSR_COLOR_RGBA32F 1u
 
-#define HDSR_CFG_KEEP_SORTED_KEYS 0x1u  /* keep the radix output keys for readback */
+#define HDSR_CFG_KEEP_SORTED_KEYS 0x1u  /* compute the 20-bit log-depth keys per entry */
 #define HDSR_CFG_NO_GRAPH         0x2u  /* launch kernels directly, no CUDA graph  */
 
 /* Options of createTileSplatCompositor — gpuTileSplatCompositor.ts:141-145
@@ -108,11 +108,11 @@ typedef struct hdsr_frame_stats {
   uint64_t total_pairs;           /* P of the last encoded frame */
   uint64_t pair_capacity;
   uint32_t visible_splats;
-  uint32_t segments;              /* per-tile / per-chunk sort segments */
+  uint32_t reserved0;
   uint32_t hot_tiles;             /* tiles with > 4096 entries */
   uint32_t chunks;                /* 4096-entry chunks of hot tiles */
   uint32_t device_flags;          /* HDSR_DEV_* */
-  uint32_t _reserved;
+  uint32_t reserved1;
 } hdsr_frame_stats;
 
 typedef struct hdsr_compositor hdsr_compositor;
@@ -179,9 +179,9 @@ typedef enum hdsr_buffer_id {
   HDSR_BUF_TILE_COUNTS = 5,   /* u32[M] */
   HDSR_BUF_TILE_OFFSETS = 6,  /* u32[M] exclusive prefix of tile counts */
   HDSR_BUF_TILE_ENTRIES = 7,  /* u32[P] sortRank per entry, final per-tile order */
-  HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] radix output: tile<<(20+R) | k20<<R | sortRank */
-  HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat tile counts */
-  HDSR_BUF_SEGMENTS = 10      /* uint2[S] (start, count) sort segments, unordered */
+  HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] per final entry: tile<<(20+R) | k20<<R | sortRank */
+  HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat tile counts, depth order */
+  HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] sortRanks in ascending (depth bits, sortRank) */
 } hdsr_buffer_id;
 
 /* Device address and byte size of an internal buffer (valid until destroy). */

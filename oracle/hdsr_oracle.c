@@ -488,6 +488,13 @@ static void sort_depth_rank(uint32_t* entries, uint32_t n, const uint32_t* depth
   for (uint32_t i = 0; i < n; ++i) entries[i] = (uint32_t)tmp[i];
 }
 
+typedef struct { uint32_t bucket; uint64_t key; } bucket_entry;
+static int cmp_bucket_entry(const void* a, const void* b) {
+  const bucket_entry* x = (const bucket_entry*)a; const bucket_entry* y = (const bucket_entry*)b;
+  if (x->bucket != y->bucket) return x->bucket < y->bucket ? -1 : 1;
+  return x->key < y->key ? -1 : (x->key > y->key ? 1 : 0);
+}
+
 /* Per-tile log-depth mapping shared by the bucket cascade and the k20 keys
  * (gpu_tile_bucket_sort.wgsl:240-244). */
 typedef struct { float logMin; float bucketScale; float keyScale; } tile_log;
@@ -622,8 +629,8 @@ int orc_render_frame(const float* U, const orc_scene* s, orc_frame* f, int threa
     }
     tile_log tl = tile_log_params(dmin, dmax);
     /* phases 2-4: bucket histogram, prefix, scatter in bucket order;
-     * within a bucket ascending (k20, sortRank). */
-    uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * count);
+     * within a bucket ascending (depth bits, sortRank). */
+    bucket_entry* tmp = (bucket_entry*)malloc(sizeof(bucket_entry) * count);
     uint32_t bucketCounts[NUM_BUCKETS];
     memset(bucketCounts, 0, sizeof(bucketCounts));
     for (uint32_t i = 0; i < count; ++i) {
@@ -632,13 +639,14 @@ int orc_render_frame(const float* U, const orc_scene* s, orc_frame* f, int threa
       uint32_t k = key20_of(ld, tl);
       if ((k >> 13) != b) flags |= ORC_FLAG_BUCKET_KEY_MISMATCH;
       bucketCounts[b]++;
-      tmp[i] = ((uint64_t)b << 55) | ((uint64_t)k << 32) | e[i];
+      tmp[i].bucket = b;
+      tmp[i].key = ((uint64_t)f->depth[e[i]] << 32) | e[i];
     }
-    qsort(tmp, count, sizeof(uint64_t), cmp_u64);
+    qsort(tmp, count, sizeof(bucket_entry), cmp_bucket_entry);
     uint32_t bucketOffsets[NUM_BUCKETS + 1];
     bucketOffsets[0] = 0;
     for (uint32_t b = 0; b < NUM_BUCKETS; ++b) bucketOffsets[b + 1] = bucketOffsets[b] + bucketCounts[b];
-    for (uint32_t i = 0; i < count; ++i) e[i] = (uint32_t)tmp[i];
+    for (uint32_t i = 0; i < count; ++i) e[i] = (uint32_t)tmp[i].key;
     free(tmp);
     /* phase 5: greedy chunk pack (gpu_tile_bucket_sort.wgsl:276-307) */
     uint32_t chunkStart = 0, cur = 0;

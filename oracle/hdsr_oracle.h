@@ -35,9 +35,13 @@
  * (each equals one of the orders the reference can produce):
  *   - small tiles (2..4096 entries): ascending (depth bits, sortRank);
  *   - hot tiles (>4096): entries in bucket order, within a bucket ascending
- *     (k20, sortRank) where k20 is the 20-bit log-depth key (a refinement of
- *     the 128 log buckets: bucket == k20 >> 13); packed greedily into 4096
- *     chunks, each chunk ascending (depth bits, sortRank);
+ *     (depth bits, sortRank) (the reference's atomic cursor leaves it open);
+ *     packed greedily into 4096-entry chunks, each chunk ascending (depth
+ *     bits, sortRank). Because this log is monotone over every positive
+ *     float, the bucket is monotone in depth and the result equals ascending
+ *     (depth bits, sortRank) over the whole tile; tiles with a negative,
+ *     NaN or infinite depth, or a log range below 1e-10, put every entry in
+ *     bucket 0 and reach the same order;
  *   - tile lists and chunk lists in ascending Morton order;
  *   - no caps: the reference's 65,535 large-splat cap, tile-ref budget drop,
  *     overflow-scratch skip and 1,024-chunk cap are reported as flags, not
@@ -123,8 +127,9 @@ void orc_exclusive_scan(const uint32_t* in, uint32_t n, uint32_t* out);
 /* Full canonical frame; returns 0, or -2 when entries_cap/chunk_cap are too
  * small (total_pairs/total_chunks are filled so the caller can retry). */
 int orc_render_frame(const float* U, const orc_scene* s, orc_frame* f, int threads);
-/* Canonical radix output: for each tile in ascending Morton order, its
- * entries in ascending (k20, sortRank). keys[i] = morton<<20 | k20. */
+/* The 20-bit log-depth keys: for each tile in ascending Morton order, its
+ * entries in ascending (k20, sortRank); keys[i] = morton<<20 | k20, where
+ * k20 is the hot-tile bucket mapping scaled to 2^20 (bucket == k20 >> 13). */
 int orc_sorted_keys20(const float* U, uint32_t N, const uint32_t* proj_cache,
                       const uint32_t* depth, uint64_t* keys, uint32_t* values, uint64_t cap,
                       uint64_t* total);

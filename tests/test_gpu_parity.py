@@ -94,6 +94,22 @@ def test_hot_tiles_bucket_cascade(cuda, pkg, orc):
     assert gpu["status"]["chunks"] == ref["total_chunks"]
 
 
+def test_near_plane_splats_negative_depth(cuda, pkg, orc):
+    """Splats between the camera and the near plane have negative NDC depth:
+    their tiles' log-depth range collapses (every entry in bucket 0) and u32
+    depth order puts them after every positive depth; order stays exact."""
+    scene = pkg.workloads.plain_scene(6000, seed=12)
+    cam = pkg.camera.look_from((0.0, 0.0, 4.0))
+    rng = np.random.default_rng(12)
+    # 40 splats 3-8 mm in front of the camera (near plane at 10 mm)
+    scene.positions[:40] = np.stack([rng.uniform(-1e-3, 1e-3, 40), rng.uniform(-1e-3, 1e-3, 40),
+                                     4.0 - rng.uniform(0.003, 0.008, 40)], 1).astype(np.float32)
+    scene.scales[:40] = -9.0
+    g = render_gpu(pkg, scene, cam, 160, 128)
+    gpu, ref = assert_frame_parity(orc, g)
+    assert (ref["depth"].view(np.float32) < 0).any()
+
+
 def test_equal_depth_ties(cuda, pkg, orc):
     n = 5000
     rng = np.random.default_rng(4)

@@ -303,3 +303,39 @@ def test_two_overlapping_splats_front_to_back(orc, pkg, hdsr_lib):
     # pixel (31,31) centre is 0.5 px from the projected centre (32,32) in x and y
     assert px[0] > px[2] > 0
     assert abs((1 - px[3]) - (1 - a0 * np.exp(-0.5 * 0)) * (1 - a1)) < 0.2
+
+
+def test_log_is_monotone(orc):
+    """The hot-tile buckets are monotone in depth only if the log is: check
+    every float in [0.5, 4) (2^24 values, all of the mantissa patterns) and a
+    stride of all positive floats. An exhaustive pass over every positive
+    float (2.1e9 values) found no decreasing step either."""
+    dense = np.arange(0x3F000000, 0x40800000, dtype=np.uint32).view(np.float32)
+    y = orc.logf(dense)
+    assert np.all(y[1:] >= y[:-1])
+    sparse = np.arange(1, 0x7F800000, 97, dtype=np.uint32).view(np.float32)
+    y = orc.logf(sparse)
+    assert np.all(y[1:] >= y[:-1])
+
+
+@pytest.mark.parametrize("near", [False, True])
+def test_every_tile_ends_in_depth_rank_order(orc, pkg, hdsr_lib, near):
+    """Canonical frame: small tiles, hot tiles (bucket cascade) and tiles with
+    negative depths (bucket range collapsed) all end in ascending (depth bits,
+    sortRank) order."""
+    rng = np.random.default_rng(31)
+    scene = _stack_scene(pkg, 9000, pos=(0.72, -0.72, 0.0), depth_jitter=1.0, seed=31)
+    if near:
+        scene.positions[:30] = np.array([0.0, 0.0, 5.0 - 0.004], np.float32) + rng.normal(0, 1e-4, (30, 3)).astype(
+            np.float32)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    u, fr = _uniforms(pkg, 64, 64, scene.count, pkg.camera.look_from((0, 0, 5)))
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order, composite=False)
+    assert f["hot_tiles"] >= 1
+    if near:
+        assert (f["depth"].view(np.float32) < 0).any()
+    for t in np.nonzero(f["tile_counts"])[0]:
+        e = f["tile_entries"][f["tile_offsets"][t]: f["tile_offsets"][t] + f["tile_counts"][t]]
+        key = f["depth"][e].astype(np.uint64) << np.uint64(32) | e.astype(np.uint64)
+        assert np.all(key[1:] > key[:-1])
