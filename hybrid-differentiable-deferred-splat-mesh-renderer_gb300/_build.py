@@ -47,11 +47,12 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     headers = sorted(CSRC.glob("*.cuh")) + [PKG_DIR.parent / "include" / "hdsr.h"]
     sources = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
     exe = nvcc()
+    extra = os.environ.get("HDSR_NVCC_FLAGS", "").split()  # tuning overrides (-D...)
 
     def compile_one(src: Path) -> Path:
         obj = build_dir / (src.stem + ".o")
         if force or _stale(obj, [src] + headers):
-            cmd = [exe, *ARCH, *FLAGS, "-c", str(src), "-o", str(obj)]
+            cmd = [exe, *ARCH, *FLAGS, *extra, "-c", str(src), "-o", str(obj)]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             res = subprocess.run(cmd, capture_output=True, text=True)

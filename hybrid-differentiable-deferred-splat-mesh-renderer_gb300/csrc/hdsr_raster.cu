@@ -80,6 +80,25 @@ __device__ __forceinline__ uint32_t oct_pack_norm(float x, float y, float z) {
   return pack2x16(px, py);
 }
 
+// exp for the rasteriser: a pixel only takes a splat when power > -4, and on
+// (-4, 0] this is hx_expf bit for bit (the scale 2^k, k in [-6, 0], is exact
+// in one multiply); outside that range the value is never used.
+__device__ __forceinline__ float raster_expf(float x) {
+  const float k = rintf(x * 1.44269502162933349609375f);
+  float r = fmaf(k, -0.693145751953125f, x);
+  r = fmaf(k, -1.428606765330187045e-06f, r);
+  float p = 1.98412701e-04f;
+  p = fmaf(p, r, 1.38888892e-03f);
+  p = fmaf(p, r, 8.33333377e-03f);
+  p = fmaf(p, r, 4.16666679e-02f);
+  p = fmaf(p, r, 1.66666672e-01f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  const int ki = (int)k;
+  return p * u2f((uint32_t)(ki + 127) << 23);
+}
+
 __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, const float (*s)[32], int i) {
   const float cx = s[F_CX][i], cy = s[F_CY][i];
   const float ka = s[F_KA][i], kb = s[F_KB][i], kc = s[F_KC][i];
@@ -101,7 +120,7 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
   const bool emits = er != 0.0f || eg != 0.0f || eb != 0.0f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const float g = hx_expf(pw[k]);
+    const float g = raster_expf(pw[k]);
     const float al = mn(0.99f, op * g);
     const float nT = q.T[k] * (1.0f - al);
     const bool valid = (pw[k] > -4.0f) && (al > (1.0f / 255.0f)) && (q.T[k] >= 0.001f);
@@ -153,67 +172,87 @@ __device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, ui
   }
 }
 
-__device__ __forceinline__ void load_batch(const FrameArgs& a, float (*s)[32], uint32_t e, uint32_t lane) {
+// One entry's cache row, as loaded (prefetched a batch ahead).
+struct Row {
+  float4 g;
+  uint4 ap, gb;
+  uint32_t conf, depth;
+};
+
+__device__ __forceinline__ Row load_row(const FrameArgs& a, uint32_t e) {
   const uint32_t r = __ldg(a.entries + e);
-  const float4 g = __ldg(a.geo + r);
-  const uint4 ap = __ldg(a.app + r);
-  const uint4 gb = __ldg(a.gb + r);
-  const uint2 ax = __ldg(a.aux + r);
-  s[F_CX][lane] = g.x;
-  s[F_CY][lane] = g.y;
-  s[F_KA][lane] = g.z * -0.5f;
-  s[F_KB][lane] = -g.w;
-  s[F_KC][lane] = u2f(ap.x) * -0.5f;
-  s[F_OP][lane] = hi16(ap.y);
-  s[F_R][lane] = lo16(ap.z);
-  s[F_G][lane] = hi16(ap.z);
-  s[F_B][lane] = lo16(ap.w);
-  s[F_D][lane] = u2f(__ldg(a.depth + r));
-  s[F_MR][lane] = lo16(gb.x);
-  s[F_MM][lane] = hi16(gb.x);
+  Row w;
+  w.g = __ldg(a.geo + r);
+  w.ap = __ldg(a.app + r);
+  w.gb = __ldg(a.gb + r);
+  w.conf = __ldg(&a.aux[r].y);
+  w.depth = __ldg(a.depth + r);
+  return w;
+}
+
+__device__ __forceinline__ void stage_row(float (*s)[32], const Row& w, uint32_t lane) {
+  s[F_CX][lane] = w.g.x;
+  s[F_CY][lane] = w.g.y;
+  s[F_KA][lane] = w.g.z * -0.5f;
+  s[F_KB][lane] = -w.g.w;
+  s[F_KC][lane] = u2f(w.ap.x) * -0.5f;
+  s[F_OP][lane] = hi16(w.ap.y);
+  s[F_R][lane] = lo16(w.ap.z);
+  s[F_G][lane] = hi16(w.ap.z);
+  s[F_B][lane] = lo16(w.ap.w);
+  s[F_D][lane] = u2f(w.depth);
+  s[F_MR][lane] = lo16(w.gb.x);
+  s[F_MM][lane] = hi16(w.gb.x);
   float nx, ny, nz;
-  oct_decode(lo16(gb.y), hi16(gb.y), nx, ny, nz);
+  oct_decode(lo16(w.gb.y), hi16(w.gb.y), nx, ny, nz);
   s[F_NX][lane] = nx;
   s[F_NY][lane] = ny;
   s[F_NZ][lane] = nz;
-  s[F_CF][lane] = lo16(ax.y);
-  s[F_ER][lane] = lo16(gb.z);
-  s[F_EG][lane] = hi16(gb.z);
-  s[F_EB][lane] = lo16(gb.w);
+  s[F_CF][lane] = lo16(w.conf);
+  s[F_ER][lane] = lo16(w.gb.z);
+  s[F_EG][lane] = hi16(w.gb.z);
+  s[F_EB][lane] = lo16(w.gb.w);
 }
 
-__global__ void __launch_bounds__(kWarps * 32, 5) k_raster(FrameArgs a) {
+// Resident blocks per SM the register budget is fitted to.
+#ifndef HDSR_RASTER_MIN_BLOCKS
+#define HDSR_RASTER_MIN_BLOCKS 4
+#endif
+
+// Work unit: half a tile (rows 0-7 or 8-15), taken from an atomic counter.
+__global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(FrameArgs a) {
   __shared__ float s_pay[kWarps][kFields][32];
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   float (*s)[32] = s_pay[warp];
+  const uint32_t items = 2u * a.tile_count;
   for (;;) {
-    uint32_t tile_idx = 0;
-    if (lane == 0) tile_idx = atomicAdd(a.ctl + kCtlRasterTile, 1u);
-    tile_idx = __shfl_sync(0xFFFFFFFFu, tile_idx, 0);
-    if (tile_idx >= a.tile_count) break;
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(a.ctl + kCtlRasterTile, 1u);
+    item = __shfl_sync(0xFFFFFFFFu, item, 0);
+    if (item >= items) break;
+    const uint32_t tile_idx = item >> 1, half = item & 1u;
     const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
     const uint32_t t = morton(tx, ty);
     const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
     const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
-    const float p00x = (float)bx + 0.5f;
-#pragma unroll 1
-    for (uint32_t half = 0; half < 2; ++half) {
-      const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
-      const float p00y = (float)by + 0.5f;
-      Quad q;
-      quad_init(q);
-      for (uint32_t b = 0; b < count; b += 32u) {
-        const uint32_t n = count - b < 32u ? count - b : 32u;
-        if (lane < n) load_batch(a, s, start + b + lane, lane);
-        __syncwarp();
-        for (uint32_t i = 0; i < n; ++i)
-          if (!q.done) quad_splat(q, p00x, p00y, s, (int)i);
-        __syncwarp();
-        if (__all_sync(0xFFFFFFFFu, q.done)) break;
-      }
-      quad_store(a, q, bx, by);
+    const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
+    const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
+    Quad q;
+    quad_init(q);
+    Row next;
+    if (lane < count) next = load_row(a, start + lane);
+    for (uint32_t b = 0; b < count; b += 32u) {
+      const uint32_t n = count - b < 32u ? count - b : 32u;
+      if (lane < n) stage_row(s, next, lane);
+      __syncwarp();
+      if (b + 32u + lane < count) next = load_row(a, start + b + 32u + lane);  // in flight during the batch
+      for (uint32_t i = 0; i < n; ++i)
+        if (!q.done) quad_splat(q, p00x, p00y, s, (int)i);
+      __syncwarp();
+      if (__all_sync(0xFFFFFFFFu, q.done)) break;
     }
+    quad_store(a, q, bx, by);
   }
 }
 
@@ -221,7 +260,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_raster(FrameArgs a) {
 
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s) {
   // persistent warps: enough blocks to fill every SM, tiles from a counter
-  const uint32_t want = (a.tile_count + kWarps - 1) / kWarps;
+  const uint32_t want = (2u * a.tile_count + kWarps - 1) / kWarps;
   const uint32_t cap = (uint32_t)a.num_sms * 8u;
   const uint32_t blocks = want < cap ? want : cap;
   if (blocks) k_raster<<<blocks, kWarps * 32, 0, s>>>(a);
