@@ -134,20 +134,25 @@ def setup_frame(pkg, wl, device_index=0):
     return dict(packed=packed, plan=plan, u=u, order=order, bufs=bufs, color=color, gb=gb, res=res, stats=st)
 
 
-def pass_bytes(name: str, N: int, P: int, px: int, sh_floats: int) -> float | None:
-    """Algorithmic HBM bytes of one launch of a pass (None: not HBM-bound)."""
+def pass_bytes(name: str, N: int, P: int, Q: int, S: int, sh_floats: int) -> float | None:
+    """Algorithmic HBM bytes of one pass of the frame (None: not HBM-bound).
+
+    N splats, P (tile, splat) pairs, Q superblock list entries, S segments."""
     if name == "project":
-        return N * (4 + 12 + 12 + 16 + 4 + 4 + 4 * sh_floats + 16 + 16 + 16 + 8 + 4 + 4)
-    if name == "count":
-        return N * (8 + 4 + 4)
-    if name == "scan_pairs":
-        return N * 8
+        # indices, position, scale, rotation, opacity, material, SH in; geo,
+        # app, gb, aux, depth, ntiles, nsb, depth key out
+        return N * (4 + 12 + 12 + 16 + 4 + 4 + 4 * sh_floats + 16 + 16 + 16 + 8 + 4 + 4 + 4 + 8)
+    if name == "tile_counts":
+        return N * 8  # tile boxes
     if name == "depth_sort":
         return 4 * (N * 8 + N * 16)  # 4 passes: upsweep read + downsweep read/write
-    if name == "emit_keys":
-        return N * 20 + P * 8
-    if name.startswith("tile_sort"):
-        return P * 8 + P * 16  # upsweep read + downsweep read/write (last pass writes 4 B)
+    if name == "superblock_lists":
+        # scan: order + gathered counts in, offsets out; emit: order, boxes,
+        # offsets in, Q keys out; one radix pass: Q keys read twice, written once
+        return N * 12 + N * 16 + Q * 8 + Q * 24
+    if name == "tile_entries":
+        # count and scatter read the Q keys; segment tables 3x; P entries out
+        return Q * 16 + S * 256 * 3 + P * 4
     return None
 
 
@@ -206,14 +211,14 @@ def run_ours(args, rank, world, local):
     sh_floats = 6 + 3 * ((wl.scene.sh_degree + 1) ** 2 - 1)
     mean_pass = {k: statistics.mean(v) for k, v in passes.items()}
     frame_ms = statistics.mean(times)
-    hbm_passes = {k: v for k, v in mean_pass.items() if pass_bytes(k, N, P, plan.viewport_width * plan.viewport_height,
-                                                                  sh_floats)}
+    Q, S = int(st["superblock_entries"]), int(st["segments"])
+    hbm_passes = {k: v for k, v in mean_pass.items() if pass_bytes(k, N, P, Q, S, sh_floats)}
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     dom = max(hbm_passes, key=hbm_passes.get) if hbm_passes else None
     roofline = None
     if dom:
-        b = pass_bytes(dom, N, P, 0, sh_floats)
+        b = pass_bytes(dom, N, P, Q, S, sh_floats)
         ach = b / (mean_pass[dom] / 1000.0) / 1e9
         traffic = load_traffic(dom)
         roofline = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",

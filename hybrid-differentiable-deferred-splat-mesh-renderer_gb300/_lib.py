@@ -79,8 +79,8 @@ class OutputViews(ctypes.Structure):
 
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_pairs", c_uint64), ("pair_capacity", c_uint64), ("visible_splats", c_uint32),
-                ("_reserved0", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
-                ("device_flags", c_uint32), ("_reserved1", c_uint32)]
+                ("superblock_entries", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
+                ("device_flags", c_uint32), ("segments", c_uint32)]
 
 
 class HdsrError(RuntimeError):

@@ -19,8 +19,8 @@ using namespace hdsr;
 namespace {
 constexpr uint32_t kMaxProfiledPasses = 24;
 // names of the profiled passes, indexed by the ids recorded in encode()
-const char* const kPassNames[] = {"upload_uniforms", "frame_init", "project", "count", "scan_pairs",
-                                  "scan_tiles", "depth_sort", "emit_keys", "tile_sort_0", "tile_sort_1",
+const char* const kPassNames[] = {"upload_uniforms", "frame_init", "project", "tile_counts", "unused_4",
+                                  "scan_tiles", "depth_sort", "superblock_lists", "tile_entries", "unused_9",
                                   "unused_10", "unused_11", "unused_12", "unused_13", "unused_14",
                                   "unused_15", "unused_16", "raster"};
 constexpr uint32_t kNumPassNames = sizeof(kPassNames) / sizeof(kPassNames[0]);
@@ -148,24 +148,21 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   a.M = M;
   a.tile_count = plan->tile_count;
   a.rank_bits = ceil_log2(N > 1 ? N : 2);
-  a.morton_bits = ceil_log2(M > 1 ? M : 2);
-  if (a.rank_bits + a.morton_bits > 64u || a.rank_bits > 32u) { delete h; return HDSR_ERR_UNSUPPORTED; }
-  a.tile_passes = (a.morton_bits + kRadixBits - 1u) / kRadixBits;
-  for (uint32_t p = 0, sh = a.rank_bits, left = a.morton_bits; p < a.tile_passes; ++p) {
-    const uint32_t w = (left + (a.tile_passes - p) - 1u) / (a.tile_passes - p);  // widest digits first
-    a.tile_shift[p] = sh;
-    a.tile_bits[p] = w;
-    sh += w;
-    left -= w;
-  }
+  if (a.rank_bits > 24u) { delete h; return HDSR_ERR_UNSUPPORTED; }  // sortRank packs into 24 key bits
+  // superblocks of 8x8 tiles (<= 32 x 32 of them)
+  a.sb_shift = kSbShift;
+  a.sb_cols = (plan->tile_columns + 7u) >> kSbShift;
+  a.sb_rows = (plan->tile_rows + 7u) >> kSbShift;
+  a.num_sb = a.sb_cols * a.sb_rows;
+  a.sb_bits = a.num_sb > 1u ? ceil_log2(a.num_sb) : 1u;
   a.cap = cap;
   a.num_sms = sms > 0 ? sms : 1;
   a.color_f32 = h->cfg.color_format == HDSR_COLOR_RGBA32F;
   a.log_keys = (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) ? 1u : 0u;
-  {
-    const uint64_t most = cap > N ? cap : N;
-    a.radix_tiles_cap = (uint32_t)((most + kRadixTile - 1) / kRadixTile);
-  }
+  const uint64_t sb_cap = (uint64_t)N * 9u;  // a tile box (<= 17 tiles a side) meets <= 3x3 superblocks
+  a.sb_cap = sb_cap;
+  a.seg_cap = (uint32_t)((sb_cap + kSegEntries - 1u) / kSegEntries + a.num_sb);
+  a.radix_tiles_cap = (uint32_t)((sb_cap + kRadixTile - 1) / kRadixTile + 1);
   const uint64_t scan_tiles_n = (N + kScanTile - 1) / kScanTile + 1;
   const uint64_t scan_tiles_m = (M + kScanTile - 1) / kScanTile + 1;
   hdsr_status s = HDSR_OK;
@@ -182,14 +179,20 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.dkeys_a, N, "depth_keys_a");
   ALLOC(a.dkeys_b, N, "depth_keys_b");
   ALLOC(a.order, N, "depth_order");
-  ALLOC(a.pair_off, N, "pair_off");
+  ALLOC(a.nsb, N, "superblock_counts");
+  ALLOC(a.sb_off, N, "superblock_offsets");
+  ALLOC(a.sbk_a, sb_cap, "superblock_keys_a");
+  ALLOC(a.sbk_b, sb_cap, "superblock_keys_b");
+  ALLOC(a.tile_diff, (uint64_t)(plan->tile_columns + 1) * (plan->tile_rows + 1), "tile_diff");
+  ALLOC(a.sb_diff, (uint64_t)(a.sb_cols + 1) * (a.sb_rows + 1), "superblock_diff");
+  ALLOC(a.sb_start, (uint64_t)a.num_sb + 1u, "superblock_starts");
+  ALLOC(a.seg_first, (uint64_t)a.num_sb + 1u, "segment_firsts");
+  ALLOC(a.seg_cnt, (uint64_t)a.seg_cap * kSbTiles, "segment_counts");
   ALLOC(a.tile_cnt, M, "tile_counts");
   ALLOC(a.tile_dmin, M, "tile_dmin");
   ALLOC(a.tile_dmax, M, "tile_dmax");
   ALLOC(a.tile_off, M, "tile_offsets");
   ALLOC(a.tile_log, M, "tile_log");
-  ALLOC(a.pairs_a, cap, "pairs_a");
-  ALLOC(a.pairs_b, cap, "pairs_b");
   ALLOC(a.entries, cap, "tile_entries");
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
   ALLOC(a.tile_digits, (uint64_t)a.radix_tiles_cap * kRadixBins, "tile_digits");
@@ -200,6 +203,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
 #undef ALLOC
   if (s != HDSR_OK) { free_all(h); delete h; return s; }
   a.U = U;
+  a.sbk_sorted = a.sb_bits > kRadixBits ? a.sbk_a : a.sbk_b;  // where the last superblock pass writes
   // status words start at epoch 0, which no frame uses
   e = cudaMemset(a.scan_status_n, 0, scan_tiles_n * 8);
   if (e == cudaSuccess) e = cudaMemset(a.scan_status_m, 0, scan_tiles_m * 8);
@@ -356,7 +360,8 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
     mark(h, s, 1);
     if ((e = launch_project(a, s)) != cudaSuccess) return cuda_fail(h, e, "project");
     mark(h, s, 2);
-    if ((e = launch_count(a, s)) != cudaSuccess) return cuda_fail(h, e, "count");
+    if ((e = launch_tile_counts(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_counts");
+    if (a.log_keys && (e = launch_depth_range(a, s)) != cudaSuccess) return cuda_fail(h, e, "depth_range");
     mark(h, s, 3);
     if ((e = launch_scan_tiles(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
     mark(h, s, 5);
@@ -378,29 +383,31 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
         return cuda_fail(h, e, "depth_sort");
     }
     mark(h, s, 6);
-    if ((e = launch_scan_pairs(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_pairs");
-    mark(h, s, 4);
-    if ((e = launch_emit(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit");
-    mark(h, s, 7);
-    // pairs: stable passes over the Morton tile bits -> tile entries
-    RadixJob tj = dj;
-    tj.count = a.ctl + kCtlPairsLo;
-    tj.out_low = a.entries;
-    tj.low_mask = (1ull << a.rank_bits) - 1ull;
-    for (uint32_t p = 0; p < a.tile_passes; ++p) {
-      tj.in = (p & 1u) ? a.pairs_b : a.pairs_a;
-      tj.out = (p & 1u) ? a.pairs_a : a.pairs_b;
-      tj.shift = a.tile_shift[p];
-      tj.bits = a.tile_bits[p];
-      if ((e = launch_radix_pass(tj, p + 1 == a.tile_passes, a.num_sms, s)) != cudaSuccess)
-        return cuda_fail(h, e, "tile_sort");
-      mark(h, s, 8 + p);
+    // superblock lists in depth order, sorted by superblock (stable)
+    if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
+    if ((e = launch_emit_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit_superblocks");
+    RadixJob sj = dj;
+    sj.count = a.ctl + kCtlSbPairs;
+    sj.out_low = nullptr;
+    const uint32_t sb_passes = a.sb_bits > kRadixBits ? 2u : 1u;
+    for (uint32_t p = 0; p < sb_passes; ++p) {
+      sj.in = (p & 1u) ? a.sbk_b : a.sbk_a;
+      sj.out = (p & 1u) ? nullptr : a.sbk_b;
+      sj.out_keys = (p & 1u) ? a.sbk_a : a.sbk_b;
+      sj.shift = kSbKeyShift + kRadixBits * p;
+      sj.bits = p == 0 ? (a.sb_bits < kRadixBits ? a.sb_bits : kRadixBits) : a.sb_bits - kRadixBits;
+      if ((e = launch_radix_pass(sj, p + 1 == sb_passes, a.num_sms, s)) != cudaSuccess)
+        return cuda_fail(h, e, "superblock_sort");
     }
+    mark(h, s, 7);
+    if ((e = launch_tile_entries(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_entries");
+    mark(h, s, 8);
     if (a.log_keys) {
       if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
-      h->launches += 1;
+      h->launches += 2;
     }
-    h->launches += 1 + 3 * n_splat_launch + 2 + 4 * (kDepthPasses + a.tile_passes);
+    h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 4 * kDepthPasses + 1 + n_splat_launch +
+                   4 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
   }
   if (!full) {
     // composite-only reuses the frame's entries; the raster's tile counter
@@ -436,12 +443,16 @@ hdsr_status hdsr_query_status(hdsr_compositor* h, hdsr_frame_stats* st) {
     st->hot_tiles = ctl[kCtlHotTiles];
     st->chunks = ctl[kCtlChunks];
     st->device_flags = ctl[kCtlFlags];
+    st->superblock_entries = ctl[kCtlSbPairs];
+    st->segments = ctl[kCtlSegments];
   }
   if (ctl[kCtlFlags] & HDSR_DEV_OVERFLOW) {
     h->sorted_valid = false;
     return fail(h, HDSR_ERR_OVERFLOW, "frame needs more (tile, splat) pairs than pair_capacity");
   }
   if (ctl[kCtlFlags] & HDSR_DEV_TIMEOUT) return fail(h, HDSR_ERR_TIMEOUT, "a device-side wait gave up");
+  if (ctl[kCtlFlags] & HDSR_DEV_COUNT_MISMATCH)
+    return fail(h, HDSR_ERR_CUDA, "internal check failed: tile counts and superblock lists disagree");
   return HDSR_OK;
 }
 
@@ -463,7 +474,7 @@ hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, u
     case HDSR_BUF_SORTED_KEYS:
       if (!a.sorted_keys) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_KEEP_SORTED_KEYS");
       *ptr = a.sorted_keys; *bytes = cap * 8; break;
-    case HDSR_BUF_PAIR_OFFSETS: *ptr = a.pair_off; *bytes = N * 4; break;
+    case HDSR_BUF_PAIR_OFFSETS: *ptr = a.sb_off; *bytes = N * 4; break;
     case HDSR_BUF_DEPTH_ORDER: *ptr = a.order; *bytes = N * 4; break;
     default: return fail(h, HDSR_ERR_INVALID_ARG, "unknown buffer id");
   }

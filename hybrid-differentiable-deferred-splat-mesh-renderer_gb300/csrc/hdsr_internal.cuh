@@ -15,6 +15,8 @@ enum Ctl : int {
   kCtlPairsLo = 2,     // P, total (tile, splat) pairs of the frame
   kCtlPairsHi = 3,
   kCtlSplats = 4,      // N, the depth sort's key count (constant per handle)
+  kCtlSbPairs = 10,    // Q, (superblock, splat) list entries of the frame
+  kCtlSegments = 11,   // 256-entry segments of the superblock lists
   kCtlHotTiles = 5,
   kCtlChunks = 6,
   kCtlVisible = 7,
@@ -27,7 +29,15 @@ enum Ctl : int {
 constexpr uint32_t kRadixBits = 8;               // widest digit
 constexpr uint32_t kRadixBins = 1u << kRadixBits;
 constexpr uint32_t kDepthPasses = 4;             // 32 depth bits
-constexpr uint32_t kMaxTilePasses = 2;           // <= 16 Morton bits
+
+// Superblocks: squares of 8x8 tiles. A superblock list entry is
+// superblock << 36 | local rect << 24 | sortRank, the local rect being the
+// splat's tile box clipped to the superblock (3 bits per edge: x0, x1, y0, y1).
+constexpr uint32_t kSbShift = 3;
+constexpr uint32_t kSbTiles = 64;
+constexpr uint32_t kSbKeyShift = 36;
+constexpr uint32_t kSegEntries = 256;            // list entries per segment
+constexpr uint32_t kMaxSuperblocks = 1024;       // 255 tiles a side -> <= 32 x 32
 
 // One LSD radix pass over u64 keys: digit = (key >> shift) & (2^bits - 1).
 struct RadixJob {
@@ -62,11 +72,12 @@ struct FrameArgs {
   uint32_t sh_degree;
   // plan
   uint32_t W, H, cols, rows, M, tile_count;
-  uint32_t rank_bits;             // low key bits holding sortRank
-  uint32_t morton_bits;           // tile bits of the pair keys
-  uint32_t tile_passes;           // radix passes over the tile bits
-  uint32_t tile_shift[kMaxTilePasses];
-  uint32_t tile_bits[kMaxTilePasses];
+  uint32_t rank_bits;             // bits of a sortRank (<= 24)
+  uint32_t sb_shift;              // superblock side = 1 << sb_shift tiles
+  uint32_t sb_cols, sb_rows, num_sb;
+  uint32_t sb_bits;               // radix digits of the superblock index
+  uint64_t sb_cap;                // capacity of the superblock lists
+  uint32_t seg_cap;               // capacity of the segment tables
   uint64_t cap;                   // pair capacity
   uint32_t log_keys;              // compute per-tile depth range + 20-bit keys
   // projection cache (SoA) and per-splat data
@@ -79,16 +90,23 @@ struct FrameArgs {
   unsigned long long* dkeys_a;    // depth << 32 | sortRank, per sortRank
   unsigned long long* dkeys_b;
   uint32_t* order;                // sortRanks in ascending (depth, sortRank)
-  uint32_t* pair_off;             // exclusive prefix of ntiles in that order
+  uint32_t* nsb;                  // superblocks touched per sortRank
+  uint32_t* sb_off;               // exclusive prefix of nsb in depth order
+  unsigned long long* sbk_a;      // superblock list entries in depth order (see kSbKeyShift)
+  unsigned long long* sbk_b;
+  const unsigned long long* sbk_sorted;  // sbk_a or sbk_b: the entries stably sorted by superblock
+  int* tile_diff;                 // (cols+1) x (rows+1) 2D difference grid of tile counts
+  int* sb_diff;                   // (sb_cols+1) x (sb_rows+1) grid of superblock list lengths
+  uint32_t* sb_start;             // num_sb + 1: first entry of each superblock's list
+  uint32_t* seg_first;            // num_sb + 1: first segment of each superblock's list
+  uint32_t* seg_cnt;              // kSbTiles per segment: tile counts, then entry bases
   // tiles
   uint32_t* tile_cnt;
   uint32_t* tile_dmin;
   uint32_t* tile_dmax;
   uint32_t* tile_off;
   float2* tile_log;               // (logMin, keyScale)
-  // pairs and entries
-  unsigned long long* pairs_a;
-  unsigned long long* pairs_b;
+  // entries
   unsigned long long* sorted_keys;  // optional: tile, 20-bit log-depth key, sortRank per entry
   uint32_t* entries;              // final per-tile order (sortRank)
   // radix scratch (shared by every pass, passes run in stream order)
@@ -124,10 +142,12 @@ HDSR_HD unsigned long long make_status(uint32_t epoch, unsigned long long flag, 
 // launchers (each returns cudaGetLastError() of its launches)
 cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_project(const FrameArgs& a, cudaStream_t s);
-cudaError_t launch_count(const FrameArgs& a, cudaStream_t s);
-cudaError_t launch_scan_pairs(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_tile_counts(const FrameArgs& a, cudaStream_t s);   // 2 launches
+cudaError_t launch_depth_range(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
-cudaError_t launch_emit(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_emit_sb(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
 cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 4 launches
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);

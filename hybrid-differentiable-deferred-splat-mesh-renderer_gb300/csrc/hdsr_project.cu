@@ -2,13 +2,19 @@
 //
 // k_project follows gpu_project_splats.wgsl:112-358 step by step (one thread
 // per sortRank) and writes the reference's 14-word projection cache as four
-// SoA streams plus the f32 depth word, and the splat's depth sort key. k_count
-// is count_tile_refs (gpu_tile_splat_composite.wgsl:65-84); when the 20-bit
-// log-depth keys are requested it also keeps the per-tile depth min/max of
-// the hot-tile bucket mapping (gpu_tile_bucket_sort.wgsl:232-237). k_emit
-// writes one 64-bit (tile, sortRank) key per pair, visiting the splats in
-// ascending (depth, sortRank) order; it replaces scatter_tile_refs and the
-// cooperative large-splat scatter (gpu_large_splat_scatter.wgsl).
+// SoA streams plus the f32 depth word, the splat's depth sort key and the
+// number of superblocks (square groups of tiles) its tile box touches.
+// Tile counts (count_tile_refs, gpu_tile_splat_composite.wgsl:65-84) come
+// from a 2D difference grid: each splat adds its tile box with four
+// additions, a 2D prefix sum gives every tile's count; a second grid at
+// superblock (8x8 tiles) granularity gives the length of every superblock's
+// list and so the lists' starts and their 256-entry segments. k_emit_sb
+// lists each splat, in ascending (depth, sortRank) order, once per
+// superblock it touches, with its tile box clipped to the superblock; the
+// lists replace scatter_tile_refs and the cooperative large-splat scatter
+// (gpu_large_splat_scatter.wgsl). When the 20-bit log-depth keys are
+// requested, k_depth_range keeps the per-tile depth min/max of the hot-tile
+// bucket mapping (gpu_tile_bucket_sort.wgsl:232-237).
 #include "hdsr_internal.cuh"
 
 namespace hdsr {
@@ -68,12 +74,15 @@ __global__ void k_frame_init(FrameArgs a) {
     a.tile_dmin[i] = 0xFFFFFFFFu;
     a.tile_dmax[i] = 0u;
   }
+  if (i < (a.cols + 1u) * (a.rows + 1u)) a.tile_diff[i] = 0;
+  if (i < (a.sb_cols + 1u) * (a.sb_rows + 1u)) a.sb_diff[i] = 0;
 }
 
 __device__ __forceinline__ void write_invisible(const FrameArgs& a, uint32_t r) {
   a.aux[r] = make_uint2(kSentinel, 0u);
   a.depth[r] = kSentinel;
   a.ntiles[r] = 0u;
+  a.nsb[r] = 0u;
   a.dkeys_a[r] = ((unsigned long long)kSentinel << 32) | r;
 }
 
@@ -250,28 +259,147 @@ __global__ void __launch_bounds__(256) k_project(FrameArgs a) {
   a.aux[r] = make_uint2(box, pack2x16(conf, 0.0f));
   a.depth[r] = f2u(depthNdc);
   a.ntiles[r] = (t1x - t0x + 1u) * (t1y - t0y + 1u);
+  a.nsb[r] = ((t1x >> a.sb_shift) - (t0x >> a.sb_shift) + 1u) * ((t1y >> a.sb_shift) - (t0y >> a.sb_shift) + 1u);
   a.dkeys_a[r] = ((unsigned long long)f2u(depthNdc) << 32) | r;
 }
 
-// count_tile_refs + per-tile depth min/max. Splats above the reference's
-// large-splat threshold (16 tiles) are spread over the warp so one lane does
-// not serialise up to 17x17 tiles. Templated on the table the atomics go to:
-// global memory, or a per-block copy in shared memory (privatised tables,
-// flushed once per block) when the M-tile tables fit there.
-template <bool MINMAX>
-struct GlobalTables {
-  uint32_t *cnt, *dmin, *dmax;
-  __device__ void add(uint32_t t, uint32_t d) const {
-    atomicAdd(cnt + t, 1u);
-    if (MINMAX) {
-      atomicMin(dmin + t, d);
-      atomicMax(dmax + t, d);
+// Tile counts: each visible splat adds +1 over its tile box to a 2D
+// difference grid (four corner updates); a privatised copy per block lives
+// in shared memory when the grid fits there.
+__device__ __forceinline__ void diff_add(int* g, uint32_t stride, uint32_t box) {
+  const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = ((box >> 16) & 0xFFu) + 1u, y1 = (box >> 24) + 1u;
+  atomicAdd(g + y0 * stride + x0, 1);
+  atomicAdd(g + y0 * stride + x1, -1);
+  atomicAdd(g + y1 * stride + x0, -1);
+  atomicAdd(g + y1 * stride + x1, 1);
+}
+
+// The superblock box of a tile box.
+__device__ __forceinline__ uint32_t sb_box(uint32_t box) {
+  const uint32_t x0 = (box & 0xFFu) >> kSbShift, y0 = ((box >> 8) & 0xFFu) >> kSbShift;
+  const uint32_t x1 = ((box >> 16) & 0xFFu) >> kSbShift, y1 = (box >> 24) >> kSbShift;
+  return x0 | (y0 << 8) | (x1 << 16) | (y1 << 24);
+}
+
+constexpr uint32_t kDiffSmemMaxWords = (200u * 1024u) / 4u;
+constexpr uint32_t kSbDiffWords = 33u * 33u;
+
+__global__ void __launch_bounds__(1024, 1) k_tile_diff_smem(FrameArgs a) {
+  extern __shared__ int s_diff[];
+  const uint32_t stride = a.cols + 1u, n = stride * (a.rows + 1u);
+  const uint32_t sstride = a.sb_cols + 1u, sn = sstride * (a.sb_rows + 1u);
+  int* s_sb = s_diff + n;
+  for (uint32_t i = threadIdx.x; i < n + sn; i += blockDim.x) s_diff[i] = 0;
+  __syncthreads();
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < a.N; r += gridDim.x * blockDim.x) {
+    const uint32_t box = a.aux[r].x;
+    if (box != kSentinel) {
+      diff_add(s_diff, stride, box);
+      diff_add(s_sb, sstride, sb_box(box));
     }
   }
-};
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (s_diff[i]) atomicAdd(a.tile_diff + i, s_diff[i]);
+  for (uint32_t i = threadIdx.x; i < sn; i += blockDim.x)
+    if (s_sb[i]) atomicAdd(a.sb_diff + i, s_sb[i]);
+}
 
-template <class Tables>
-__device__ __forceinline__ void count_splats(const FrameArgs& a, const Tables& tb, uint32_t r) {
+__global__ void __launch_bounds__(256) k_tile_diff(FrameArgs a) {
+  __shared__ int s_sb[kSbDiffWords];
+  const uint32_t sstride = a.sb_cols + 1u, sn = sstride * (a.sb_rows + 1u);
+  for (uint32_t i = threadIdx.x; i < sn; i += blockDim.x) s_sb[i] = 0;
+  __syncthreads();
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < a.N) {
+    const uint32_t box = a.aux[r].x;
+    if (box != kSentinel) {
+      diff_add(a.tile_diff, a.cols + 1u, box);
+      diff_add(s_sb, sstride, sb_box(box));
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < sn; i += blockDim.x)
+    if (s_sb[i]) atomicAdd(a.sb_diff + i, s_sb[i]);
+}
+
+// 2D inclusive prefix of the difference grid: rows, then columns; writes the
+// count of tile (x, y) to tile_cnt[morton(x, y)]. The same on the superblock
+// grid gives every superblock's list length; one exclusive block scan of
+// (length, segments) turns those into list starts and the segment plan.
+// One block of 1024 threads (>= kMaxSuperblocks).
+__global__ void __launch_bounds__(1024) k_tile_prefix(FrameArgs a) {
+  __shared__ unsigned long long s_warp[32];
+  const uint32_t stride = a.cols + 1u;
+  for (uint32_t y = threadIdx.x; y < a.rows; y += blockDim.x) {
+    int run = 0;
+    int* row = a.tile_diff + y * stride;
+    for (uint32_t x = 0; x < a.cols; ++x) {
+      run += row[x];
+      row[x] = run;
+    }
+  }
+  __syncthreads();
+  for (uint32_t x = threadIdx.x; x < a.cols; x += blockDim.x) {
+    int run = 0;
+    for (uint32_t y = 0; y < a.rows; ++y) {
+      run += a.tile_diff[y * stride + x];
+      a.tile_cnt[morton(x, y)] = (uint32_t)run;
+    }
+  }
+  // superblock list lengths
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t ss = a.sb_cols + 1u;
+  if (tid < a.sb_rows) {
+    int run = 0;
+    for (uint32_t x = 0; x < a.sb_cols; ++x) {
+      run += a.sb_diff[tid * ss + x];
+      a.sb_diff[tid * ss + x] = run;
+    }
+  }
+  __syncthreads();
+  if (tid < a.sb_cols) {
+    int run = 0;
+    for (uint32_t y = 0; y < a.sb_rows; ++y) {
+      run += a.sb_diff[y * ss + tid];
+      a.sb_diff[y * ss + tid] = run;
+    }
+  }
+  __syncthreads();
+  // exclusive scan of (segments << 32 | length) over the superblocks
+  unsigned long long v = 0ull;
+  if (tid < a.num_sb) {
+    const uint32_t len = (uint32_t)a.sb_diff[(tid / a.sb_cols) * ss + tid % a.sb_cols];
+    v = ((unsigned long long)((len + kSegEntries - 1u) / kSegEntries) << 32) | len;
+  }
+  unsigned long long inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= (uint32_t)o) inc += t;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  unsigned long long off = 0ull;
+  for (uint32_t w = 0; w < warp; ++w) off += s_warp[w];
+  const unsigned long long ex = off + inc - v;
+  if (tid < a.num_sb) {
+    a.sb_start[tid] = (uint32_t)ex;
+    a.seg_first[tid] = (uint32_t)(ex >> 32);
+  }
+  if (tid + 1u == a.num_sb) {  // totals
+    const unsigned long long all = ex + v;
+    a.sb_start[a.num_sb] = (uint32_t)all;
+    a.seg_first[a.num_sb] = (uint32_t)(all >> 32);
+    a.ctl[kCtlSegments] = (uint32_t)(all >> 32);
+    if ((uint32_t)all > a.sb_cap || (uint32_t)(all >> 32) > a.seg_cap) atomicOr(a.ctl + kCtlFlags, 0x1u);
+  }
+}
+
+// Per-tile depth min/max (verification mode only): one thread per splat,
+// splats above 16 tiles spread over the warp.
+__global__ void __launch_bounds__(256) k_depth_range(FrameArgs a) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t box = kSentinel, d = 0u, n = 0u;
   if (r < a.N) {
@@ -279,11 +407,12 @@ __device__ __forceinline__ void count_splats(const FrameArgs& a, const Tables& t
     if (box != kSentinel) { d = a.depth[r]; n = a.ntiles[r]; }
   }
   if (box != kSentinel && n <= kLargeSplatTiles) {
-    uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
+    const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
     for (uint32_t ty = y0; ty <= y1; ++ty)
       for (uint32_t tx = x0; tx <= x1; ++tx) {
-        uint32_t t = morton(tx, ty);
-        if (t < a.M) tb.add(t, d);
+        const uint32_t t = morton(tx, ty);
+        atomicMin(a.tile_dmin + t, d);
+        atomicMax(a.tile_dmax + t, d);
       }
   }
   uint32_t large = __ballot_sync(0xFFFFFFFFu, box != kSentinel && n > kLargeSplatTiles);
@@ -296,87 +425,36 @@ __device__ __forceinline__ void count_splats(const FrameArgs& a, const Tables& t
     const uint32_t x0 = lb & 0xFFu, y0 = (lb >> 8) & 0xFFu, x1 = (lb >> 16) & 0xFFu;
     const uint32_t spanX = x1 - x0 + 1u;
     for (uint32_t i = lane; i < ln; i += 32u) {
-      uint32_t t = morton(x0 + i % spanX, y0 + i / spanX);
-      if (t < a.M) tb.add(t, ld);
+      const uint32_t t = morton(x0 + i % spanX, y0 + i / spanX);
+      atomicMin(a.tile_dmin + t, ld);
+      atomicMax(a.tile_dmax + t, ld);
     }
   }
 }
 
-template <bool MINMAX>
-__global__ void __launch_bounds__(256) k_count(FrameArgs a) {
-  count_splats(a, GlobalTables<MINMAX>{a.tile_cnt, a.tile_dmin, a.tile_dmax}, blockIdx.x * blockDim.x + threadIdx.x);
-}
-
-constexpr uint32_t kCountSmemThreads = 1024;
-
-template <bool MINMAX>
-__global__ void __launch_bounds__(kCountSmemThreads, 1) k_count_smem(FrameArgs a) {
-  extern __shared__ uint32_t s_tab[];
-  const uint32_t M = a.M;
-  GlobalTables<MINMAX> tb{s_tab, s_tab + M, s_tab + 2 * M};
-  for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
-    tb.cnt[i] = 0u;
-    if (MINMAX) {
-      tb.dmin[i] = 0xFFFFFFFFu;
-      tb.dmax[i] = 0u;
-    }
-  }
-  __syncthreads();
-  for (uint32_t base = blockIdx.x * blockDim.x; base < a.N; base += gridDim.x * blockDim.x)
-    count_splats(a, tb, base + threadIdx.x);
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
-    const uint32_t c = tb.cnt[i];
-    if (c) {
-      atomicAdd(a.tile_cnt + i, c);
-      if (MINMAX) {
-        atomicMin(a.tile_dmin + i, tb.dmin[i]);
-        atomicMax(a.tile_dmax + i, tb.dmax[i]);
-      }
-    }
-  }
-}
-
-// Key emission: key = tile << R | sortRank, splats visited in ascending
-// (depth, sortRank) order (`order`, from the depth sort) at the prefix
-// offsets of their tile counts in that order. A warp emits the pairs of its
-// 32 consecutive splats as one contiguous range, lane l writing pair
-// begin + l + 32k (coalesced stores); each lane finds the splat owning its
-// pair by a binary search over the warp's prefix offsets.
-__global__ void __launch_bounds__(256) k_emit(FrameArgs a) {
-  if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t P = a.ctl[kCtlPairsLo];
+// Superblock lists: splat i of the depth order writes one entry per
+// superblock its tile box touches, superblock << 36 | local rect << 24 |
+// sortRank, at the prefix offsets of the superblock counts in depth order.
+__global__ void __launch_bounds__(256) k_emit_sb(FrameArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t lane = threadIdx.x & 31u;
-  uint32_t box = kSentinel, n = 0u, base = P, r = 0u;
-  if (i < a.N) {
-    r = a.order[i];
-    base = a.pair_off[i];
-    box = a.aux[r].x;
-    if (box != kSentinel) n = a.ntiles[r];
-  }
-  const uint32_t R = a.rank_bits;
-  const uint32_t begin = __shfl_sync(0xFFFFFFFFu, base, 0);
-  const uint32_t end = __shfl_sync(0xFFFFFFFFu, base + n, 31);
-  for (uint32_t p0 = begin; p0 < end; p0 += 32u) {
-    const uint32_t p = p0 + lane;
-    // owner: the largest lane whose base <= p (empty splats share the base of
-    // the next splat, so they are never chosen for a pair they do not own)
-    uint32_t lo = 0;
-#pragma unroll
-    for (uint32_t step = 16; step > 0; step >>= 1) {
-      const uint32_t b = __shfl_sync(0xFFFFFFFFu, base, lo + step);
-      if (b <= p) lo += step;
-    }
-    const uint32_t ob = __shfl_sync(0xFFFFFFFFu, base, lo);
-    const uint32_t obox = __shfl_sync(0xFFFFFFFFu, box, lo);
-    const uint32_t orank = __shfl_sync(0xFFFFFFFFu, r, lo);
-    if (p < end) {
-      const uint32_t j = p - ob;
-      const uint32_t x0 = obox & 0xFFu, y0 = (obox >> 8) & 0xFFu, x1 = (obox >> 16) & 0xFFu;
-      const uint32_t spanX = x1 - x0 + 1u;
-      const uint32_t t = morton(x0 + j % spanX, y0 + j / spanX);
-      a.pairs_a[p] = ((unsigned long long)t << R) | orank;
+  if (i >= a.N) return;
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t r = a.order[i];
+  const uint32_t box = a.aux[r].x;
+  if (box == kSentinel) return;
+  const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
+  uint32_t o = a.sb_off[i];
+  for (uint32_t sy = y0 >> kSbShift; sy <= y1 >> kSbShift; ++sy) {
+    const uint32_t by = sy << kSbShift;
+    const uint32_t ly0 = y0 > by ? y0 - by : 0u, ly1 = y1 - by < 7u ? y1 - by : 7u;
+    for (uint32_t sx = x0 >> kSbShift; sx <= x1 >> kSbShift; ++sx) {
+      const uint32_t bx = sx << kSbShift;
+      const uint32_t lx0 = x0 > bx ? x0 - bx : 0u, lx1 = x1 - bx < 7u ? x1 - bx : 7u;
+      const uint32_t rect = lx0 | (lx1 << 3) | (ly0 << 6) | (ly1 << 9);
+      if (o < a.sb_cap)
+        a.sbk_a[o] = ((unsigned long long)(sy * a.sb_cols + sx) << kSbKeyShift) |
+                     ((unsigned long long)rect << 24) | r;
+      ++o;
     }
   }
 }
@@ -384,7 +462,9 @@ __global__ void __launch_bounds__(256) k_emit(FrameArgs a) {
 }  // namespace
 
 cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s) {
-  uint32_t n = a.M > 1u ? a.M : 1u;
+  const uint32_t grid_words = (a.cols + 1u) * (a.rows + 1u);
+  uint32_t n = a.M > grid_words ? a.M : grid_words;
+  if (n < (a.sb_cols + 1u) * (a.sb_rows + 1u)) n = (a.sb_cols + 1u) * (a.sb_rows + 1u);
   k_frame_init<<<(n + 255) / 256, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
@@ -394,34 +474,33 @@ cudaError_t launch_project(const FrameArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// Largest M whose three privatised u32 tables fit one block's shared memory.
-uint32_t count_smem_max_tiles() { return (200u * 1024u) / 12u; }
-
-cudaError_t launch_count(const FrameArgs& a, cudaStream_t s) {
-  if (!a.N) return cudaSuccess;
-  if (a.M <= count_smem_max_tiles()) {
-    const size_t smem = (size_t)a.M * (a.log_keys ? 12u : 4u);
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(k_count_smem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(count_smem_max_tiles() * 12u));
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_count_smem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(count_smem_max_tiles() * 12u));
-      if (e != cudaSuccess) return e;
-      attr_set = true;
+cudaError_t launch_tile_counts(const FrameArgs& a, cudaStream_t s) {
+  const uint32_t words = (a.cols + 1u) * (a.rows + 1u) + (a.sb_cols + 1u) * (a.sb_rows + 1u);
+  if (a.N) {
+    if (words <= kDiffSmemMaxWords) {
+      static bool attr_set = false;
+      if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_tile_diff_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(kDiffSmemMaxWords * 4u));
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+      }
+      k_tile_diff_smem<<<a.num_sms, 1024, words * 4u, s>>>(a);
+    } else {
+      k_tile_diff<<<(a.N + 255) / 256, 256, 0, s>>>(a);
     }
-    if (a.log_keys) k_count_smem<true><<<a.num_sms, kCountSmemThreads, smem, s>>>(a);
-    else k_count_smem<false><<<a.num_sms, kCountSmemThreads, smem, s>>>(a);
-  } else {
-    if (a.log_keys) k_count<true><<<(a.N + 255) / 256, 256, 0, s>>>(a);
-    else k_count<false><<<(a.N + 255) / 256, 256, 0, s>>>(a);
   }
+  k_tile_prefix<<<1, 1024, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_emit(const FrameArgs& a, cudaStream_t s) {
-  if (a.N) k_emit<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+cudaError_t launch_depth_range(const FrameArgs& a, cudaStream_t s) {
+  if (a.N) k_depth_range<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_emit_sb(const FrameArgs& a, cudaStream_t s) {
+  if (a.N) k_emit_sb<<<(a.N + 255) / 256, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

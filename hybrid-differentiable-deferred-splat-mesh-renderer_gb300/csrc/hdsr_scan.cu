@@ -3,8 +3,8 @@
 // Replaces the reference's three-pass Hillis-Steele scan (scan,
 // scan_block_sums, add_block_sums in gpu_prefix_sum.wgsl:169-240, driven by
 // gpuTileSplatCompositor.ts:1063-1088) with one launch per array:
-//   - per-splat tile counts, taken in ascending (depth, sortRank) order (N)
-//     -> pair offsets of the emission and P, the frame's pair total;
+//   - per-splat superblock counts, taken in ascending (depth, sortRank)
+//     order (N) -> offsets of the superblock list emission and Q, its total;
 //   - per-tile counts (M) -> tile offsets (bit-identical to the reference's
 //     tileOffsets), the hot-tile statistics of classify_tiles
 //     (gpu_tile_classify.wgsl:44-86) and, when requested, the per-tile
@@ -50,17 +50,13 @@ __device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t
   return prefix;
 }
 
-struct PairScan {
+struct SbScan {
   static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
-  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.ntiles[a.order[i]]; }
-  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) { a.pair_off[i] = excl; }
-  static __device__ void finish(const FrameArgs& a, uint32_t total) {
-    a.ctl[kCtlPairsLo] = total;
-    a.ctl[kCtlPairsHi] = 0u;
-    if ((uint64_t)total > a.cap) atomicOr(a.ctl + kCtlFlags, 0x1u);
-  }
+  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.nsb[a.order[i]]; }
+  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) { a.sb_off[i] = excl; }
+  static __device__ void finish(const FrameArgs& a, uint32_t total) { a.ctl[kCtlSbPairs] = total; }
 };
 
 struct TileScan {
@@ -80,7 +76,11 @@ struct TileScan {
       atomicAdd(a.ctl + kCtlChunks, (c + kMaxTileEntries - 1u) / kMaxTileEntries);
     }
   }
-  static __device__ void finish(const FrameArgs&, uint32_t) {}
+  static __device__ void finish(const FrameArgs& a, uint32_t total) {
+    a.ctl[kCtlPairsLo] = total;
+    a.ctl[kCtlPairsHi] = 0u;
+    if ((uint64_t)total > a.cap) atomicOr(a.ctl + kCtlFlags, 0x1u);
+  }
 };
 
 template <class Policy>
@@ -174,8 +174,8 @@ int scan_grid(const FrameArgs& a, uint32_t n) {
 
 }  // namespace
 
-cudaError_t launch_scan_pairs(const FrameArgs& a, cudaStream_t s) {
-  k_scan<PairScan><<<scan_grid(a, a.N), kScanThreads, 0, s>>>(a);
+cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s) {
+  k_scan<SbScan><<<scan_grid(a, a.N), kScanThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -12,9 +12,11 @@
 //   1. the depth digits on the N splats (depth is per splat): 4 passes of 8
 //      bits over u64 keys depth << 32 | sortRank; the pairs are then emitted
 //      in that depth order (hdsr_project.cu);
-//   2. the tile digits on the P pairs: 2 passes over u64 keys
-//      tile << R | sortRank (R = rank bits); the last pass writes the 1-u32
-//      tile entries (sortRank).
+//   2. the tile: the pairs are listed per superblock of 8x8 tiles by one
+//      (two above 256 superblocks) stable 8-bit pass over the superblock
+//      index, and each list is split by tile with a stable count/scan/scatter
+//      over 256-entry segments (k_seg_*), which writes the 1-u32 tile
+//      entries (sortRank).
 // Each pass is reduce-then-scan: an upsweep counts the digits of every block
 // tile of keys, a column scan turns the counts into per-tile digit offsets,
 // a bin scan gives the digits' global bases, and a downsweep ranks the keys
@@ -218,13 +220,176 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
       const unsigned long long k = S.keys[jj];
       const uint32_t o = S.excl[(uint32_t)(k >> shift) & dmask] + jj;
       if (LAST) {
-        j.out_low[o] = (uint32_t)(k & j.low_mask);
+        if (j.out_low) j.out_low[o] = (uint32_t)(k & j.low_mask);
         if (j.out_keys) j.out_keys[o] = k;
       } else {
         j.out[o] = k;
       }
     }
     __syncthreads();
+  }
+}
+
+// Tile entries from the superblock lists. Each superblock's list (its
+// splats in ascending (depth, sortRank) order, each with its tile box
+// clipped to the superblock) is cut into 256-entry segments; then
+//   k_seg_count:   per segment, how many of its entries cover each of the
+//                  superblock's 64 tiles (a 9x9 difference grid per warp);
+//   k_seg_scan:    per superblock and tile, an exclusive scan over the
+//                  segments plus the tile's offset: every segment's first
+//                  entry position in every tile;
+//   k_seg_scatter: per segment, in list order, every entry appended to every
+//                  tile it covers: one ballot per covered tile gives the
+//                  entries' ranks, the tile's running position lives in
+//                  lane (tile & 31) of the warp.
+// Tile j of a superblock is (j & 7, j >> 3) in its local coordinates.
+
+// Segment s: its superblock and its [beg, end) in the sorted list entries.
+__device__ __forceinline__ void seg_locate(const FrameArgs& a, uint32_t s, uint32_t& sb, uint32_t& beg,
+                                           uint32_t& end) {
+  uint32_t lo = 0u, hi = a.num_sb;  // seg_first[lo] <= s < seg_first[hi]
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a.seg_first[mid] <= s) lo = mid;
+    else hi = mid;
+  }
+  sb = lo;
+  beg = a.sb_start[sb] + (s - a.seg_first[sb]) * kSegEntries;
+  const uint32_t lim = a.sb_start[sb + 1u];
+  end = lim - beg < kSegEntries ? lim : beg + kSegEntries;
+}
+
+__device__ __forceinline__ uint32_t local_rect(unsigned long long k) { return (uint32_t)(k >> 24) & 0xFFFu; }
+
+__global__ void __launch_bounds__(256) k_seg_count(FrameArgs a) {
+  constexpr uint32_t kGrid = 9u * 9u;
+  __shared__ int s_diff[8][kGrid + 3u];
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t lane = threadIdx.x & 31u;
+  int* d = s_diff[threadIdx.x >> 5];
+  const uint32_t total = a.ctl[kCtlSegments];
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < total; s += nw) {
+    uint32_t sb, beg, end;
+    seg_locate(a, s, sb, beg, end);
+    for (uint32_t i = lane; i < kGrid; i += 32u) d[i] = 0;
+    __syncwarp();
+    for (uint32_t i = beg + lane; i < end; i += 32u) {
+      const uint32_t rc = local_rect(a.sbk_sorted[i]);
+      const uint32_t x0 = rc & 7u, x1 = ((rc >> 3) & 7u) + 1u, y0 = (rc >> 6) & 7u, y1 = (rc >> 9) + 1u;
+      atomicAdd(d + y0 * 9u + x0, 1);
+      atomicAdd(d + y0 * 9u + x1, -1);
+      atomicAdd(d + y1 * 9u + x0, -1);
+      atomicAdd(d + y1 * 9u + x1, 1);
+    }
+    __syncwarp();
+    if (lane < 8u) {
+      int run = 0;
+      for (uint32_t x = 0; x < 8u; ++x) {
+        run += d[lane * 9u + x];
+        d[lane * 9u + x] = run;
+      }
+    }
+    __syncwarp();
+    if (lane < 8u) {
+      int run = 0;
+      for (uint32_t y = 0; y < 8u; ++y) {
+        run += d[y * 9u + lane];
+        a.seg_cnt[(size_t)s * kSbTiles + y * 8u + lane] = (uint32_t)run;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// One block per superblock: 16 groups of 64 threads (one per tile), each
+// group a contiguous run of the superblock's segments.
+__global__ void __launch_bounds__(1024) k_seg_scan(FrameArgs a) {
+  constexpr uint32_t G = 16;
+  __shared__ uint32_t s_part[G][kSbTiles];
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t sb = blockIdx.x, j = threadIdx.x & (kSbTiles - 1u), g = threadIdx.x / kSbTiles;
+  const uint32_t f0 = a.seg_first[sb], f1 = a.seg_first[sb + 1u];
+  const uint32_t per = (f1 - f0 + G - 1u) / G;
+  const uint32_t s0 = f0 + g * per < f1 ? f0 + g * per : f1;
+  const uint32_t s1 = s0 + per < f1 ? s0 + per : f1;
+  uint32_t* cnt = a.seg_cnt + j;
+  uint32_t sum = 0u;
+  for (uint32_t s = s0; s < s1; ++s) sum += cnt[(size_t)s * kSbTiles];
+  s_part[g][j] = sum;
+  __syncthreads();
+  uint32_t excl = 0u;
+  for (uint32_t k = 0; k < g; ++k) excl += s_part[k][j];
+  const uint32_t tx = (sb % a.sb_cols) * 8u + (j & 7u), ty = (sb / a.sb_cols) * 8u + (j >> 3);
+  const bool in_frame = tx < a.cols && ty < a.rows;
+  const uint32_t t = in_frame ? morton(tx, ty) : 0u;
+  uint32_t run = (in_frame ? a.tile_off[t] : 0u) + excl;
+  for (uint32_t s = s0; s < s1; ++s) {
+    const uint32_t c = cnt[(size_t)s * kSbTiles];
+    cnt[(size_t)s * kSbTiles] = run;
+    run += c;
+  }
+  if (g == G - 1u && excl + sum != (in_frame ? a.tile_cnt[t] : 0u))
+    atomicOr(a.ctl + kCtlFlags, 0x8u);  // tile counts and superblock lists disagree
+  if (sb == 0u && threadIdx.x == 0u && a.sb_start[a.num_sb] != a.ctl[kCtlSbPairs])
+    atomicOr(a.ctl + kCtlFlags, 0x8u);
+}
+
+__global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
+  constexpr uint32_t C = kSegEntries / 32u;
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt = lanemask_lt();
+  const uint32_t total = a.ctl[kCtlSegments];
+  const uint32_t P = a.ctl[kCtlPairsLo];
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < total; s += nw) {
+    uint32_t sb, beg, end;
+    seg_locate(a, s, sb, beg, end);
+    uint32_t pos_lo = a.seg_cnt[(size_t)s * kSbTiles + lane];        // tile lane (rows 0..3)
+    uint32_t pos_hi = a.seg_cnt[(size_t)s * kSbTiles + 32u + lane];  // tile 32 + lane (rows 4..7)
+    unsigned long long k[C];
+#pragma unroll
+    for (uint32_t c = 0; c < C; ++c) {
+      const uint32_t i = beg + c * 32u + lane;
+      k[c] = i < end ? a.sbk_sorted[i] : 0ull;
+    }
+#pragma unroll
+    for (uint32_t c = 0; c < C; ++c) {
+      if (beg + c * 32u >= end) break;
+      uint32_t m_lo = 0u, m_hi = 0u;
+      if (beg + c * 32u + lane < end) {
+        const uint32_t rc = local_rect(k[c]);
+        const uint32_t x0 = rc & 7u, x1 = (rc >> 3) & 7u, y0 = (rc >> 6) & 7u, y1 = rc >> 9;
+        const uint32_t cols = ((2u << x1) - 1u) & ~((1u << x0) - 1u);
+        const uint32_t rows = ((2u << y1) - 1u) & ~((1u << y0) - 1u);
+        const uint32_t rep = cols * 0x01010101u;
+        // spread row bits 0..3 (4..7) to the low bit of bytes 0..3, then fill the bytes
+        m_lo = rep & ((((rows & 0xFu) * 0x00204081u) & 0x01010101u) * 0xFFu);
+        m_hi = rep & ((((rows >> 4) * 0x00204081u) & 0x01010101u) * 0xFFu);
+      }
+      const uint32_t r = (uint32_t)k[c] & 0xFFFFFFu;
+      uint32_t u = __reduce_or_sync(0xFFFFFFFFu, m_lo);
+      while (u) {
+        const uint32_t t = __ffs(u) - 1u;
+        u &= u - 1u;
+        const bool take = (m_lo >> t) & 1u;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, take);
+        const uint32_t o = __shfl_sync(0xFFFFFFFFu, pos_lo, t) + __popc(b & lt);
+        if (take && o < P) a.entries[o] = r;
+        if (lane == t) pos_lo += __popc(b);
+      }
+      u = __reduce_or_sync(0xFFFFFFFFu, m_hi);
+      while (u) {
+        const uint32_t t = __ffs(u) - 1u;
+        u &= u - 1u;
+        const bool take = (m_hi >> t) & 1u;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, take);
+        const uint32_t o = __shfl_sync(0xFFFFFFFFu, pos_hi, t) + __popc(b & lt);
+        if (take && o < P) a.entries[o] = r;
+        if (lane == t) pos_hi += __popc(b);
+      }
+    }
   }
 }
 
@@ -279,6 +444,14 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
   k_radix_binscan<<<1, 256, 0, s>>>(j);
   if (last) k_radix_downsweep<true><<<grid_last, kRadixThreads, smem, s>>>(j);
   else k_radix_downsweep<false><<<grid_mid, kRadixThreads, smem, s>>>(j);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s) {
+  if (!a.tile_count) return cudaSuccess;
+  k_seg_count<<<a.num_sms * 8, 256, 0, s>>>(a);
+  k_seg_scan<<<a.num_sb, 1024, 0, s>>>(a);
+  k_seg_scatter<<<a.num_sms * 8, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

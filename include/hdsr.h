@@ -41,6 +41,7 @@ typedef enum hdsr_status {
 #define HDSR_DEV_OVERFLOW   0x1u  /* pairs > pair_capacity: frame skipped       */
 #define HDSR_DEV_TIMEOUT    0x2u  /* a lookback wait exceeded its spin limit    */
 #define HDSR_DEV_BAD_INDEX  0x4u  /* sortedIndices held an id >= splatCount     */
+#define HDSR_DEV_COUNT_MISMATCH 0x8u /* tile counts and tile lists disagree (bug)  */
 
 /* planTileSplatCompositor input — gpuTileSplatCompositor.ts:109-116. */
 typedef struct hdsr_plan_input {
@@ -108,11 +109,11 @@ typedef struct hdsr_frame_stats {
   uint64_t total_pairs;           /* P of the last encoded frame */
   uint64_t pair_capacity;
   uint32_t visible_splats;
-  uint32_t reserved0;
+  uint32_t superblock_entries;    /* (8x8-tile superblock, splat) list entries */
   uint32_t hot_tiles;             /* tiles with > 4096 entries */
   uint32_t chunks;                /* 4096-entry chunks of hot tiles */
   uint32_t device_flags;          /* HDSR_DEV_* */
-  uint32_t reserved1;
+  uint32_t segments;              /* 256-entry segments of the superblock lists */
 } hdsr_frame_stats;
 
 typedef struct hdsr_compositor hdsr_compositor;
@@ -180,7 +181,7 @@ typedef enum hdsr_buffer_id {
   HDSR_BUF_TILE_OFFSETS = 6,  /* u32[M] exclusive prefix of tile counts */
   HDSR_BUF_TILE_ENTRIES = 7,  /* u32[P] sortRank per entry, final per-tile order */
   HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] per final entry: tile<<(20+R) | k20<<R | sortRank */
-  HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat tile counts, depth order */
+  HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat superblock counts, depth order */
   HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] sortRanks in ascending (depth bits, sortRank) */
 } hdsr_buffer_id;
 

@@ -38,6 +38,7 @@ def read_gpu(g) -> dict:
     P = int(st["total_pairs"])
     N = g["plan"].splat_count
     out = dict(status=st, P=P)
+    P = min(P, int(st["pair_capacity"]))  # an overflowing frame fails on its status, not on the readback
     out["geo"] = u32(res.buffer("cache_geo", count=4 * N)).reshape(N, 4)
     out["app"] = u32(res.buffer("cache_app", count=4 * N)).reshape(N, 4)
     out["gb"] = u32(res.buffer("cache_gb", count=4 * N)).reshape(N, 4)

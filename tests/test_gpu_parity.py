@@ -94,6 +94,26 @@ def test_hot_tiles_bucket_cascade(cuda, pkg, orc):
     assert gpu["status"]["chunks"] == ref["total_chunks"]
 
 
+def test_4k_viewport_two_superblock_passes(cuda, pkg, orc):
+    # 240 x 135 tiles = 30 x 17 superblocks of 8x8 tiles: more than 256, so
+    # the superblock lists take two 8-bit radix passes; ragged last row and
+    # column of superblocks
+    scene = pkg.workloads.hot_scene(60_000, 4)
+    cam = pkg.camera.OrbitCamera(**pkg.workloads.HOT760K_CAMERA)
+    g = render_gpu(pkg, scene, cam, 3840, 2160, pair_capacity=16_000_000)
+    gpu, ref = assert_frame_parity(orc, g)
+    assert g["res"].query_status()["superblock_entries"] > 0
+    g["res"].destroy()
+
+
+def test_single_superblock_viewport(cuda, pkg, orc):
+    # 8 x 8 tiles: one superblock, a 1-bit superblock digit
+    scene = pkg.workloads.plain_scene(3000, 9)
+    g = render_gpu(pkg, scene, pkg.camera.look_from((0.2, 0.1, 3.0)), 128, 128)
+    assert_frame_parity(orc, g)
+    g["res"].destroy()
+
+
 def test_near_plane_splats_negative_depth(cuda, pkg, orc):
     """Splats between the camera and the near plane have negative NDC depth:
     their tiles' log-depth range collapses (every entry in bucket 0) and u32
