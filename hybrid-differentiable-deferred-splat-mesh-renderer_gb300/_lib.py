@@ -111,6 +111,8 @@ SIGNATURES = {
     "hdsr_pass_times": (c_int, [c_void_p, POINTER(c_float), POINTER(c_uint32), c_uint32, POINTER(c_uint32)]),
     "hdsr_pass_name": (c_char_p, [c_uint32]),
     "hdsr_launch_count": (c_uint64, [c_void_p]),
+    "hdsr_count_tile_refs_static": (c_int, [c_void_p, c_uint32, c_uint64, c_uint32, c_uint32, c_void_p, c_uint64,
+                                            c_void_p]),
 }
 
 _LIB = None

@@ -207,6 +207,24 @@ const char* hdsr_pass_name(uint32_t id);
 /* Number of kernels this handle has queued since creation. */
 uint64_t hdsr_launch_count(const hdsr_compositor* h);
 
+/* Per-tile splat counts of a projected frame (the counts of count_tile_refs)
+ * without any device allocation and without a handle. No reference
+ * counterpart: the reference only counts inside its full pipeline.
+ *   tile_boxes: device u32 tile boxes (u8 x0, y0, x1, y1; 0xFFFFFFFF =
+ *     invisible), one every box_stride_words words (1: packed; 2: the
+ *     handle's HDSR_BUF_CACHE_AUX stream; 14: the reference cache rows);
+ *   tile_counts: device, tile_counts_len >= the plan's morton_tile_count
+ *     words; written in Morton order, every other word set to 0.
+ * Scratch is a static 256 KiB device array (a grid of <= 256 x 256 words):
+ * tile grids beyond 255 x 255 tiles return HDSR_ERR_UNSUPPORTED. The first
+ * call on a device (made with that device current) looks the scratch up;
+ * make it before capturing a stream. Nothing needs to start at zero. Calls
+ * on one device share the scratch: calls that may run concurrently race.
+ * Asynchronous on `stream`; returns launch errors only. */
+hdsr_status hdsr_count_tile_refs_static(const uint32_t* tile_boxes, uint32_t box_stride_words,
+                                        uint64_t splat_count, uint32_t tile_columns, uint32_t tile_rows,
+                                        uint32_t* tile_counts, uint64_t tile_counts_len, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
