@@ -328,22 +328,36 @@ __global__ void __launch_bounds__(256) k_tile_diff(FrameArgs a) {
 // grid gives every superblock's list length; one exclusive block scan of
 // (length, segments) turns those into list starts and the segment plan.
 // One block of 1024 threads (>= kMaxSuperblocks).
+// The cols x rows part of the grid is staged in shared memory when it fits
+// (launch with that much dynamic shared memory), else scanned in place.
+constexpr uint32_t kPrefixSmemMaxWords = (200u * 1024u) / 4u;
+
 __global__ void __launch_bounds__(1024) k_tile_prefix(FrameArgs a) {
   __shared__ unsigned long long s_warp[32];
-  const uint32_t stride = a.cols + 1u;
-  for (uint32_t y = threadIdx.x; y < a.rows; y += blockDim.x) {
+  extern __shared__ int s_grid[];
+  const uint32_t stride = a.cols + 1u, cols = a.cols, rows = a.rows;
+  int* g = a.tile_diff;
+  uint32_t gs = stride;
+  if (cols * rows <= kPrefixSmemMaxWords) {
+    for (uint32_t i = threadIdx.x; i < cols * rows; i += blockDim.x)
+      s_grid[i] = a.tile_diff[(i / cols) * stride + i % cols];
+    g = s_grid;
+    gs = cols;
+    __syncthreads();
+  }
+  for (uint32_t y = threadIdx.x; y < rows; y += blockDim.x) {
     int run = 0;
-    int* row = a.tile_diff + y * stride;
-    for (uint32_t x = 0; x < a.cols; ++x) {
+    int* row = g + y * gs;
+    for (uint32_t x = 0; x < cols; ++x) {
       run += row[x];
       row[x] = run;
     }
   }
   __syncthreads();
-  for (uint32_t x = threadIdx.x; x < a.cols; x += blockDim.x) {
+  for (uint32_t x = threadIdx.x; x < cols; x += blockDim.x) {
     int run = 0;
-    for (uint32_t y = 0; y < a.rows; ++y) {
-      run += a.tile_diff[y * stride + x];
+    for (uint32_t y = 0; y < rows; ++y) {
+      run += g[y * gs + x];
       a.tile_cnt[morton(x, y)] = (uint32_t)run;
     }
   }
@@ -490,7 +504,16 @@ cudaError_t launch_tile_counts(const FrameArgs& a, cudaStream_t s) {
       k_tile_diff<<<(a.N + 255) / 256, 256, 0, s>>>(a);
     }
   }
-  k_tile_prefix<<<1, 1024, 0, s>>>(a);
+  const uint32_t pw = a.cols * a.rows;
+  const size_t psmem = pw <= kPrefixSmemMaxWords ? pw * 4u : 0u;
+  static bool prefix_attr_set = false;
+  if (!prefix_attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_tile_prefix, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kPrefixSmemMaxWords * 4u));
+    if (e != cudaSuccess) return e;
+    prefix_attr_set = true;
+  }
+  k_tile_prefix<<<1, 1024, psmem, s>>>(a);
   return cudaGetLastError();
 }
 

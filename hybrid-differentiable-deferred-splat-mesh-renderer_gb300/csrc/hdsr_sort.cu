@@ -335,19 +335,23 @@ __global__ void __launch_bounds__(1024) k_seg_scan(FrameArgs a) {
     atomicOr(a.ctl + kCtlFlags, 0x8u);
 }
 
+// Two warps per segment: half h takes tile rows 4h..4h+3 (tiles 32h + lane).
 __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
   constexpr uint32_t C = kSegEntries / 32u;
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt = lanemask_lt();
-  const uint32_t total = a.ctl[kCtlSegments];
+  const uint32_t total = a.ctl[kCtlSegments] * 2u;
   const uint32_t P = a.ctl[kCtlPairsLo];
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < total; s += nw) {
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
+    const uint32_t s = w >> 1, half = w & 1u;
     uint32_t sb, beg, end;
     seg_locate(a, s, sb, beg, end);
-    uint32_t pos_lo = a.seg_cnt[(size_t)s * kSbTiles + lane];        // tile lane (rows 0..3)
-    uint32_t pos_hi = a.seg_cnt[(size_t)s * kSbTiles + 32u + lane];  // tile 32 + lane (rows 4..7)
+    // lane t: first position of tile 32 * half + t in this segment; the
+    // chunk's appends to it collect in inc and land after the chunk (every
+    // tile is visited at most once per chunk)
+    uint32_t pos = a.seg_cnt[(size_t)s * kSbTiles + 32u * half + lane];
     unsigned long long k[C];
 #pragma unroll
     for (uint32_t c = 0; c < C; ++c) {
@@ -357,38 +361,36 @@ __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
 #pragma unroll
     for (uint32_t c = 0; c < C; ++c) {
       if (beg + c * 32u >= end) break;
-      uint32_t m_lo = 0u, m_hi = 0u;
+      uint32_t m = 0u;
       if (beg + c * 32u + lane < end) {
         const uint32_t rc = local_rect(k[c]);
         const uint32_t x0 = rc & 7u, x1 = (rc >> 3) & 7u, y0 = (rc >> 6) & 7u, y1 = rc >> 9;
         const uint32_t cols = ((2u << x1) - 1u) & ~((1u << x0) - 1u);
-        const uint32_t rows = ((2u << y1) - 1u) & ~((1u << y0) - 1u);
-        const uint32_t rep = cols * 0x01010101u;
-        // spread row bits 0..3 (4..7) to the low bit of bytes 0..3, then fill the bytes
-        m_lo = rep & ((((rows & 0xFu) * 0x00204081u) & 0x01010101u) * 0xFFu);
-        m_hi = rep & ((((rows >> 4) * 0x00204081u) & 0x01010101u) * 0xFFu);
+        const uint32_t rows = (((2u << y1) - 1u) & ~((1u << y0) - 1u)) >> (4u * half);
+        // spread row bits 0..3 to the low bit of bytes 0..3, then fill the bytes
+        m = (cols * 0x01010101u) & ((((rows & 0xFu) * 0x00204081u) & 0x01010101u) * 0xFFu);
       }
       const uint32_t r = (uint32_t)k[c] & 0xFFFFFFu;
-      uint32_t u = __reduce_or_sync(0xFFFFFFFFu, m_lo);
+      uint32_t u = __reduce_or_sync(0xFFFFFFFFu, m);
+      uint32_t inc = 0u;
       while (u) {
-        const uint32_t t = __ffs(u) - 1u;
+        const uint32_t t0 = __ffs(u) - 1u;
         u &= u - 1u;
-        const bool take = (m_lo >> t) & 1u;
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, take);
-        const uint32_t o = __shfl_sync(0xFFFFFFFFu, pos_lo, t) + __popc(b & lt);
-        if (take && o < P) a.entries[o] = r;
-        if (lane == t) pos_lo += __popc(b);
+        const bool has1 = u != 0u;
+        const uint32_t t1 = has1 ? __ffs(u) - 1u : t0;
+        u &= u - 1u;  // no-op when u == 0
+        const bool take0 = (m >> t0) & 1u;
+        const bool take1 = has1 && ((m >> t1) & 1u);
+        const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, take0);
+        const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, take1);
+        const uint32_t o0 = __shfl_sync(0xFFFFFFFFu, pos, t0) + __popc(b0 & lt);
+        const uint32_t o1 = __shfl_sync(0xFFFFFFFFu, pos, t1) + __popc(b1 & lt);
+        if (take0 && o0 < P) a.entries[o0] = r;
+        if (take1 && o1 < P) a.entries[o1] = r;
+        if (lane == t0) inc += __popc(b0);
+        if (has1 && lane == t1) inc += __popc(b1);
       }
-      u = __reduce_or_sync(0xFFFFFFFFu, m_hi);
-      while (u) {
-        const uint32_t t = __ffs(u) - 1u;
-        u &= u - 1u;
-        const bool take = (m_hi >> t) & 1u;
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, take);
-        const uint32_t o = __shfl_sync(0xFFFFFFFFu, pos_hi, t) + __popc(b & lt);
-        if (take && o < P) a.entries[o] = r;
-        if (lane == t) pos_hi += __popc(b);
-      }
+      pos += inc;
     }
   }
 }
