@@ -4,13 +4,14 @@ The compute path is libhdsr.so (hand-written sm_103a CUDA behind the C ABI in
 include/hdsr.h); this package is the host-side mirror of the reference's
 operator API plus scene packing, camera conventions and synthetic workloads.
 """
-from . import _build, _lib, camera, splats, workloads
+from . import _build, _lib, camera, differentiable, splats, workloads
 from .compositor import (
     TileSplatCompositorPlan,
     TileSplatCompositorResources,
     create_output_textures,
     create_tile_splat_bind_groups,
     create_tile_splat_compositor,
+    encode_backward,
     encode_composite_only,
     encode_full_compute_compositor_pipeline,
     frame_uniforms_for,
@@ -30,6 +31,8 @@ __all__ = [
     "create_output_textures",
     "create_tile_splat_bind_groups",
     "create_tile_splat_compositor",
+    "differentiable",
+    "encode_backward",
     "encode_composite_only",
     "encode_full_compute_compositor_pipeline",
     "frame_uniforms_for",

@@ -29,6 +29,7 @@ COLOR_RGBA16F = 0
 COLOR_RGBA32F = 1
 CFG_KEEP_SORTED_KEYS = 0x1
 CFG_NO_GRAPH = 0x2
+CFG_BACKWARD = 0x4
 
 DEV_OVERFLOW = 0x1
 DEV_TIMEOUT = 0x2
@@ -77,6 +78,12 @@ class OutputViews(ctypes.Structure):
                 ("material_pitch", c_uint64)]
 
 
+class GradViews(ctypes.Structure):
+    _fields_ = [("d_color", c_void_p), ("d_color_pitch", c_uint64), ("d_positions", c_void_p),
+                ("d_log_scales", c_void_p), ("d_rotations", c_void_p), ("d_opacities", c_void_p),
+                ("d_sh", c_void_p)]
+
+
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_pairs", c_uint64), ("pair_capacity", c_uint64), ("visible_splats", c_uint32),
                 ("superblock_entries", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
@@ -97,6 +104,7 @@ SIGNATURES = {
     "hdsr_destroy_tile_splat_compositor": (None, [c_void_p]),
     "hdsr_bind_scene": (c_int, [c_void_p, POINTER(SceneViews)]),
     "hdsr_bind_outputs": (c_int, [c_void_p, POINTER(OutputViews)]),
+    "hdsr_encode_backward": (c_int, [c_void_p, POINTER(GradViews), c_void_p]),
     "hdsr_write_tile_splat_frame_uniforms": (None, [POINTER(c_float), POINTER(c_float), POINTER(Plan), c_float,
                                                     c_uint32, POINTER(c_float), POINTER(c_float),
                                                     POINTER(c_float), POINTER(c_float)]),

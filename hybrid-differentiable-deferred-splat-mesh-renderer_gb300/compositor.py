@@ -70,11 +70,11 @@ class TileSplatCompositorResources:
     """Owner of one compositor handle (and of every internal device buffer)."""
 
     def __init__(self, plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,
-                 keep_sorted_keys: bool = False):
+                 keep_sorted_keys: bool = False, backward: bool = False):
         self.plan = plan
         self._lib = _lib.load()
-        cfg = _lib.Config(int(pair_capacity), _lib.COLOR_RGBA32F if f32_color else _lib.COLOR_RGBA16F,
-                          _lib.CFG_KEEP_SORTED_KEYS if keep_sorted_keys else 0)
+        flags = (_lib.CFG_KEEP_SORTED_KEYS if keep_sorted_keys else 0) | (_lib.CFG_BACKWARD if backward else 0)
+        cfg = _lib.Config(int(pair_capacity), _lib.COLOR_RGBA32F if f32_color else _lib.COLOR_RGBA16F, flags)
         handle = ctypes.c_void_p()
         status = self._lib.hdsr_create_tile_splat_compositor(ctypes.byref(plan._c()), ctypes.byref(cfg),
                                                              ctypes.byref(handle))
@@ -168,8 +168,22 @@ class _DeviceView:
 
 
 def create_tile_splat_compositor(plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,
-                                 keep_sorted_keys: bool = False) -> TileSplatCompositorResources:
-    return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys)
+                                 keep_sorted_keys: bool = False, backward: bool = False) -> TileSplatCompositorResources:
+    return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys, backward)
+
+
+def encode_backward(stream, resources: TileSplatCompositorResources, d_color, grads: dict) -> None:
+    """Adjoint of the last full encode (hdsr_encode_backward).
+
+    d_color: (H, W, 4) float32 CUDA tensor, dL/d(color output). grads: float32
+    CUDA tensors positions (N, 3), log_scales (N, 3), rotations (N, 4),
+    opacities (N,), sh (N, 6 + 3K); overwritten with the gradients."""
+    assert d_color.dtype.itemsize == 4 and d_color.is_contiguous()
+    gv = _lib.GradViews(_ptr(d_color), int(d_color.stride(0) * 4), _ptr(grads["positions"]),
+                        _ptr(grads["log_scales"]), _ptr(grads["rotations"]), _ptr(grads["opacities"]),
+                        _ptr(grads["sh"]))
+    _lib.check(resources._lib.hdsr_encode_backward(resources.handle, ctypes.byref(gv), _stream_handle(stream)),
+               resources.handle, "encode_backward")
 
 
 @dataclass

@@ -31,6 +31,8 @@ struct hdsr_compositor {
   hdsr_config cfg{};
   int device = 0;
   FrameArgs args{};
+  float4* bwd_par = nullptr;      // adjoint buffers (HDSR_CFG_BACKWARD)
+  float* bwd_g2d = nullptr;
   std::vector<void*> allocs;
   float uniforms[64] = {};
   bool have_uniforms = false;
@@ -200,6 +202,10 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.scan_status_n, scan_tiles_n, "scan_status_n");
   ALLOC(a.scan_status_m, scan_tiles_m, "scan_status_m");
   ALLOC(a.ctl, (uint64_t)kCtlWords, "ctl");
+  if (h->cfg.flags & HDSR_CFG_BACKWARD) {
+    ALLOC(h->bwd_par, (uint64_t)N * 3u, "backward_screen_parameters");
+    ALLOC(h->bwd_g2d, (uint64_t)N * kG2d, "backward_screen_gradients");
+  }
 #undef ALLOC
   if (s != HDSR_OK) { free_all(h); delete h; return s; }
   a.U = U;
@@ -425,6 +431,45 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
 }
 
 hdsr_status hdsr_encode_full(hdsr_compositor* h, void* stream) { return encode(h, stream, true); }
+
+hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* g, void* stream) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (!(h->cfg.flags & HDSR_CFG_BACKWARD)) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_BACKWARD");
+  if (!g || !g->d_color) return fail(h, HDSR_ERR_INVALID_ARG, "gradient views are NULL");
+  if (!h->sorted_valid) return fail(h, HDSR_ERR_NOT_BOUND, "no frame: encode_full first");
+  const FrameArgs& a = h->args;
+  if (a.N && (!g->d_positions || !g->d_log_scales || !g->d_rotations || !g->d_opacities || !g->d_sh))
+    return fail(h, HDSR_ERR_INVALID_ARG, "a gradient output is NULL");
+  if (g->d_color_pitch < (uint64_t)a.W * 16u || (g->d_color_pitch & 15u))
+    return fail(h, HDSR_ERR_INVALID_ARG, "d_color pitch must be >= 16*W bytes and a multiple of 16");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const uint64_t N = a.N;
+  const uint64_t sh_row = 6u + 3u * (((uint64_t)a.sh_degree + 1u) * (a.sh_degree + 1u) - 1u);
+  cudaError_t e = cudaSuccess;
+  if (N) {
+    e = cudaMemsetAsync(g->d_positions, 0, N * 12, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->d_log_scales, 0, N * 12, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->d_rotations, 0, N * 16, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->d_opacities, 0, N * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->d_sh, 0, N * sh_row * 4, s);
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.ctl + kCtlBwdTile, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "backward clears");
+  BwdArgs b{};
+  b.f = a;
+  b.d_color = g->d_color;
+  b.d_color_pitch = g->d_color_pitch;
+  b.par = h->bwd_par;
+  b.g2d = h->bwd_g2d;
+  b.d_pos = g->d_positions;
+  b.d_lsc = g->d_log_scales;
+  b.d_rot = g->d_rotations;
+  b.d_opa = g->d_opacities;
+  b.d_sh = g->d_sh;
+  if ((e = launch_backward(b, s)) != cudaSuccess) return cuda_fail(h, e, "backward");
+  h->launches += (a.N ? 2 : 0) + (a.tile_count ? 1 : 0);
+  return HDSR_OK;
+}
 
 hdsr_status hdsr_encode_composite_only(hdsr_compositor* h, void* stream) { return encode(h, stream, false); }
 

@@ -1,0 +1,554 @@
+// hdsr_backward.cu — the adjoint of one frame: dL/d(colour image) ->
+// dL/d(positions, log-scales, rotations, opacities, SH coefficients).
+//
+// No reference counterpart (the reference renders only). The differentiated
+// function is the frame's mathematics at fp32: the cache's f16 opacity and
+// colour are taken unrounded, and the 2D conic is evaluated without the
+// cancellation of XX*YY - XY^2 (detOrig = |b0 x b1|^2, the Lagrange identity,
+// and detBlur = detOrig + 0.3 (XX + YY) + 0.09), which for splats seen
+// edge-on (a nearly singular covariance) loses several digits in fp32.
+// Every threshold of the composite (power > -4, alpha > 1/255, T >= 0.001,
+// the 0.99 alpha cap) and every clamp of the projection (opacity, colour,
+// view depth, w) is held fixed: a clamped quantity passes no gradient. The
+// per-tile entry lists of the forward frame are reused.
+//   1. k_bwd_prep: per sortRank, the screen-space parameters of the adjoint
+//      (centre, conic, clamped opacity with the anti-aliasing factor, clamped
+//      SH colour); zeroes the screen-space accumulators.
+//   2. k_raster_bwd: one warp per half tile (rows 0-7 or 8-15, from an atomic
+//      counter), each lane one 2x2 quad. Pass A recomputes the composite
+//      front to back and keeps, per pixel, the final transmittance T_f and
+//      output O = sum c_k w_k + bg T_f. Pass B walks the same entries again:
+//      with C_k = sum_{j<=k} c_j w_j, the light behind entry k is O - C_k, so
+//        dL/dalpha_k = sum_ch dL/dO_ch (c_k,ch T_k - (O_ch - C_k,ch) / (1 -
+//                      alpha_k)) + dL/dA T_f / (1 - alpha_k),   A = 1 - T_f,
+//      and dL/dc_k = dL/dO w_k. Per entry the warp sums its lanes' values
+//      (butterfly shuffles) and one lane adds them to the entry's accumulators.
+//   3. k_project_bwd: per sortRank, recompute the projection in fp32 and apply
+//      the chain rule back to the scene arrays (atomic adds: a splat id may
+//      appear in sortedIndices more than once).
+#include "hdsr_internal.cuh"
+
+namespace hdsr {
+
+namespace {
+
+// Scalar type of the projection recompute and its adjoint (per splat, not
+// per pixel): fp64. For splats seen nearly edge-on the conic's adjoint
+// combines large terms that cancel; at fp32 a few of them land 1e-3 to 1e-2
+// away from the FP64 gradient, at fp64 they agree to the fp32 raster's
+// precision. -DHDSR_BWD_REAL=float builds the fp32 variant.
+#ifndef HDSR_BWD_REAL
+#define HDSR_BWD_REAL double
+#endif
+using real = HDSR_BWD_REAL;
+__device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float rexp_(float x) { return hx_expf(x); }
+__device__ __forceinline__ double rexp_(double x) { return exp(x); }
+__device__ __forceinline__ real rmax_(real a, real b) { return a > b ? a : b; }
+__device__ __forceinline__ real rmin_(real a, real b) { return a < b ? a : b; }
+__device__ __forceinline__ real rclamp_(real x, real lo, real hi) { return rmin_(rmax_(x, lo), hi); }
+
+struct F3 { real x, y, z; };
+__device__ __forceinline__ F3 f3(real x, real y, real z) { return F3{x, y, z}; }
+__device__ __forceinline__ real dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 mul(F3 a, real s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ F3 cross(F3 a, F3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+constexpr real kBgR = 0.02f, kBgG = 0.02f, kBgB = 0.04f;  // composite background (T-weighted)
+
+// Projection of one splat, recomputed in fp32 with every intermediate the
+// adjoint needs (gpu_project_splats.wgsl:112-358, colour part and 2D conic).
+struct Proj {
+  F3 p;
+  real clip[4], safeW;
+  bool w_free;          // safeW == clip[3] (not clamped to 1e-4)
+  real vc[3], vz;
+  bool vz_free;         // vz == vc[2]
+  real fx, fy, J1x, J1y, J2x, J2y;
+  F3 w0, w1, w2, tt0, tt1;
+  real qn[4], qlen;    // normalised quaternion (w, x, y, z), its length
+  F3 R[3];              // rotated unit axes (columns of R)
+  real s[3];           // axis scales exp(logScale) * splatScale
+  F3 ax[3];
+  F3 b0, b1, cr;         // b0_i = ax_i . tt0, b1_i = ax_i . tt1, cr = b0 x b1
+  real XXr, XY, YYr, detOrig, cXX, cYY, D, ratio, aa;
+  real cx, cy;
+  real op_in, op_aa;   // input opacity, opacity * aa (before the clamp)
+  F3 cam, dir;
+  real dlen;
+  real craw[3];        // SH colour before the clamp
+};
+
+__device__ __forceinline__ real ld(const float* p) { return (real)__ldg(p); }
+
+__device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
+  const float* U = a.U;
+  const float* pp = a.pos + (uint64_t)id * 3;
+  P.p = f3(ld(pp), ld(pp + 1), ld(pp + 2));
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    P.clip[k] = ((ld(U + k) * P.p.x + ld(U + 4 + k) * P.p.y) + ld(U + 8 + k) * P.p.z) + ld(U + 12 + k);
+  P.safeW = rmax_(P.clip[3], 0.0001f);
+  P.w_free = P.clip[3] > 0.0001f;
+  P.cx = (P.clip[0] / P.safeW * 0.5f + 0.5f) * ld(U + 16);
+  P.cy = (1.0f - (P.clip[1] / P.safeW * 0.5f + 0.5f)) * ld(U + 17);
+  // axes
+  const float4 q = __ldg(reinterpret_cast<const float4*>(a.rot) + id);
+  P.qlen = rsqrt_(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  const real d = rmax_(P.qlen, 0.000001f);
+  P.qn[0] = q.x / d; P.qn[1] = q.y / d; P.qn[2] = q.z / d; P.qn[3] = q.w / d;
+  const real w = P.qn[0], x = P.qn[1], y = P.qn[2], z = P.qn[3];
+  P.R[0] = f3(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + w * z), 2.0f * (x * z - w * y));
+  P.R[1] = f3(2.0f * (x * y - w * z), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + w * x));
+  P.R[2] = f3(2.0f * (x * z + w * y), 2.0f * (y * z - w * x), 1.0f - 2.0f * (x * x + y * y));
+  const float* sl = a.scl + (uint64_t)id * 3;
+  const real ss = ld(U + 24);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    P.s[i] = rexp_(ld(sl + i)) * ss;
+    P.ax[i] = mul(P.R[i], P.s[i]);
+  }
+  // Jacobian of the perspective projection in view space
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    P.vc[k] = ((ld(U + 32 + k) * P.p.x + ld(U + 36 + k) * P.p.y) + ld(U + 40 + k) * P.p.z) + ld(U + 44 + k);
+  P.vz = rmin_(P.vc[2], -0.001f);
+  P.vz_free = P.vc[2] < -0.001f;
+  P.fx = ld(U + 48);
+  P.fy = ld(U + 49);
+  P.J1x = P.fx / P.vz;
+  P.J1y = P.fy / P.vz;
+  P.J2x = (-P.J1x / P.vz) * P.vc[0];
+  P.J2y = (-P.J1y / P.vz) * P.vc[1];
+  P.w0 = f3(ld(U + 32), ld(U + 36), ld(U + 40));
+  P.w1 = f3(ld(U + 33), ld(U + 37), ld(U + 41));
+  P.w2 = f3(ld(U + 34), ld(U + 38), ld(U + 42));
+  P.tt0 = add(mul(P.w0, P.J1x), mul(P.w2, P.J2x));
+  P.tt1 = add(mul(P.w1, P.J1y), mul(P.w2, P.J2y));
+  P.b0 = f3(dot(P.ax[0], P.tt0), dot(P.ax[1], P.tt0), dot(P.ax[2], P.tt0));
+  P.b1 = f3(dot(P.ax[0], P.tt1), dot(P.ax[1], P.tt1), dot(P.ax[2], P.tt1));
+  P.XXr = dot(P.b0, P.b0);
+  P.XY = dot(P.b0, P.b1);
+  P.YYr = dot(P.b1, P.b1);
+  P.cr = cross(P.b0, P.b1);
+  P.detOrig = dot(P.cr, P.cr);
+  P.cXX = P.XXr + 0.3f;
+  P.cYY = P.YYr + 0.3f;
+  P.D = P.detOrig + 0.3f * (P.XXr + P.YYr) + 0.09f;  // >= 0.09: never below the 1e-6 floor
+  P.ratio = P.detOrig / P.D;
+  P.aa = rsqrt_(P.ratio);
+  P.op_in = ld(a.opa + id);
+  P.op_aa = P.op_in * P.aa;
+  // SH colour (WGSL basis and signs)
+  P.cam = f3(ld(U + 28), ld(U + 29), ld(U + 30));
+  const F3 dv = sub(P.cam, P.p);
+  P.dlen = rsqrt_(dot(dv, dv));
+  P.dir = f3(dv.x / P.dlen, dv.y / P.dlen, dv.z / P.dlen);
+  const uint32_t deg = f2u(ld(U + 25));
+  const uint32_t shStride = ((deg + 1) * (deg + 1) - 1) * 3;
+  const float* sh = a.sh + (uint64_t)id * (3 + shStride + 3);
+  real basis[15];
+  const real vx = P.dir.x, vy = P.dir.y, vzz = P.dir.z;
+  const real xx = vx * vx, yy = vy * vy, zz = vzz * vzz;
+  basis[0] = 0.4886025119029199f * vy;
+  basis[1] = 0.4886025119029199f * vzz;
+  basis[2] = 0.4886025119029199f * vx;
+  basis[3] = 1.0925484305920792f * vx * vy;
+  basis[4] = 1.0925484305920792f * vy * vzz;
+  basis[5] = 0.31539156525252005f * ((2.0f * zz - xx) - yy);
+  basis[6] = 1.0925484305920792f * vx * vzz;
+  basis[7] = 0.5462742152960396f * (xx - yy);
+  basis[8] = 0.5900435899266435f * vy * (3.0f * xx - yy);
+  basis[9] = 2.890611442640554f * vx * vy * vzz;
+  basis[10] = 0.4570457994644658f * vy * ((4.0f * zz - xx) - yy);
+  basis[11] = 0.3731763325901154f * vzz * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
+  basis[12] = 0.4570457994644658f * vx * ((4.0f * zz - xx) - yy);
+  basis[13] = 1.445305721320277f * vzz * (xx - yy);
+  basis[14] = 0.5900435899266435f * vx * (xx - 3.0f * yy);
+  const uint32_t nb = (deg + 1) * (deg + 1) - 1;
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    real c = ld(sh + ch);
+    for (uint32_t k = 0; k < nb && k < 15u; ++k) c += ld(sh + 3 + 3 * k + ch) * basis[k];
+    P.craw[ch] = c;
+  }
+}
+
+// d(basis_k)/d(dir), k < 15 (same order as proj_recompute)
+__device__ __forceinline__ F3 dbasis(int k, F3 v) {
+  const real vx = v.x, vy = v.y, vz = v.z, xx = vx * vx, yy = vy * vy, zz = vz * vz;
+  const real C1 = 0.4886025119029199f, A = 1.0925484305920792f, B = 0.31539156525252005f;
+  const real Cc = 0.5462742152960396f, Dd = 0.5900435899266435f, E = 2.890611442640554f;
+  const real Ff = 0.4570457994644658f, G = 0.3731763325901154f, Hh = 1.445305721320277f;
+  switch (k) {
+    case 0: return f3(0.0f, C1, 0.0f);
+    case 1: return f3(0.0f, 0.0f, C1);
+    case 2: return f3(C1, 0.0f, 0.0f);
+    case 3: return f3(A * vy, A * vx, 0.0f);
+    case 4: return f3(0.0f, A * vz, A * vy);
+    case 5: return f3(-2.0f * B * vx, -2.0f * B * vy, 4.0f * B * vz);
+    case 6: return f3(A * vz, 0.0f, A * vx);
+    case 7: return f3(2.0f * Cc * vx, -2.0f * Cc * vy, 0.0f);
+    case 8: return f3(6.0f * Dd * vx * vy, Dd * (3.0f * xx - 3.0f * yy), 0.0f);
+    case 9: return f3(E * vy * vz, E * vx * vz, E * vx * vy);
+    case 10: return f3(-2.0f * Ff * vx * vy, Ff * (4.0f * zz - xx - 3.0f * yy), 8.0f * Ff * vy * vz);
+    case 11: return f3(-6.0f * G * vx * vz, -6.0f * G * vy * vz, G * (6.0f * zz - 3.0f * xx - 3.0f * yy));
+    case 12: return f3(Ff * (4.0f * zz - 3.0f * xx - yy), -2.0f * Ff * vx * vy, 8.0f * Ff * vx * vz);
+    case 13: return f3(2.0f * Hh * vx * vz, -2.0f * Hh * vy * vz, Hh * (xx - yy));
+    default: return f3(Dd * (3.0f * xx - 3.0f * yy), -6.0f * Dd * vx * vy, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bwd_prep(BwdArgs b) {
+  const FrameArgs& a = b.f;
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.N) return;
+#pragma unroll
+  for (uint32_t j = 0; j < kG2d; ++j) b.g2d[(size_t)r * kG2d + j] = 0.0f;
+  float4* par = b.par + (size_t)r * 3;
+  if (a.aux[r].x == kSentinel) {
+    par[0] = par[1] = par[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return;
+  }
+  Proj P;
+  proj_recompute(a, __ldg(a.sorted + r), P);
+  const real Di = 1.0f / P.D;
+  par[0] = make_float4(P.cx, P.cy, P.cYY * Di, -P.XY * Di);
+  par[1] = make_float4(P.cXX * Di, rclamp_(P.op_aa, 0.0f, 0.99f), rclamp_(P.craw[0], 0.0f, 1.0f),
+                       rclamp_(P.craw[1], 0.0f, 1.0f));
+  par[2] = make_float4(rclamp_(P.craw[2], 0.0f, 1.0f), 0.0f, 0.0f, 0.0f);
+}
+
+constexpr int kBwdWarps = 4;
+enum BField { B_CX, B_CY, B_KA, B_KB, B_KC, B_OP, B_R, B_G, B_B, B_IA, B_IB, B_IC, B_RANK, kBFields };
+
+__device__ __forceinline__ void bwd_stage(const BwdArgs& b, float (*s)[32], uint32_t e, uint32_t lane) {
+  const FrameArgs& a = b.f;
+  const uint32_t r = __ldg(a.entries + e);
+  const float4 p0 = b.par[(size_t)r * 3], p1 = b.par[(size_t)r * 3 + 1], p2 = b.par[(size_t)r * 3 + 2];
+  s[B_CX][lane] = p0.x;
+  s[B_CY][lane] = p0.y;
+  s[B_KA][lane] = p0.z * -0.5f;
+  s[B_KB][lane] = -p0.w;
+  s[B_KC][lane] = p1.x * -0.5f;
+  s[B_OP][lane] = p1.y;
+  s[B_R][lane] = p1.z;
+  s[B_G][lane] = p1.w;
+  s[B_B][lane] = p2.x;
+  s[B_IA][lane] = p0.z;
+  s[B_IB][lane] = p0.w;
+  s[B_IC][lane] = p1.x;
+  s[B_RANK][lane] = u2f(r);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
+  __shared__ float s_pay[kBwdWarps][kBFields][32];
+  const FrameArgs& a = b.f;
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  float (*s)[32] = s_pay[warp];
+  const uint32_t items = 2u * a.tile_count;
+  for (;;) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(a.ctl + kCtlBwdTile, 1u);
+    item = __shfl_sync(0xFFFFFFFFu, item, 0);
+    if (item >= items) break;
+    const uint32_t tile_idx = item >> 1, half = item & 1u;
+    const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
+    const uint32_t t = morton(tx, ty);
+    const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
+    const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
+    const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
+    const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
+    float dxv[4], dyv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      dxv[k] = p00x + (float)(k & 1);
+      dyv[k] = p00y + (float)(k >> 1);
+    }
+    // pass A: forward recompute
+    float T[4], C[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { T[k] = 1.0f; C[k][0] = C[k][1] = C[k][2] = 0.0f; }
+    bool done = false;
+    uint32_t n_end = 0;
+    for (uint32_t b0 = 0; b0 < count; b0 += 32u) {
+      const uint32_t n = count - b0 < 32u ? count - b0 : 32u;
+      if (lane < n) bwd_stage(b, s, start + b0 + lane, lane);
+      __syncwarp();
+      for (uint32_t i = 0; i < n && !done; ++i) {
+        const float cx = s[B_CX][i], cy = s[B_CY][i], ka = s[B_KA][i], kb = s[B_KB][i], kc = s[B_KC][i];
+        const float op = s[B_OP][i];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float dx = dxv[k] - cx, dy = dyv[k] - cy;
+          const float pw = fmaf(kc * dy, dy, fmaf(kb * dx, dy, (ka * dx) * dx));
+          const float al = mn(0.99f, op * hx_expf(pw));
+          const bool valid = (pw > -4.0f) && (al > (1.0f / 255.0f)) && (T[k] >= 0.001f);
+          if (valid) {
+            const float w = al * T[k];
+            C[k][0] = fmaf(s[B_R][i], w, C[k][0]);
+            C[k][1] = fmaf(s[B_G][i], w, C[k][1]);
+            C[k][2] = fmaf(s[B_B][i], w, C[k][2]);
+            T[k] = T[k] * (1.0f - al);
+          }
+        }
+        done = T[0] < 0.001f && T[1] < 0.001f && T[2] < 0.001f && T[3] < 0.001f;
+      }
+      __syncwarp();
+      n_end = b0 + n;
+      if (__all_sync(0xFFFFFFFFu, done)) break;
+    }
+    // outputs and their incoming gradients (pixels outside the image: none)
+    float O[4][3], Tf[4], gO[4][3], gA[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      Tf[k] = T[k];
+      O[k][0] = fmaf(T[k], kBgR, C[k][0]);
+      O[k][1] = fmaf(T[k], kBgG, C[k][1]);
+      O[k][2] = fmaf(T[k], kBgB, C[k][2]);
+      const uint32_t px = bx + (uint32_t)(k & 1), py = by + (uint32_t)(k >> 1);
+      float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (px < a.W && py < a.H)
+        g = reinterpret_cast<const float4*>(reinterpret_cast<const char*>(b.d_color) + (size_t)py * b.d_color_pitch)[px];
+      gO[k][0] = g.x; gO[k][1] = g.y; gO[k][2] = g.z; gA[k] = g.w;
+      T[k] = 1.0f;
+      C[k][0] = C[k][1] = C[k][2] = 0.0f;
+    }
+    // pass B: gradients, same entries in the same order
+    for (uint32_t b0 = 0; b0 < n_end; b0 += 32u) {
+      const uint32_t n = n_end - b0 < 32u ? n_end - b0 : 32u;
+      if (lane < n) bwd_stage(b, s, start + b0 + lane, lane);
+      __syncwarp();
+      for (uint32_t i = 0; i < n; ++i) {
+        const float cx = s[B_CX][i], cy = s[B_CY][i], ka = s[B_KA][i], kb = s[B_KB][i], kc = s[B_KC][i];
+        const float op = s[B_OP][i], cr = s[B_R][i], cg = s[B_G][i], cb = s[B_B][i];
+        const float ia = s[B_IA][i], ib = s[B_IB][i], ic = s[B_IC][i];
+        float g[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float dx = dxv[k] - cx, dy = dyv[k] - cy;
+          const float pw = fmaf(kc * dy, dy, fmaf(kb * dx, dy, (ka * dx) * dx));
+          const float ge = hx_expf(pw);
+          const float raw = op * ge;
+          const float al = mn(0.99f, raw);
+          const bool valid = (pw > -4.0f) && (al > (1.0f / 255.0f)) && (T[k] >= 0.001f);
+          if (!valid) continue;
+          any = true;
+          const float w = al * T[k];
+          C[k][0] = fmaf(cr, w, C[k][0]);
+          C[k][1] = fmaf(cg, w, C[k][1]);
+          C[k][2] = fmaf(cb, w, C[k][2]);
+          const float inv1m = 1.0f / (1.0f - al);
+          float dal = gO[k][0] * (cr * T[k] - (O[k][0] - C[k][0]) * inv1m) +
+                      gO[k][1] * (cg * T[k] - (O[k][1] - C[k][1]) * inv1m) +
+                      gO[k][2] * (cb * T[k] - (O[k][2] - C[k][2]) * inv1m) + gA[k] * Tf[k] * inv1m;
+          g[6] += gO[k][0] * w;
+          g[7] += gO[k][1] * w;
+          g[8] += gO[k][2] * w;
+          if (raw < 0.99f) {
+            g[5] += dal * ge;
+            const float dpw = dal * raw;
+            g[0] += dpw * (ia * dx + ib * dy);
+            g[1] += dpw * (ib * dx + ic * dy);
+            g[2] += dpw * (-0.5f * dx * dx);
+            g[3] += dpw * (-dx * dy);
+            g[4] += dpw * (-0.5f * dy * dy);
+          }
+          T[k] = T[k] * (1.0f - al);
+        }
+        if (__any_sync(0xFFFFFFFFu, any)) {
+          float* dst = b.g2d + (size_t)f2u(s[B_RANK][i]) * kG2d;
+#pragma unroll
+          for (int j = 0; j < 9; ++j) {
+            const float v = warp_sum(g[j]);
+            if (lane == (uint32_t)j && v != 0.0f) atomicAdd(dst + j, v);
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_project_bwd(BwdArgs b) {
+  const FrameArgs& a = b.f;
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.N) return;
+  if (a.aux[r].x == kSentinel) return;
+  const float* gr = b.g2d + (size_t)r * kG2d;
+  const real g_cx = gr[0], g_cy = gr[1], g_ia = gr[2], g_ib = gr[3], g_ic = gr[4];
+  const real g_op = gr[5];
+  const real g_col[3] = {gr[6], gr[7], gr[8]};
+  if (g_cx == 0.0f && g_cy == 0.0f && g_ia == 0.0f && g_ib == 0.0f && g_ic == 0.0f && g_op == 0.0f &&
+      g_col[0] == 0.0f && g_col[1] == 0.0f && g_col[2] == 0.0f)
+    return;
+  const uint32_t id = __ldg(a.sorted + r);
+  Proj P;
+  proj_recompute(a, id, P);
+  const float* U = a.U;
+  F3 g_p = f3(0.0f, 0.0f, 0.0f);
+
+  // opacity = clamp(op * aa, 0, 0.99)
+  real g_aa = 0.0f;
+  if (P.op_aa > 0.0f && P.op_aa < 0.99f) {
+    atomicAdd(b.d_opa + id, g_op * P.aa);
+    g_aa = g_op * P.op_in;
+  }
+  // inverse conic: ia = cYY/D, ib = -XY/D, ic = cXX/D
+  const real Di = 1.0f / P.D;
+  real g_cXX = g_ic * Di, g_cYY = g_ia * Di, g_XY = -g_ib * Di;
+  real g_D = -(g_ia * P.cYY - g_ib * P.XY + g_ic * P.cXX) * Di * Di;
+  // aa = sqrt(detOrig / D)
+  real g_detOrig = 0.0f;
+  if (P.aa > 0.0f) {
+    const real g_ratio = g_aa * 0.5f / P.aa;
+    g_detOrig += g_ratio * Di;
+    g_D -= g_ratio * P.detOrig * Di * Di;
+  }
+  // D = detOrig + 0.3 (XXr + YYr) + 0.09; cXX = XXr + 0.3, cYY = YYr + 0.3
+  g_detOrig += g_D;
+  const real g_XXr = g_cXX + 0.3f * g_D;
+  const real g_YYr = g_cYY + 0.3f * g_D;
+  // XXr = |b0|^2, XY = b0.b1, YYr = |b1|^2, detOrig = |b0 x b1|^2
+  const F3 gb0 = add(add(mul(P.b0, 2.0f * g_XXr), mul(P.b1, g_XY)), mul(cross(P.b1, P.cr), 2.0f * g_detOrig));
+  const F3 gb1 = add(add(mul(P.b1, 2.0f * g_YYr), mul(P.b0, g_XY)), mul(cross(P.cr, P.b0), 2.0f * g_detOrig));
+  // b0_i = ax_i . tt0, b1_i = ax_i . tt1
+  const real gb0v[3] = {gb0.x, gb0.y, gb0.z}, gb1v[3] = {gb1.x, gb1.y, gb1.z};
+  F3 g_tt0 = f3(0.0f, 0.0f, 0.0f), g_tt1 = f3(0.0f, 0.0f, 0.0f);
+  F3 g_ax[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    g_ax[i] = add(mul(P.tt0, gb0v[i]), mul(P.tt1, gb1v[i]));
+    g_tt0 = add(g_tt0, mul(P.ax[i], gb0v[i]));
+    g_tt1 = add(g_tt1, mul(P.ax[i], gb1v[i]));
+  }
+  // tt0 = J1x w0 + J2x w2, tt1 = J1y w1 + J2y w2
+  const real g_J1x = dot(g_tt0, P.w0), g_J2x = dot(g_tt0, P.w2);
+  const real g_J1y = dot(g_tt1, P.w1), g_J2y = dot(g_tt1, P.w2);
+  // J1 = f / vz, J2 = -f vc / vz^2
+  const real vz = P.vz, vz2 = vz * vz, vz3 = vz2 * vz;
+  real g_vc[3];
+  g_vc[0] = -g_J2x * P.fx / vz2;
+  g_vc[1] = -g_J2y * P.fy / vz2;
+  const real g_vz = -g_J1x * P.fx / vz2 - g_J1y * P.fy / vz2 + g_J2x * 2.0f * P.fx * P.vc[0] / vz3 +
+                     g_J2y * 2.0f * P.fy * P.vc[1] / vz3;
+  g_vc[2] = P.vz_free ? g_vz : 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) g_p = add(g_p, mul(f3(ld(U + 32 + k), ld(U + 36 + k), ld(U + 40 + k)), g_vc[k]));
+  // axes: ax_i = R_i s_i, s_i = exp(logScale_i) * splatScale
+  real gR[3][3];  // gR[i] = dL/d(column i)
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    atomicAdd(b.d_lsc + (size_t)id * 3 + i, dot(g_ax[i], P.R[i]) * P.s[i]);
+    const F3 gc = mul(g_ax[i], P.s[i]);
+    gR[i][0] = gc.x; gR[i][1] = gc.y; gR[i][2] = gc.z;
+  }
+  // R from (w, x, y, z); column i holds R[row][i] = gR[i][row]
+  {
+    const real w = P.qn[0], x = P.qn[1], y = P.qn[2], z = P.qn[3];
+    // dL/dR_rc with r = row, c = column
+    const real g00 = gR[0][0], g10 = gR[0][1], g20 = gR[0][2];
+    const real g01 = gR[1][0], g11 = gR[1][1], g21 = gR[1][2];
+    const real g02 = gR[2][0], g12 = gR[2][1], g22 = gR[2][2];
+    const real gw = 2.0f * (-z * g01 + y * g02 + z * g10 - x * g12 - y * g20 + x * g21);
+    const real gx = 2.0f * (y * g01 + z * g02 + y * g10 - 2.0f * x * g11 - w * g12 + z * g20 + w * g21 - 2.0f * x * g22);
+    const real gy = 2.0f * (-2.0f * y * g00 + x * g01 + w * g02 + x * g10 + z * g12 - w * g20 + z * g21 - 2.0f * y * g22);
+    const real gz = 2.0f * (-2.0f * z * g00 - w * g01 + x * g02 + w * g10 - 2.0f * z * g11 + y * g12 + x * g20 + y * g21);
+    // q_hat = q / max(|q|, 1e-6)
+    const real gq[4] = {gw, gx, gy, gz};
+    const real qd = gw * w + gx * x + gy * y + gz * z;
+    const real dn = rmax_(P.qlen, 0.000001f);
+    const bool norm_free = P.qlen > 0.000001f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      atomicAdd(b.d_rot + (size_t)id * 4 + k, (gq[k] - (norm_free ? P.qn[k] * qd : 0.0f)) / dn);
+  }
+  // centre: cpx = (clip0/safeW * 0.5 + 0.5) W, cpy = (1 - (clip1/safeW * 0.5 + 0.5)) H
+  {
+    const real vpW = ld(U + 16), vpH = ld(U + 17);
+    const real g_nx = g_cx * 0.5f * vpW, g_ny = -g_cy * 0.5f * vpH;
+    real g_clip[4];
+    g_clip[0] = g_nx / P.safeW;
+    g_clip[1] = g_ny / P.safeW;
+    g_clip[2] = 0.0f;
+    g_clip[3] = P.w_free ? -(g_nx * P.clip[0] + g_ny * P.clip[1]) / (P.safeW * P.safeW) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) g_p = add(g_p, mul(f3(ld(U + k), ld(U + 4 + k), ld(U + 8 + k)), g_clip[k]));
+  }
+  // colour = clamp(SH(dir), 0, 1), dir = normalize(cam - p)
+  {
+    const uint32_t deg = f2u(ld(U + 25));
+    const uint32_t nb = (deg + 1) * (deg + 1) - 1;
+    const uint32_t shStride = nb * 3;
+    const uint64_t base = (uint64_t)id * (3 + shStride + 3);
+    const float* sh = a.sh + base;
+    real basis[15];
+    {
+      const real vx = P.dir.x, vy = P.dir.y, vzz = P.dir.z;
+      const real xx = vx * vx, yy = vy * vy, zz = vzz * vzz;
+      basis[0] = 0.4886025119029199f * vy;
+      basis[1] = 0.4886025119029199f * vzz;
+      basis[2] = 0.4886025119029199f * vx;
+      basis[3] = 1.0925484305920792f * vx * vy;
+      basis[4] = 1.0925484305920792f * vy * vzz;
+      basis[5] = 0.31539156525252005f * ((2.0f * zz - xx) - yy);
+      basis[6] = 1.0925484305920792f * vx * vzz;
+      basis[7] = 0.5462742152960396f * (xx - yy);
+      basis[8] = 0.5900435899266435f * vy * (3.0f * xx - yy);
+      basis[9] = 2.890611442640554f * vx * vy * vzz;
+      basis[10] = 0.4570457994644658f * vy * ((4.0f * zz - xx) - yy);
+      basis[11] = 0.3731763325901154f * vzz * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
+      basis[12] = 0.4570457994644658f * vx * ((4.0f * zz - xx) - yy);
+      basis[13] = 1.445305721320277f * vzz * (xx - yy);
+      basis[14] = 0.5900435899266435f * vx * (xx - 3.0f * yy);
+    }
+    F3 g_dir = f3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      if (!(P.craw[ch] > 0.0f && P.craw[ch] < 1.0f) || g_col[ch] == 0.0f) continue;
+      const real gc = g_col[ch];
+      atomicAdd(b.d_sh + base + ch, gc);
+      for (uint32_t k = 0; k < nb && k < 15u; ++k) {
+        atomicAdd(b.d_sh + base + 3 + 3 * k + ch, gc * basis[k]);
+        g_dir = add(g_dir, mul(dbasis((int)k, P.dir), gc * ld(sh + 3 + 3 * k + ch)));
+      }
+    }
+    if (nb) {
+      const real proj = dot(g_dir, P.dir);
+      const F3 g_d = mul(sub(g_dir, mul(P.dir, proj)), 1.0f / P.dlen);
+      g_p = sub(g_p, g_d);
+    }
+  }
+  atomicAdd(b.d_pos + (size_t)id * 3 + 0, g_p.x);
+  atomicAdd(b.d_pos + (size_t)id * 3 + 1, g_p.y);
+  atomicAdd(b.d_pos + (size_t)id * 3 + 2, g_p.z);
+}
+
+}  // namespace
+
+cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s) {
+  const FrameArgs& a = b.f;
+  if (a.N) k_bwd_prep<<<(a.N + 255) / 256, 256, 0, s>>>(b);
+  if (a.tile_count) {
+    const uint32_t want = (2u * a.tile_count + kBwdWarps - 1) / kBwdWarps;
+    const uint32_t cap = (uint32_t)a.num_sms * 8u;
+    k_raster_bwd<<<want < cap ? want : cap, kBwdWarps * 32, 0, s>>>(b);
+  }
+  if (a.N) k_project_bwd<<<(a.N + 127) / 128, 128, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+}  // namespace hdsr

@@ -23,6 +23,7 @@ enum Ctl : int {
   kCtlScanNTile = 8,   // dynamic tile counters of the scans
   kCtlScanMTile = 9,
   kCtlRasterTile = 19, // dynamic tile counter of the rasteriser
+  kCtlBwdTile = 20,    // dynamic tile counter of the adjoint rasteriser
   kCtlWords = 64
 };
 
@@ -129,6 +130,22 @@ struct FrameArgs {
   int num_sms;
 };
 
+// Adjoint of one frame (hdsr_encode_backward): the frame's own buffers plus
+// the incoming image gradient and the outgoing scene gradients.
+constexpr uint32_t kG2d = 12;   // per-sortRank screen-space gradient words (9 used)
+struct BwdArgs {
+  FrameArgs f;
+  const float* d_color;           // dL/d(color output), rgba f32 per pixel
+  uint64_t d_color_pitch;         // bytes per row
+  float4* par;                    // per sortRank, 3 x float4: cx, cy, ia, ib | ic, opacity, r, g | b
+  float* g2d;                     // per sortRank: dL/d(cx, cy, ia, ib, ic, opacity, r, g, b)
+  float* d_pos;                   // per splat id: N*3
+  float* d_lsc;                   // N*3
+  float* d_rot;                   // N*4
+  float* d_opa;                   // N
+  float* d_sh;                    // N*(6 + 3K)
+};
+
 // Bounded spin for decoupled-lookback waits (iterations of ~100 ns).
 constexpr uint32_t kSpinLimit = 1u << 22;
 
@@ -151,6 +168,7 @@ cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launc
 cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 4 launches
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
+cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s);  // 3 launches
 
 // sizing helpers shared with the API
 constexpr uint32_t kScanItems = 16;

@@ -69,7 +69,8 @@ typedef struct hdsr_plan {
 #define HDSR_COLOR_RGBA32F 1u
 
 #define HDSR_CFG_KEEP_SORTED_KEYS 0x1u  /* compute the 20-bit log-depth keys per entry */
-#define HDSR_CFG_NO_GRAPH         0x2u  /* launch kernels directly, no CUDA graph  */
+#define HDSR_CFG_NO_GRAPH         0x2u  /* reserved: kernels are always launched directly */
+#define HDSR_CFG_BACKWARD         0x4u  /* allocate the adjoint's buffers (hdsr_encode_backward) */
 
 /* Options of createTileSplatCompositor — gpuTileSplatCompositor.ts:141-145
  * ({f16?}); the f16 composite variant is not rebuilt (FP32 transmittance). */
@@ -206,6 +207,30 @@ const char* hdsr_pass_name(uint32_t id);
 
 /* Number of kernels this handle has queued since creation. */
 uint64_t hdsr_launch_count(const hdsr_compositor* h);
+
+/* Gradients of one frame (no reference counterpart: the reference renders
+ * only). Input: dL/d(color output) as rgba f32 per pixel. Outputs, written
+ * (not accumulated), in the layouts of hdsr_scene_views, indexed by splat id:
+ * positions N*3, log-scales N*3, rotations N*4 (wxyz), activated opacities
+ * N, SH rows N*(6+3K) (dc, higher orders; the emissive slots get 0). */
+typedef struct hdsr_grad_views {
+  const float* d_color;   uint64_t d_color_pitch;   /* W x H rgba f32, bytes per row */
+  float* d_positions;
+  float* d_log_scales;
+  float* d_rotations;
+  float* d_opacities;
+  float* d_sh;
+} hdsr_grad_views;
+
+/* Adjoint of the last hdsr_encode_full (same scene, uniforms and tile
+ * entries), on `stream`. The differentiated function is the frame with the
+ * cache's f16 opacity and colour taken at fp32, every composite threshold
+ * (power > -4, alpha > 1/255, T >= 0.001, alpha cap 0.99) and projection
+ * clamp held fixed (clamped quantities pass no gradient). Needs a handle
+ * created with HDSR_CFG_BACKWARD; gradients w.r.t. the G-buffer outputs and
+ * the emissive colour are not computed. Float atomics: results are not
+ * bitwise reproducible from run to run. */
+hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* grads, void* stream);
 
 /* Per-tile splat counts of a projected frame (the counts of count_tile_refs)
  * without any device allocation and without a handle. No reference

@@ -79,6 +79,7 @@ def lib() -> ctypes.CDLL:
                                     c_int]
         L.orc_render_frame_f64.restype = c_int
         L.orc_render_frame_f64.argtypes = [c_void_p, POINTER(Scene), c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+        L.orc_project_f64.argtypes = [c_void_p, POINTER(Scene), c_void_p, c_int]
         L.orc_sort_back_to_front.restype = c_int
         L.orc_sort_back_to_front.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p, c_int]
         L.orc_gpu_sort_prototype_order.restype = c_int
@@ -203,6 +204,19 @@ def render_frame_f64(U, packed, sorted_indices, frame: dict, threads: int | None
     if rc != 0:
         raise RuntimeError("orc_render_frame_f64 failed")
     return out.reshape(H, W, 4)
+
+
+def project_f64(U, packed, sorted_indices, threads: int | None = None) -> np.ndarray:
+    """(N, 10) FP64 screen-space parameters per sortRank: cx, cy, ia, ib, ic,
+    opacity, r, g, b, visible."""
+    L = lib()
+    U = np.ascontiguousarray(U, np.float32)
+    scene, keep = scene_struct(packed, sorted_indices)
+    n = int(packed.count)
+    out = np.zeros((max(n, 1), 10), np.float64)
+    L.orc_project_f64(U.ctypes.data_as(c_void_p), ctypes.byref(scene), _p(out), threads or threads_default())
+    del keep
+    return out[:n]
 
 
 def sort_back_to_front(positions, view, threads: int = 1) -> np.ndarray:

@@ -939,6 +939,18 @@ static proj64 project_one_f64(const float* U, const orc_scene* s, uint32_t sortR
   return o;
 }
 
+void orc_project_f64(const float* U, const orc_scene* s, double* out, int threads) {
+  const uint32_t N = Uu(U, 22);
+  int nt = threads > 0 ? threads : 1;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t r = 0; r < (int64_t)N; ++r) {
+    proj64 p = project_one_f64(U, s, (uint32_t)r);
+    double* o = out + r * 10;
+    o[0] = p.cx; o[1] = p.cy; o[2] = p.ia; o[3] = p.ib; o[4] = p.ic;
+    o[5] = p.op; o[6] = p.r; o[7] = p.g; o[8] = p.b; o[9] = p.visible;
+  }
+}
+
 int orc_render_frame_f64(const float* U, const orc_scene* s, const uint32_t* counts,
                          const uint32_t* offsets, const uint32_t* entries, double* out,
                          int threads) {

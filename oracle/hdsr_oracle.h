@@ -144,6 +144,10 @@ int orc_render_frame_f64(const float* U, const orc_scene* s, const uint32_t* til
                          const uint32_t* tile_offsets, const uint32_t* tile_entries,
                          double* out_rgba, int threads);
 
+/* Per sortRank, the FP64 screen-space parameters of the twin: cx, cy, ia,
+ * ib, ic, opacity, r, g, b, visible (10 doubles). */
+void orc_project_f64(const float* U, const orc_scene* s, double* out, int threads);
+
 /* --- CPU depth sort baseline (splatSort.ts:32-55,178-195) ----------------
  * returns 0, -1 on a non-finite depth (the reference throws RangeError). */
 int orc_sort_back_to_front(const float* positions, uint32_t n, const float* view,

@@ -1,0 +1,238 @@
+"""The frame's adjoint (hdsr_encode_backward) and its torch.autograd binding.
+
+Gradients are checked against central differences of the oracle's FP64
+forward (same per-tile entry lists, no f16 rounding) on a 2,000-splat,
+64x64, SH degree 1 sub-scene of the training distribution. Tolerance: 1e-3
+relative; a gradient below 1% of the RMS gradient is held to 1e-3 of that
+floor instead (absolute 1e-5 x RMS: the fp32 sums over pixels carry about that
+much noise). Masked, as the threshold-adjacent entries of that comparison:
+ - parameters whose FP64 difference quotient changes between steps h and 4h
+   (the perturbation crosses a threshold of the composite);
+ - splats with a (pixel, entry) within 1e-4 relative of a threshold of the
+   composite (power -4, alpha 1/255, the 0.99 alpha cap, T 0.001) or of a
+   clamp (opacity 0.99, colour 0 or 1), where fp32 and FP64 may decide
+   differently.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from gpu_helpers import u32
+
+pytestmark = pytest.mark.gpu
+
+GROUPS = [("positions", "positions", 3), ("log_scales", "scales", 3), ("rotations", "rotations", 4),
+          ("opacities", "opacities", 1), ("sh", "sh_data", 15)]
+
+
+def _sub_scene(pkg, n=2000, W=64, H=64, seed=5):
+    sc = pkg.workloads.hot_scene(n, seed, sh_degree=1)
+    cam = pkg.camera.OrbitCamera(azimuth=0.4, elevation=0.2, distance=3.0)
+    packed = pkg.splats.pack_splat_attributes(sc)
+    plan = pkg.plan_tile_splat_compositor(W, H, 16, sc.count)
+    u, fr = pkg.frame_uniforms_for(plan, cam, sh_degree=1)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    return sc, packed, plan, u, order
+
+
+def _tensors(packed, order):
+    import torch
+
+    def t(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+    n = packed.count
+    return (t(packed.positions.reshape(n, 3)), t(packed.scales.reshape(n, 3)), t(packed.rotations.reshape(n, 4)),
+            t(packed.opacities.reshape(n)), t(packed.sh_data.reshape(n, -1)),
+            t(np.asarray(order, np.uint32).view(np.int32)))
+
+
+def _gpu_gradients(pkg, renderer, tens, u, weights):
+    import torch
+
+    pos, lsc, rot, opa, sh, srt = tens
+    renderer.forward_frame(pos, lsc, rot, opa, sh, srt, u)
+    grads = {"positions": torch.empty_like(pos), "log_scales": torch.empty_like(lsc),
+             "rotations": torch.empty_like(rot), "opacities": torch.empty_like(opa), "sh": torch.empty_like(sh)}
+    pkg.encode_backward(None, renderer.res, torch.from_numpy(weights).cuda(), grads)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in grads.items()}
+
+
+def threshold_adjacent_ranks(u, par, frame, rel=1e-4):
+    """sortRanks with a (pixel, entry) near a composite threshold or clamp,
+    traced in FP64 over the frame's entry lists."""
+    U = np.asarray(u, np.float32)
+    cols, rows = int(U[20:21].view(np.uint32)[0]), int(U[21:22].view(np.uint32)[0])
+    W, H = int(U[16]), int(U[17])
+    counts, offs, ents = frame["tile_counts"], frame["tile_offsets"], frame["tile_entries"]
+    flagged = set()
+    op = par[:, 5]
+    for r in np.nonzero((np.abs(op - 0.99) < rel) | (op == 0.0))[0]:
+        flagged.add(int(r))
+    col = par[:, 6:9]
+    for r in np.nonzero(((col < rel) | (col > 1 - rel)).any(1))[0]:
+        flagged.add(int(r))
+    gy, gx = np.mgrid[0:16, 0:16]
+    for ty in range(rows):
+        for tx in range(cols):
+            t = int(u32_morton(tx, ty))
+            X, Y = tx * 16 + gx + 0.5, ty * 16 + gy + 0.5
+            inside = (X < W) & (Y < H)
+            T = np.ones(X.shape)
+            for e in ents[offs[t]:offs[t] + counts[t]]:
+                cx, cy, ia, ib, ic, o = par[e, :6]
+                dx, dy = X - cx, Y - cy
+                pw = -0.5 * ia * dx * dx - 0.5 * ic * dy * dy - ib * dx * dy
+                raw = o * np.exp(pw)
+                a = np.minimum(raw, 0.99)
+                near = (np.abs(pw + 4.0) < 4.0 * rel) | (np.abs(a * 255.0 - 1.0) < rel) | \
+                       (np.abs(raw / 0.99 - 1.0) < rel) | (np.abs(T / 0.001 - 1.0) < rel)
+                if (near & inside).any():
+                    flagged.add(int(e))
+                valid = (pw > -4.0) & (a > 1.0 / 255.0) & (T >= 0.001)
+                T = np.where(valid, T * (1.0 - a), T)
+    return flagged
+
+
+def u32_morton(x, y):
+    a, b = x, y
+    out = 0
+    for i in range(16):
+        out |= ((a >> i) & 1) << (2 * i) | ((b >> i) & 1) << (2 * i + 1)
+    return out
+
+
+def test_gradients_match_fp64_central_differences(cuda, pkg, orc):
+    sc, packed, plan, u, order = _sub_scene(pkg)
+    renderer = pkg.differentiable.SplatFrameRenderer(plan.viewport_width, plan.viewport_height, sc.count,
+                                                    sh_degree=1)
+    tens = _tensors(packed, order)
+    rng = np.random.default_rng(0)
+    weights = rng.standard_normal((plan.viewport_height, plan.viewport_width, 4)).astype(np.float32)
+    G = _gpu_gradients(pkg, renderer, tens, u, weights)
+    frame = orc.render_frame(u, packed, order)
+    assert np.array_equal(u32(renderer.res.buffer("tile_entries", count=frame["total_pairs"])),
+                          frame["tile_entries"])
+    par = orc.project_f64(u, packed, order)
+    flagged = threshold_adjacent_ranks(u, par, frame)
+    inv = np.empty(sc.count, np.int64)
+    inv[np.asarray(order, np.int64)] = np.arange(sc.count)
+
+    def loss(pk):
+        return float((orc.render_frame_f64(u, pk, order, frame) * weights).sum())
+
+    contributing = np.nonzero(np.abs(G["opacities"]) > 0)[0]
+    clean = np.array([i for i in contributing if int(inv[i]) not in flagged])
+    assert clean.size > 200, (contributing.size, clean.size)
+    rows = []
+    for trial in range(200):
+        gname, pname, width = GROUPS[trial % len(GROUPS)]
+        sid = int(rng.choice(clean))
+        j = int(rng.integers(0, 9 if gname == "sh" else width))  # not the emissive slots
+        idx = sid * width + j
+        arr = getattr(packed, pname)
+        flat = arr.reshape(-1)
+        th = float(flat[idx])
+        fds = []
+        for h in (1e-6, 4e-6):
+            hh = h * max(1.0, abs(th))
+            tp, tm = np.float32(th + hh), np.float32(th - hh)
+            pk = copy.copy(packed)
+            a2 = flat.copy()
+            a2[idx] = tp
+            setattr(pk, pname, a2.reshape(arr.shape))
+            lp = loss(pk)
+            a2[idx] = tm
+            setattr(pk, pname, a2.reshape(arr.shape))
+            lm = loss(pk)
+            fds.append((lp - lm) / (float(tp) - float(tm)))
+        rows.append((trial % len(GROUPS), float(G[gname].reshape(-1)[idx]), fds[0], fds[1]))
+    rows = np.array(rows)
+    consistent = np.abs(rows[:, 2] - rows[:, 3]) <= 1e-4 * np.maximum(np.abs(rows[:, 2]), 1e-3)
+    assert consistent.sum() >= 150
+    r = rows[consistent]
+    scale = np.sqrt(np.mean(r[:, 2] ** 2))
+    rel = np.abs(r[:, 1] - r[:, 2]) / np.maximum(np.abs(r[:, 2]), 1e-2 * scale)
+    for k, (gname, _, _) in enumerate(GROUPS):
+        sel = r[:, 0] == k
+        assert sel.sum() >= 20, gname
+        assert rel[sel].max() <= 1e-3, (gname, float(rel[sel].max()), r[sel][np.argmax(rel[sel])])
+    renderer.destroy()
+
+
+def test_autograd_matches_the_c_abi_and_trains(cuda, pkg):
+    import torch
+
+    sc, packed, plan, u, order = _sub_scene(pkg, n=3000, W=96, H=80, seed=8)
+    renderer = pkg.differentiable.SplatFrameRenderer(plan.viewport_width, plan.viewport_height, sc.count,
+                                                    sh_degree=1)
+    pos, lsc, rot, opa, sh, srt = _tensors(packed, order)
+    target = renderer.render(pos, lsc, rot, opa, sh, srt, u).detach().clone()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    params = [pos + 0.01 * torch.randn(pos.shape, device="cuda", generator=g), lsc.clone(), rot.clone(),
+              torch.logit(opa.clamp(1e-4, 1 - 1e-4)), sh.clone()]
+    for p in params:
+        p.requires_grad_(True)
+    img = renderer.render(params[0], params[1], params[2], torch.sigmoid(params[3]), params[4], srt, u)
+    loss = ((img - target) ** 2).mean()
+    loss.backward()
+    # the same frame's gradients straight through the C ABI
+    d_color = (2.0 * (img.detach() - target) / img.numel()).contiguous()
+    direct = {k: torch.empty_like(v) for k, v in (("positions", pos), ("log_scales", lsc), ("rotations", rot),
+                                                  ("opacities", opa), ("sh", sh))}
+    renderer.forward_frame(params[0].detach(), params[1].detach(), params[2].detach(),
+                           torch.sigmoid(params[3]).detach(), params[4].detach(), srt, u)
+    pkg.encode_backward(None, renderer.res, d_color, direct)
+    torch.cuda.synchronize()
+    for p, k in zip(params[:3], ("positions", "log_scales", "rotations")):
+        assert torch.isfinite(p.grad).all()
+        assert torch.allclose(p.grad, direct[k], rtol=1e-4, atol=1e-9), k
+    s = torch.sigmoid(params[3]).detach()
+    assert torch.allclose(params[3].grad, direct["opacities"] * s * (1 - s), rtol=1e-4, atol=1e-9)
+    assert torch.allclose(params[4].grad, direct["sh"], rtol=1e-4, atol=1e-9)
+    assert float(params[0].grad.abs().sum()) > 0
+    # the gradient is a descent direction: normalised steps on the positions
+    # (at most 5e-4 per coordinate) lower the loss
+    first = float(loss.detach())
+    cur = params[0].detach().clone()
+    grad = params[0].grad.detach()
+    for _ in range(5):
+        cur = cur - 5e-4 * grad / grad.abs().max()
+        p0 = cur.clone().requires_grad_(True)
+        img = renderer.render(p0, params[1].detach(), params[2].detach(), torch.sigmoid(params[3]).detach(),
+                              params[4].detach(), srt, u)
+        loss = ((img - target) ** 2).mean()
+        loss.backward()
+        grad = p0.grad.detach()
+    assert float(loss.detach()) < first
+    renderer.destroy()
+
+
+def test_backward_is_repeatable_and_validated(cuda, pkg):
+    import torch
+
+    sc, packed, plan, u, order = _sub_scene(pkg, n=1500, W=64, H=48, seed=9)
+    renderer = pkg.differentiable.SplatFrameRenderer(plan.viewport_width, plan.viewport_height, sc.count,
+                                                    sh_degree=1)
+    tens = _tensors(packed, order)
+    w = np.random.default_rng(1).standard_normal((plan.viewport_height, plan.viewport_width, 4)).astype(np.float32)
+    a = _gpu_gradients(pkg, renderer, tens, u, w)
+    b = _gpu_gradients(pkg, renderer, tens, u, w)
+    for k in a:
+        assert np.allclose(a[k], b[k], rtol=1e-5, atol=1e-7), k
+    # a handle without the adjoint buffers refuses; so does one with no frame
+    res = pkg.create_tile_splat_compositor(plan)
+    grads = {k: torch.zeros(1, device="cuda") for k in ("positions", "log_scales", "rotations", "opacities", "sh")}
+    d = torch.zeros((plan.viewport_height, plan.viewport_width, 4), device="cuda")
+    with pytest.raises(pkg._lib.HdsrError) as e:
+        pkg.encode_backward(None, res, d, grads)
+    assert e.value.status == 6
+    res.destroy()
+    fresh = pkg.create_tile_splat_compositor(plan, backward=True)
+    with pytest.raises(pkg._lib.HdsrError) as e:
+        pkg.encode_backward(None, fresh, d, grads)
+    assert e.value.status == 7
+    fresh.destroy()
+    renderer.destroy()
