@@ -156,6 +156,78 @@ def pass_bytes(name: str, N: int, P: int, Q: int, S: int, sh_floats: int) -> flo
     return None
 
 
+def run_train(pkg, args, dev) -> dict:
+    """fwd+bwd iterations/s on the training workload (500k splats, SH 1,
+    1024x1024) against plain forward frames/s on the same scene.
+
+    One iteration: hdsr_encode_full, the L2 loss gradient against a fixed
+    target (a torch elementwise kernel), hdsr_encode_backward. The target is
+    the frame of the scene with means + N(0, 0.01) and colours + N(0, 0.05).
+    Timed with CUDA events over K iterations, no host synchronisation inside."""
+    import torch
+
+    wl = pkg.workloads.train500k()
+    n = wl.scene.count
+    packed = pkg.splats.pack_splat_attributes(wl.scene)
+    rng = np.random.default_rng(17)
+    plan = pkg.plan_tile_splat_compositor(wl.width, wl.height, 16, n)
+    u, fr = pkg.frame_uniforms_for(plan, wl.cameras[0], sh_degree=wl.scene.sh_degree)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    r = pkg.differentiable.SplatFrameRenderer(wl.width, wl.height, n, sh_degree=wl.scene.sh_degree, device=dev)
+
+    def t(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    pos, lsc, rot = t(packed.positions.reshape(n, 3)), t(packed.scales.reshape(n, 3)), t(packed.rotations.reshape(n, 4))
+    opa, sh = t(packed.opacities.reshape(n)), t(packed.sh_data.reshape(n, -1))
+    srt = t(np.asarray(order, np.uint32).view(np.int32))
+    tpos = pos + t(rng.normal(0.0, 0.01, (n, 3)).astype(np.float32))
+    tsh = sh.clone()
+    tsh[:, :3] += t(rng.normal(0.0, 0.05, (n, 3)).astype(np.float32))
+    target = r.forward_frame(tpos, lsc, rot, opa, tsh, srt, u).clone()
+    r.forward_frame(pos, lsc, rot, opa, sh, srt, u)  # sizes the pair capacity, binds the scene
+    res = r.res
+    grads = {"positions": torch.empty_like(pos), "log_scales": torch.empty_like(lsc),
+             "rotations": torch.empty_like(rot), "opacities": torch.empty_like(opa), "sh": torch.empty_like(sh)}
+    d_color = torch.empty_like(target)
+    scale = 2.0 / target.numel()
+    stream = torch.cuda.current_stream()
+
+    def fwd():
+        pkg.encode_full_compute_compositor_pipeline(stream, res)
+
+    def it():
+        fwd()
+        torch.sub(r.color, target, out=d_color)
+        d_color.mul_(scale)
+        pkg.encode_backward(stream, res, d_color, grads)
+
+    def timed(fn, k):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(k):
+            fn()
+        e.record(stream)
+        e.synchronize()
+        return s.elapsed_time(e) / k
+
+    k = max(args.steps, 5)
+    fwd_ms = timed(fwd, k)
+    it_ms = timed(it, k)
+    st = res.check_frame()
+    loss = float(((r.color - target) ** 2).mean())
+    ok = all(bool(torch.isfinite(g).all()) for g in grads.values())
+    r.destroy()
+    return {"workload": "train500k_1024x1024", "splats": n, "sh_degree": wl.scene.sh_degree,
+            "pairs": int(st["total_pairs"]), "fwd_bwd_it_per_s": round(1000.0 / it_ms, 2),
+            "fwd_frames_per_s": round(1000.0 / fwd_ms, 2), "fwd_bwd_ms": round(it_ms, 4),
+            "fwd_ms": round(fwd_ms, 4), "bwd_over_fwd": round((it_ms - fwd_ms) / fwd_ms, 3),
+            "loss": loss, "grads_finite": ok, "timing": "CUDA events, K iterations back to back"}
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -237,6 +309,8 @@ def run_ours(args, rank, world, local):
         "pass_share": {k: round(v / frame_ms, 4) for k, v in mean_pass.items()},
         "roofline": roofline, "clocks": clocks.summary(),
     }
+    if rank == 0 and not args.no_train:
+        out["train"] = run_train(pkg, args, dev)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(pkg, wl, F)
     if world > 1:
@@ -366,6 +440,7 @@ def main():
     ap.add_argument("--workload", default="hot760k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiler runs)")
+    ap.add_argument("--no-train", action="store_true", help="skip the fwd+bwd leg (train500k)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
