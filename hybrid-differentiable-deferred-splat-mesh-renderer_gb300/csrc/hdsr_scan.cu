@@ -51,6 +51,8 @@ __device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t
 }
 
 struct SbScan {
+  // an overflowed frame skipped the depth sort: order holds no permutation
+  static __device__ bool skip(const FrameArgs& a) { return (a.ctl[kCtlFlags] & 0x1u) != 0u; }
   static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
@@ -60,6 +62,7 @@ struct SbScan {
 };
 
 struct TileScan {
+  static __device__ bool skip(const FrameArgs&) { return false; }  // it decides the overflow
   static __device__ uint32_t size(const FrameArgs& a) { return a.M; }
   static __device__ uint32_t counter() { return kCtlScanMTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_m; }
@@ -90,6 +93,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(FrameArgs a) {
   __shared__ uint32_t s_warp[kScanThreads / 32];
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_prefix;
+  if (Policy::skip(a)) return;
   const uint32_t n = Policy::size(a);
   const uint32_t num_tiles = (n + kScanTile - 1) / kScanTile;
   const uint32_t epoch = a.ctl[kCtlEpoch];

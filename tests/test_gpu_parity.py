@@ -173,6 +173,8 @@ def test_composite_only_and_determinism(cuda, pkg, orc):
 
 
 def test_overflow_is_reported_not_faulted(cuda, pkg, orc):
+    import torch
+
     wl = pkg.workloads.plain50k()
     g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height, pair_capacity=1000)
     st = g["res"].query_status()
@@ -180,6 +182,14 @@ def test_overflow_is_reported_not_faulted(cuda, pkg, orc):
     assert st["total_pairs"] > 1000 and st["device_flags"] & pkg._lib.DEV_OVERFLOW
     with pytest.raises(pkg._lib.HdsrError):
         pkg.encode_composite_only(None, g["res"])
+    # an overflowed frame skips the depth sort, so nothing may read the
+    # depth order: with it full of out-of-range values the frame still only
+    # reports the overflow
+    g["res"].buffer("depth_order").fill_(-1)
+    torch.cuda.synchronize()
+    pkg.encode_full_compute_compositor_pipeline(None, g["res"])
+    st = g["res"].query_status()
+    assert st["status"] == pkg._lib.HDSR_ERR_OVERFLOW and st["total_pairs"] > 1000
 
 
 def test_bad_sorted_index_is_flagged(cuda, pkg, orc):
