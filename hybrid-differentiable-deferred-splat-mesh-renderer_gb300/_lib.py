@@ -22,8 +22,13 @@ STATUS_NAMES = {
     6: "HDSR_ERR_UNSUPPORTED",
     7: "HDSR_ERR_NOT_BOUND",
 }
+HDSR_ERR_INVALID_ARG = 1
+HDSR_ERR_OOM = 2
+HDSR_ERR_CUDA = 3
 HDSR_ERR_OVERFLOW = 4
 HDSR_ERR_TIMEOUT = 5
+HDSR_ERR_UNSUPPORTED = 6
+HDSR_ERR_NOT_BOUND = 7
 
 COLOR_RGBA16F = 0
 COLOR_RGBA32F = 1
@@ -84,6 +89,29 @@ class GradViews(ctypes.Structure):
                 ("d_sh", c_void_p)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_uint64), ("max_in_flight", c_uint32), ("flags", c_uint32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("scene_id", c_uint32), ("color_format", c_uint32), ("uniforms", c_float * 64),
+                ("outputs", OutputViews)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("reruns", c_uint32), ("total_pairs", c_uint64),
+                ("submit_ms", c_double), ("start_ms", c_double), ("done_ms", c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("budget_bytes", c_uint64), ("scene_bytes", c_uint64), ("slot_bytes", c_uint64),
+                ("scenes", c_uint32), ("slots", c_uint32), ("graphs", c_uint32), ("evictions", c_uint32),
+                ("completed", c_uint64), ("reruns", c_uint64)]
+
+
+SERVER_NO_GRAPH = 0x1
+
+
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_pairs", c_uint64), ("pair_capacity", c_uint64), ("visible_splats", c_uint32),
                 ("superblock_entries", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
@@ -105,6 +133,13 @@ SIGNATURES = {
     "hdsr_bind_scene": (c_int, [c_void_p, POINTER(SceneViews)]),
     "hdsr_bind_outputs": (c_int, [c_void_p, POINTER(OutputViews)]),
     "hdsr_encode_backward": (c_int, [c_void_p, POINTER(GradViews), c_void_p]),
+    "hdsr_server_create": (c_int, [POINTER(ServerConfig), POINTER(c_void_p)]),
+    "hdsr_server_destroy": (None, [c_void_p]),
+    "hdsr_server_add_scene": (c_int, [c_void_p, c_uint32, POINTER(SceneViews)]),
+    "hdsr_server_submit": (c_int, [c_void_p, POINTER(Request), POINTER(c_uint64)]),
+    "hdsr_server_wait": (c_int, [c_void_p, c_uint64, POINTER(RequestResult)]),
+    "hdsr_server_query": (c_int, [c_void_p, POINTER(ServerStats)]),
+    "hdsr_server_last_error": (c_char_p, [c_void_p]),
     "hdsr_write_tile_splat_frame_uniforms": (None, [POINTER(c_float), POINTER(c_float), POINTER(Plan), c_float,
                                                     c_uint32, POINTER(c_float), POINTER(c_float),
                                                     POINTER(c_float), POINTER(c_float)]),

@@ -32,6 +32,7 @@ struct hdsr_compositor {
   int device = 0;
   FrameArgs args{};
   float4* bwd_par = nullptr;      // adjoint buffers (HDSR_CFG_BACKWARD)
+  uint64_t device_bytes = 0;      // sum of this handle's device allocations
   float* bwd_g2d = nullptr;
   std::vector<void*> allocs;
   float uniforms[64] = {};
@@ -82,6 +83,7 @@ hdsr_status dev_alloc(hdsr_compositor* h, T** p, uint64_t count, const char* wha
     return cuda_fail(h, e, msg);
   }
   h->allocs.push_back(ptr);
+  h->device_bytes += bytes;
   *p = static_cast<T*>(ptr);
   return HDSR_OK;
 }
@@ -89,6 +91,7 @@ hdsr_status dev_alloc(hdsr_compositor* h, T** p, uint64_t count, const char* wha
 void free_all(hdsr_compositor* h) {
   for (void* p : h->allocs) cudaFree(p);
   h->allocs.clear();
+  h->device_bytes = 0;
 }
 
 }  // namespace
@@ -345,7 +348,7 @@ static void mark(hdsr_compositor* h, cudaStream_t s, uint32_t id) {
   cudaEventRecord(h->ev[++h->ev_used], s);
 }
 
-static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
+static hdsr_status encode_checks(hdsr_compositor* h, bool full) {
   if (!h) return HDSR_ERR_INVALID_ARG;
   if (!h->scene_bound || !h->outputs_bound) return fail(h, HDSR_ERR_NOT_BOUND, "bind scene and outputs first");
   if (!h->have_uniforms) return fail(h, HDSR_ERR_NOT_BOUND, "set frame uniforms first");
@@ -353,68 +356,73 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
   uint32_t deg;
   std::memcpy(&deg, h->uniforms + 25, 4);
   if (deg != h->args.sh_degree) return fail(h, HDSR_ERR_INVALID_ARG, "uniform shDegree differs from the bound scene");
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return HDSR_OK;
+}
+
+// Every kernel of a full frame before the rasteriser (no host work, no
+// allocation: a CUDA graph can capture it).
+static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   FrameArgs& a = h->args;
-  h->ev_used = 0;
-  if (h->profiling) cudaEventRecord(h->ev[0], s);
-  cudaError_t e = cudaMemcpyAsync(const_cast<float*>(a.U), h->uniforms, 256, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(h, e, "upload uniforms");
-  mark(h, s, 0);
   const uint64_t n_splat_launch = a.N ? 1 : 0;
-  if (full) {
-    if ((e = launch_frame_init(a, s)) != cudaSuccess) return cuda_fail(h, e, "frame_init");
-    mark(h, s, 1);
-    if ((e = launch_project(a, s)) != cudaSuccess) return cuda_fail(h, e, "project");
-    mark(h, s, 2);
-    if ((e = launch_tile_counts(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_counts");
-    if (a.log_keys && (e = launch_depth_range(a, s)) != cudaSuccess) return cuda_fail(h, e, "depth_range");
-    mark(h, s, 3);
-    if ((e = launch_scan_tiles(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
-    mark(h, s, 5);
-    // splats: 4 passes over the 32 depth bits -> order (sortRanks by depth)
-    RadixJob dj{};
-    dj.count = a.ctl + kCtlSplats;
-    dj.flags = a.ctl + kCtlFlags;
-    dj.tile_digits = a.tile_digits;
-    dj.bin_base = a.bin_base;
-    dj.tiles_cap = a.radix_tiles_cap;
-    dj.out_low = a.order;
-    dj.low_mask = 0xFFFFFFFFull;
-    for (uint32_t p = 0; p < kDepthPasses; ++p) {
-      dj.in = (p & 1u) ? a.dkeys_b : a.dkeys_a;
-      dj.out = (p & 1u) ? a.dkeys_a : a.dkeys_b;
-      dj.shift = 32u + 8u * p;
-      dj.bits = 8u;
-      if ((e = launch_radix_pass(dj, p + 1 == kDepthPasses, a.num_sms, s)) != cudaSuccess)
-        return cuda_fail(h, e, "depth_sort");
-    }
-    mark(h, s, 6);
-    // superblock lists in depth order, sorted by superblock (stable)
-    if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
-    if ((e = launch_emit_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit_superblocks");
-    RadixJob sj = dj;
-    sj.count = a.ctl + kCtlSbPairs;
-    sj.out_low = nullptr;
-    const uint32_t sb_passes = a.sb_bits > kRadixBits ? 2u : 1u;
-    for (uint32_t p = 0; p < sb_passes; ++p) {
-      sj.in = (p & 1u) ? a.sbk_b : a.sbk_a;
-      sj.out = (p & 1u) ? nullptr : a.sbk_b;
-      sj.out_keys = (p & 1u) ? a.sbk_a : a.sbk_b;
-      sj.shift = kSbKeyShift + kRadixBits * p;
-      sj.bits = p == 0 ? (a.sb_bits < kRadixBits ? a.sb_bits : kRadixBits) : a.sb_bits - kRadixBits;
-      if ((e = launch_radix_pass(sj, p + 1 == sb_passes, a.num_sms, s)) != cudaSuccess)
-        return cuda_fail(h, e, "superblock_sort");
-    }
-    mark(h, s, 7);
-    if ((e = launch_tile_entries(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_entries");
-    mark(h, s, 8);
-    if (a.log_keys) {
-      if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
-      h->launches += 2;
-    }
-    h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 4 * kDepthPasses + 1 + n_splat_launch +
-                   4 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
+  cudaError_t e;
+  if ((e = launch_frame_init(a, s)) != cudaSuccess) return cuda_fail(h, e, "frame_init");
+  mark(h, s, 1);
+  if ((e = launch_project(a, s)) != cudaSuccess) return cuda_fail(h, e, "project");
+  mark(h, s, 2);
+  if ((e = launch_tile_counts(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_counts");
+  if (a.log_keys && (e = launch_depth_range(a, s)) != cudaSuccess) return cuda_fail(h, e, "depth_range");
+  mark(h, s, 3);
+  if ((e = launch_scan_tiles(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
+  mark(h, s, 5);
+  // splats: 4 passes over the 32 depth bits -> order (sortRanks by depth)
+  RadixJob dj{};
+  dj.count = a.ctl + kCtlSplats;
+  dj.flags = a.ctl + kCtlFlags;
+  dj.tile_digits = a.tile_digits;
+  dj.bin_base = a.bin_base;
+  dj.tiles_cap = a.radix_tiles_cap;
+  dj.out_low = a.order;
+  dj.low_mask = 0xFFFFFFFFull;
+  for (uint32_t p = 0; p < kDepthPasses; ++p) {
+    dj.in = (p & 1u) ? a.dkeys_b : a.dkeys_a;
+    dj.out = (p & 1u) ? a.dkeys_a : a.dkeys_b;
+    dj.shift = 32u + 8u * p;
+    dj.bits = 8u;
+    if ((e = launch_radix_pass(dj, p + 1 == kDepthPasses, a.num_sms, s)) != cudaSuccess)
+      return cuda_fail(h, e, "depth_sort");
   }
+  mark(h, s, 6);
+  // superblock lists in depth order, sorted by superblock (stable)
+  if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
+  if ((e = launch_emit_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit_superblocks");
+  RadixJob sj = dj;
+  sj.count = a.ctl + kCtlSbPairs;
+  sj.out_low = nullptr;
+  const uint32_t sb_passes = a.sb_bits > kRadixBits ? 2u : 1u;
+  for (uint32_t p = 0; p < sb_passes; ++p) {
+    sj.in = (p & 1u) ? a.sbk_b : a.sbk_a;
+    sj.out = (p & 1u) ? nullptr : a.sbk_b;
+    sj.out_keys = (p & 1u) ? a.sbk_a : a.sbk_b;
+    sj.shift = kSbKeyShift + kRadixBits * p;
+    sj.bits = p == 0 ? (a.sb_bits < kRadixBits ? a.sb_bits : kRadixBits) : a.sb_bits - kRadixBits;
+    if ((e = launch_radix_pass(sj, p + 1 == sb_passes, a.num_sms, s)) != cudaSuccess)
+      return cuda_fail(h, e, "superblock_sort");
+  }
+  mark(h, s, 7);
+  if ((e = launch_tile_entries(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_entries");
+  mark(h, s, 8);
+  if (a.log_keys) {
+    if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
+    h->launches += 2;
+  }
+  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 4 * kDepthPasses + 1 + n_splat_launch +
+                 4 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
+  return HDSR_OK;
+}
+
+static hdsr_status encode_raster(hdsr_compositor* h, cudaStream_t s, bool full) {
+  FrameArgs& a = h->args;
+  cudaError_t e;
   if (!full) {
     // composite-only reuses the frame's entries; the raster's tile counter
     // is the one control word it must start from zero
@@ -428,6 +436,20 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
   h->has_last_stream = true;
   if (full) h->sorted_valid = true;
   return HDSR_OK;
+}
+
+static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
+  hdsr_status st = encode_checks(h, full);
+  if (st != HDSR_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  FrameArgs& a = h->args;
+  h->ev_used = 0;
+  if (h->profiling) cudaEventRecord(h->ev[0], s);
+  cudaError_t e = cudaMemcpyAsync(const_cast<float*>(a.U), h->uniforms, 256, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "upload uniforms");
+  mark(h, s, 0);
+  if (full && (st = encode_pre_raster(h, s)) != HDSR_OK) return st;
+  return encode_raster(h, s, full);
 }
 
 hdsr_status hdsr_encode_full(hdsr_compositor* h, void* stream) { return encode(h, stream, true); }
@@ -563,3 +585,23 @@ const char* hdsr_pass_name(uint32_t id) { return id < kNumPassNames ? kPassNames
 uint64_t hdsr_launch_count(const hdsr_compositor* h) { return h ? h->launches : 0u; }
 
 }  // extern "C"
+
+// ---- internal entry points of the serving loop (C++ linkage) --------------
+namespace hdsr {
+
+uint64_t handle_device_bytes(const hdsr_compositor* h) { return h ? h->device_bytes : 0u; }
+
+const FrameArgs* handle_args(const hdsr_compositor* h) { return h ? &h->args : nullptr; }
+
+int handle_frame_checks(hdsr_compositor* h) { return encode_checks(h, true); }
+
+int handle_upload_uniforms(hdsr_compositor* h, const float* pinned_uniforms, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(const_cast<float*>(h->args.U), pinned_uniforms, 256, cudaMemcpyHostToDevice, s);
+  return e == cudaSuccess ? HDSR_OK : cuda_fail(h, e, "upload uniforms");
+}
+
+int handle_encode_pre_raster(hdsr_compositor* h, cudaStream_t s) { return encode_pre_raster(h, s); }
+
+int handle_encode_raster(hdsr_compositor* h, cudaStream_t s) { return encode_raster(h, s, true); }
+
+}  // namespace hdsr

@@ -170,6 +170,18 @@ cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s);  // 3 launches
 
+// internal entry points of one compositor handle for the serving loop
+// (hdsr_api.cu); C++ linkage, not part of the C ABI
+}  // namespace hdsr
+struct hdsr_compositor;
+namespace hdsr {
+uint64_t handle_device_bytes(const hdsr_compositor* h);
+const FrameArgs* handle_args(const hdsr_compositor* h);
+int handle_frame_checks(hdsr_compositor* h);                       // hdsr_status
+int handle_upload_uniforms(hdsr_compositor* h, const float* pinned_uniforms, cudaStream_t s);
+int handle_encode_pre_raster(hdsr_compositor* h, cudaStream_t s);  // capturable
+int handle_encode_raster(hdsr_compositor* h, cudaStream_t s);
+
 // sizing helpers shared with the API
 constexpr uint32_t kScanItems = 16;
 constexpr uint32_t kScanThreads = 256;

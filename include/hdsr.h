@@ -232,6 +232,58 @@ typedef struct hdsr_grad_views {
  * bitwise reproducible from run to run. */
 hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* grads, void* stream);
 
+/* ---- Serving loop ---------------------------------------------------------
+ * No reference counterpart: the reference renders one scene per page
+ * (splatRenderer.ts loadScene :866-961, renderFrame :1024-1140). A server
+ * keeps scenes resident on the device and renders (scene, camera, viewport)
+ * requests: each request runs on an idle compositor handle ("slot") of its
+ * (scene, viewport, colour format), with its own stream; slots are created on
+ * demand inside an HBM budget (idle slots are evicted least recently used
+ * first), a slot's kernels before the rasteriser run as one CUDA graph after
+ * its first frame, and a frame that overflows its slot is re-run once on a
+ * slot sized to it. Results do not depend on what else is in flight. */
+typedef struct hdsr_server hdsr_server;
+
+#define HDSR_SERVER_NO_GRAPH 0x1u   /* launch every kernel directly */
+
+typedef struct hdsr_server_config {
+  uint64_t hbm_budget_bytes;    /* resident scenes + slots, bytes (> 0) */
+  uint32_t max_in_flight;       /* frames running at once, 1..64 */
+  uint32_t flags;               /* HDSR_SERVER_* */
+} hdsr_server_config;
+
+typedef struct hdsr_request {
+  uint32_t scene_id;
+  uint32_t color_format;        /* HDSR_COLOR_* */
+  float uniforms[64];           /* hdsr_write_tile_splat_frame_uniforms: gives the viewport */
+  hdsr_output_views outputs;    /* caller-owned device images of that viewport */
+} hdsr_request;
+
+typedef struct hdsr_request_result {
+  int32_t status;               /* hdsr_status of the frame */
+  uint32_t reruns;              /* overflow re-runs on a larger slot */
+  uint64_t total_pairs;
+  double submit_ms, start_ms, done_ms;  /* host clock, ms since the server was created */
+} hdsr_request_result;
+
+typedef struct hdsr_server_stats {
+  uint64_t budget_bytes, scene_bytes, slot_bytes;
+  uint32_t scenes, slots, graphs, evictions;
+  uint64_t completed, reruns;
+} hdsr_server_stats;
+
+hdsr_status hdsr_server_create(const hdsr_server_config* cfg, hdsr_server** out);
+void hdsr_server_destroy(hdsr_server* s);
+/* Registers resident device arrays (borrowed; the caller keeps them alive
+ * and unchanged while the server uses them). Counted against the budget. */
+hdsr_status hdsr_server_add_scene(hdsr_server* s, uint32_t scene_id, const hdsr_scene_views* scene);
+/* Queues a request; returns at once with a ticket. */
+hdsr_status hdsr_server_submit(hdsr_server* s, const hdsr_request* req, uint64_t* ticket);
+/* Blocks until the ticket's frame is complete on the device. */
+hdsr_status hdsr_server_wait(hdsr_server* s, uint64_t ticket, hdsr_request_result* result);
+hdsr_status hdsr_server_query(hdsr_server* s, hdsr_server_stats* stats);
+const char* hdsr_server_last_error(const hdsr_server* s);
+
 /* Per-tile splat counts of a projected frame (the counts of count_tile_refs)
  * without any device allocation and without a handle. No reference
  * counterpart: the reference only counts inside its full pipeline.

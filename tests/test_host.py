@@ -134,3 +134,14 @@ def test_hot_camera_has_twenty_hot_tiles(orc, pkg, hdsr_lib):
     L.orc_count_tile_refs(u.ctypes.data_as(ctypes.c_void_p), wl.scene.count, cache.ctypes.data_as(ctypes.c_void_p),
                           plan.morton_tile_count, counts.ctypes.data_as(ctypes.c_void_p))
     assert int((counts > 4096).sum()) >= 20
+
+
+def test_server_rejects_bad_configs_without_a_gpu(pkg, hdsr_lib):
+    import ctypes
+
+    out = ctypes.c_void_p()
+    for budget, inflight in ((0, 4), (1 << 30, 0), (1 << 30, 65)):
+        cfg = pkg._lib.ServerConfig(budget, inflight, 0)
+        assert hdsr_lib.hdsr_server_create(ctypes.byref(cfg), ctypes.byref(out)) == pkg._lib.HDSR_ERR_INVALID_ARG
+    assert hdsr_lib.hdsr_server_create(None, ctypes.byref(out)) == pkg._lib.HDSR_ERR_INVALID_ARG
+    assert hdsr_lib.hdsr_server_submit(None, None, None) == pkg._lib.HDSR_ERR_INVALID_ARG
