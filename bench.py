@@ -43,6 +43,11 @@ METRIC = "760k-splat 1080p frames/s"
 UNIT = "frames/s"
 
 
+def log(msg: str) -> None:
+    """Progress on stderr (stdout carries the one JSON line)."""
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
         os.environ.get("LOCAL_RANK", "0"))
@@ -228,6 +233,130 @@ def run_train(pkg, args, dev) -> dict:
             "loss": loss, "grads_finite": ok, "timing": "CUDA events, K iterations back to back"}
 
 
+SERVE_RESOLUTIONS = [(512, 512), (1280, 720), (1920, 1080)]
+
+
+def run_serve(pkg, args, dev) -> dict:
+    """Serving: 8 resident scenes (N log-uniform in [100k, 3M], the hot-tile
+    distribution, SH 0), 2,000 requests of a random scene, random orbit
+    camera and a resolution of {512x512, 1280x720, 1920x1080}, 120 GB budget.
+
+    plain: the per-frame path, one request at a time (encode, then read the
+    frame status: one host round trip per frame), one handle per
+    (scene, resolution). server: hdsr_server_* with every request queued at
+    once (saturated throughput), then Poisson arrivals at 70% of that rate
+    for p50/p99 latency (submit to completion on the device, host clock).
+    Every key is rendered once before timing (slots sized, graphs captured)."""
+    import torch
+
+    rng = np.random.default_rng(41)
+    n_req = 2000
+    ns = np.exp(rng.uniform(np.log(1e5), np.log(3e6), 8)).astype(int)
+    scenes = {}
+    for sid, n in enumerate(ns):
+        sc = pkg.workloads.hot_scene(int(n), 100 + sid)
+        packed = pkg.splats.pack_splat_attributes(sc)
+        bufs = pkg.splats.upload_splat_attribute_buffers(packed, np.arange(sc.count, dtype=np.uint32), device=dev)
+        scenes[sid] = (sc, bufs)
+    reqs = []
+    for _ in range(n_req):
+        sid = int(rng.integers(0, 8))
+        W, H = SERVE_RESOLUTIONS[int(rng.integers(0, 3))]
+        cam = pkg.camera.OrbitCamera(azimuth=float(rng.uniform(0, 2 * np.pi)), elevation=float(rng.uniform(-0.5, 0.5)),
+                                     distance=float(rng.uniform(4.0, 9.0)))
+        plan = pkg.plan_tile_splat_compositor(W, H, 16, scenes[sid][0].count)
+        u, _ = pkg.frame_uniforms_for(plan, cam)
+        reqs.append((sid, W, H, u))
+    ring = 32  # output image sets per resolution, reused in submission order
+    outs = {r: [pkg.create_output_textures(pkg.plan_tile_splat_compositor(r[0], r[1], 16, 1), device=dev)
+                for _ in range(ring)] for r in SERVE_RESOLUTIONS}
+    keys = sorted({(sid, W, H) for sid, W, H, _ in reqs})
+
+    # plain per-frame path
+    handles = {}
+
+    def plain(sid, W, H, u, out):
+        sc, bufs = scenes[sid]
+        res = handles.get((sid, W, H))
+        if res is None:
+            res = pkg.create_tile_splat_compositor(pkg.plan_tile_splat_compositor(W, H, 16, sc.count))
+            handles[(sid, W, H)] = res
+        pkg.create_tile_splat_bind_groups(res, bufs, out[0], out[1])
+        pkg.write_frame_uniform_buffer(res, u)
+        pkg.encode_full_compute_compositor_pipeline(None, res)
+        st = res.query_status()
+        if st["status"] == pkg._lib.HDSR_ERR_OVERFLOW:
+            need = int(st["total_pairs"])
+            res.destroy()
+            res = pkg.create_tile_splat_compositor(pkg.plan_tile_splat_compositor(W, H, 16, sc.count),
+                                                   pair_capacity=need + need // 4 + 4096)
+            handles[(sid, W, H)] = res
+            return plain(sid, W, H, u, out)
+        return st
+
+    log("serving: scenes resident, plain path sizing")
+    for sid, W, H, u in reqs:  # size every handle on the requests themselves
+        plain(sid, W, H, u, outs[(W, H)][0])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i, (sid, W, H, u) in enumerate(reqs):
+        plain(sid, W, H, u, outs[(W, H)][i % ring])
+    plain_s = time.perf_counter() - t0
+    for res in handles.values():
+        res.destroy()
+    handles.clear()
+    torch.cuda.synchronize()
+
+    log(f"serving: plain path {n_req / plain_s:.1f} frames/s; server warm-up")
+    server = pkg.serving.Server(hbm_budget_bytes=120 << 30, max_in_flight=8)
+    for sid, (_, bufs) in scenes.items():
+        server.add_scene(sid, bufs)
+
+    def run_batch(arrivals=None):
+        tickets, lat = [], []
+        used = {r: [None] * ring for r in SERVE_RESOLUTIONS}
+        t_start = time.perf_counter()
+        results = []
+        for i, (sid, W, H, u) in enumerate(reqs):
+            slot = used[(W, H)]
+            if slot[i % ring] is not None:  # the output set is reused: its frame must be done
+                results.append(server.wait(slot[i % ring]))
+                slot[i % ring] = None
+            if arrivals is not None:
+                while time.perf_counter() - t_start < arrivals[i]:
+                    pass
+            color, gb = outs[(W, H)][i % ring]
+            slot[i % ring] = server.submit(sid, u, color, gb)
+        for r in SERVE_RESOLUTIONS:
+            for t in used[r]:
+                if t is not None:
+                    results.append(server.wait(t))
+        return time.perf_counter() - t_start, results
+
+    for sid, W, H in keys:  # warm: one frame per key twice (slot sizing, graph capture)
+        u = next(q[3] for q in reqs if q[:3] == (sid, W, H))
+        for _ in range(2):
+            color, gb = outs[(W, H)][0]
+            server.wait(server.submit(sid, u, color, gb))
+    log("serving: saturated run")
+    sat_s, sat_res = run_batch()
+    log(f"serving: {n_req / sat_s:.1f} frames/s saturated; Poisson run")
+    rate = 0.7 * n_req / sat_s
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    _, lat_res = run_batch(arrivals)
+    lat = np.array([r["done_ms"] - r["submit_ms"] for r in lat_res])
+    st = server.stats()
+    bad = sum(1 for r in sat_res + lat_res if r["status"] != 0)
+    server.destroy()
+    return {"workload": "serve8_mixed", "scene_splats": [int(x) for x in ns], "requests": n_req,
+            "resolutions": [f"{w}x{h}" for w, h in SERVE_RESOLUTIONS], "budget_gb": 120,
+            "plain_frames_per_s": round(n_req / plain_s, 1), "server_frames_per_s": round(n_req / sat_s, 1),
+            "speedup_vs_plain": round(plain_s / sat_s, 2), "offered_rps": round(rate, 1),
+            "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "slots": st["slots"], "graphs": st["graphs"], "evictions": st["evictions"], "reruns": st["reruns"],
+            "slot_gb": round(st["slot_bytes"] / 2 ** 30, 2), "failed": bad, "max_in_flight": 8}
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -277,6 +406,7 @@ def run_ours(args, rank, world, local):
     value = args.steps * world / total_s
 
     # end to end through the C ABI with host buffers
+    log(f"frames timed: {value:.1f} frames/s")
     e2e = None if args.no_e2e else run_e2e(pkg, F, args, stream, world, dev)
 
     # roofline of the dominant HBM-bound pass
@@ -310,7 +440,11 @@ def run_ours(args, rank, world, local):
         "roofline": roofline, "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_train:
+        log("training leg")
         out["train"] = run_train(pkg, args, dev)
+    if rank == 0 and not args.no_serve:
+        log("serving leg")
+        out["serve"] = run_serve(pkg, args, dev)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(pkg, wl, F)
     if world > 1:
@@ -441,6 +575,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiler runs)")
     ap.add_argument("--no-train", action="store_true", help="skip the fwd+bwd leg (train500k)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg (8 scenes, 2,000 requests)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -213,12 +213,15 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   if (s != HDSR_OK) { free_all(h); delete h; return s; }
   a.U = U;
   a.sbk_sorted = a.sb_bits > kRadixBits ? a.sbk_a : a.sbk_b;  // where the last superblock pass writes
-  // status words start at epoch 0, which no frame uses
-  e = cudaMemset(a.scan_status_n, 0, scan_tiles_n * 8);
-  if (e == cudaSuccess) e = cudaMemset(a.scan_status_m, 0, scan_tiles_m * 8);
-  if (e == cudaSuccess) e = cudaMemset(a.ctl, 0, kCtlWords * 4);
-  if (e == cudaSuccess) e = cudaMemset(U, 0, 256);
-  if (e != cudaSuccess) { s = cuda_fail(h, e, "cudaMemset"); free_all(h); delete h; return s; }
+  // status words start at epoch 0, which no frame uses. The clears run on the
+  // legacy stream and are complete when create returns: the caller's stream
+  // may be a non-blocking one, which does not wait for the legacy stream.
+  e = cudaMemsetAsync(a.scan_status_n, 0, scan_tiles_n * 8, cudaStreamLegacy);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.scan_status_m, 0, scan_tiles_m * 8, cudaStreamLegacy);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.ctl, 0, kCtlWords * 4, cudaStreamLegacy);
+  if (e == cudaSuccess) e = cudaMemsetAsync(U, 0, 256, cudaStreamLegacy);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
+  if (e != cudaSuccess) { s = cuda_fail(h, e, "clear handle state"); free_all(h); delete h; return s; }
   *out = h;
   return HDSR_OK;
 }
@@ -520,6 +523,8 @@ hdsr_status hdsr_query_status(hdsr_compositor* h, hdsr_frame_stats* st) {
   if (ctl[kCtlFlags] & HDSR_DEV_TIMEOUT) return fail(h, HDSR_ERR_TIMEOUT, "a device-side wait gave up");
   if (ctl[kCtlFlags] & HDSR_DEV_COUNT_MISMATCH)
     return fail(h, HDSR_ERR_CUDA, "internal check failed: tile counts and superblock lists disagree");
+  if (ctl[kCtlFlags] & HDSR_DEV_BAD_ENTRY)
+    return fail(h, HDSR_ERR_CUDA, "internal check failed: a list held a sortRank >= splat count");
   return HDSR_OK;
 }
 

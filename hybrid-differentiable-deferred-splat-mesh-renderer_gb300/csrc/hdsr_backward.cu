@@ -229,7 +229,7 @@ enum BField { B_CX, B_CY, B_KA, B_KB, B_KC, B_OP, B_R, B_G, B_B, B_IA, B_IB, B_I
 
 __device__ __forceinline__ void bwd_stage(const BwdArgs& b, float (*s)[32], uint32_t e, uint32_t lane) {
   const FrameArgs& a = b.f;
-  const uint32_t r = __ldg(a.entries + e);
+  const uint32_t r = checked_rank(__ldg(a.entries + e), a.N, a.ctl);
   const float4 p0 = b.par[(size_t)r * 3], p1 = b.par[(size_t)r * 3 + 1], p2 = b.par[(size_t)r * 3 + 2];
   s[B_CX][lane] = p0.x;
   s[B_CY][lane] = p0.y;

@@ -146,6 +146,15 @@ struct BwdArgs {
   float* d_sh;                    // N*(6 + 3K)
 };
 
+// A sortRank read from a list (tile entries, depth order) that must be < N:
+// out of range sets HDSR_DEV_BAD_ENTRY and yields 0, so a broken list is
+// reported instead of indexing outside the per-splat arrays.
+__device__ __forceinline__ uint32_t checked_rank(uint32_t r, uint32_t N, uint32_t* ctl) {
+  if (r < N) return r;
+  atomicOr(ctl + kCtlFlags, 0x10u);
+  return 0u;
+}
+
 // Bounded spin for decoupled-lookback waits (iterations of ~100 ns).
 constexpr uint32_t kSpinLimit = 1u << 22;
 

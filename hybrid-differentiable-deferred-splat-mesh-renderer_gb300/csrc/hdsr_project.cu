@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(256) k_emit_sb(FrameArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.N) return;
   if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t r = a.order[i];
+  const uint32_t r = checked_rank(a.order[i], a.N, a.ctl);
   const uint32_t box = a.aux[r].x;
   if (box == kSentinel) return;
   const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;

@@ -180,7 +180,7 @@ struct Row {
 };
 
 __device__ __forceinline__ Row load_row(const FrameArgs& a, uint32_t e) {
-  const uint32_t r = __ldg(a.entries + e);
+  const uint32_t r = checked_rank(__ldg(a.entries + e), a.N, a.ctl);
   Row w;
   w.g = __ldg(a.geo + r);
   w.ap = __ldg(a.app + r);

@@ -56,7 +56,7 @@ struct SbScan {
   static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
-  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.nsb[a.order[i]]; }
+  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.nsb[checked_rank(a.order[i], a.N, a.ctl)]; }
   static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) { a.sb_off[i] = excl; }
   static __device__ void finish(const FrameArgs& a, uint32_t total) { a.ctl[kCtlSbPairs] = total; }
 };

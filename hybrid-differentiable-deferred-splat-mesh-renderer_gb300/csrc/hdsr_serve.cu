@@ -62,6 +62,7 @@ struct Slot {
 struct Ticket {
   hdsr_request req{};
   hdsr_request_result res{};
+  cudaEvent_t ready = nullptr;  // legacy-stream work issued before submit
   bool done = false;
 };
 
@@ -198,6 +199,12 @@ hdsr_status launch_frame(hdsr_server* s, Slot* sl, Ticket& t) {
     server_fail(s, st, hdsr_last_error(h));
     return st;
   }
+  // the request's outputs (and anything else the caller queued on the legacy
+  // stream before submit) are ready first
+  if (t.ready && cudaStreamWaitEvent(sl->stream, t.ready, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return server_fail(s, HDSR_ERR_CUDA, "wait for the request's inputs");
+  }
   std::memcpy(sl->pinned_u, t.req.uniforms, 256);
   st = (hdsr_status)handle_upload_uniforms(h, sl->pinned_u, sl->stream);
   const bool use_graph = !(s->cfg.flags & HDSR_SERVER_NO_GRAPH);
@@ -250,6 +257,10 @@ hdsr_status launch_frame(hdsr_server* s, Slot* sl, Ticket& t) {
 }
 
 void finish_ticket(hdsr_server* s, Ticket& t, hdsr_status st) {
+  if (t.ready) {
+    cudaEventDestroy(t.ready);  // does not block: a pending event is released when it completes
+    t.ready = nullptr;
+  }
   t.res.status = st;
   t.done = true;
   if (t.res.done_ms == 0.0) t.res.done_ms = ms_since(s);
@@ -326,7 +337,7 @@ void dispatcher_main(hdsr_server* s) {
       hdsr_status st = HDSR_OK;
       if (flags & HDSR_DEV_OVERFLOW) st = HDSR_ERR_OVERFLOW;
       else if (flags & HDSR_DEV_TIMEOUT) st = HDSR_ERR_TIMEOUT;
-      else if (flags & HDSR_DEV_COUNT_MISMATCH) st = HDSR_ERR_CUDA;
+      else if (flags & (HDSR_DEV_COUNT_MISMATCH | HDSR_DEV_BAD_ENTRY)) st = HDSR_ERR_CUDA;
       finish_ticket(s, t, st);
       sl->busy = false;
       sl->last_used = ++s->use_clock;
@@ -500,6 +511,11 @@ hdsr_status hdsr_server_add_scene(hdsr_server* s, uint32_t scene_id, const hdsr_
       (!scene->positions || !scene->scales || !scene->rotations || !scene->opacities || !scene->material ||
        !scene->sh_data || !scene->sorted_indices))
     return server_fail(s, HDSR_ERR_INVALID_ARG, "a scene array is NULL");
+  // the scene's arrays may still be written by work on the legacy stream
+  if (cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) {
+    cudaGetLastError();
+    return server_fail(s, HDSR_ERR_CUDA, "synchronize before registering the scene");
+  }
   std::lock_guard<std::mutex> lock(s->mu);
   if (s->scenes.count(scene_id)) return server_fail(s, HDSR_ERR_INVALID_ARG, "scene id already registered");
   const uint64_t b = scene_device_bytes(*scene);
@@ -523,17 +539,30 @@ hdsr_status hdsr_server_submit(hdsr_server* s, const hdsr_request* req, uint64_t
     return server_fail(s, HDSR_ERR_INVALID_ARG, "uniform viewport must be whole pixels in 1..4080");
   if (!req->outputs.color || !req->outputs.depth || !req->outputs.normal || !req->outputs.material)
     return server_fail(s, HDSR_ERR_INVALID_ARG, "an output image is NULL");
+  cudaEvent_t ready = nullptr;
+  if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventRecord(ready, cudaStreamLegacy) != cudaSuccess) {
+    cudaGetLastError();
+    if (ready) cudaEventDestroy(ready);
+    return server_fail(s, HDSR_ERR_CUDA, "record the request's ready event");
+  }
   std::lock_guard<std::mutex> lock(s->mu);
   auto sc = s->scenes.find(req->scene_id);
-  if (sc == s->scenes.end()) return server_fail(s, HDSR_ERR_INVALID_ARG, "unknown scene id");
+  if (sc == s->scenes.end()) {
+    cudaEventDestroy(ready);
+    return server_fail(s, HDSR_ERR_INVALID_ARG, "unknown scene id");
+  }
   uint32_t n, deg;
   std::memcpy(&n, req->uniforms + 22, 4);
   std::memcpy(&deg, req->uniforms + 25, 4);
-  if (n != sc->second.views.splat_count || deg != sc->second.views.sh_degree)
+  if (n != sc->second.views.splat_count || deg != sc->second.views.sh_degree) {
+    cudaEventDestroy(ready);
     return server_fail(s, HDSR_ERR_INVALID_ARG, "uniform splatCount / shDegree differ from the scene");
+  }
   const uint64_t id = s->next_ticket++;
   Ticket& t = s->tickets[id];
   t.req = *req;
+  t.ready = ready;
   t.res.submit_ms = ms_since(s);
   s->queue.push_back(id);
   ++s->events;

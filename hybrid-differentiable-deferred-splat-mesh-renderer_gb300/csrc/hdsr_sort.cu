@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(256) k_log_depth_keys(FrameArgs a) {
     const uint32_t off = a.tile_off[t];
     const float2 tl = a.tile_log[t];
     for (uint32_t i = lane; i < c; i += 32u) {
-      const uint32_t r = a.entries[off + i];
+      const uint32_t r = checked_rank(a.entries[off + i], a.N, a.ctl);
       const uint32_t k = key20(log_depth(a.depth[r]), tl);
       a.sorted_keys[off + i] = ((unsigned long long)t << (20u + R)) | ((unsigned long long)k << R) | r;
     }

@@ -42,6 +42,7 @@ typedef enum hdsr_status {
 #define HDSR_DEV_TIMEOUT    0x2u  /* a lookback wait exceeded its spin limit    */
 #define HDSR_DEV_BAD_INDEX  0x4u  /* sortedIndices held an id >= splatCount     */
 #define HDSR_DEV_COUNT_MISMATCH 0x8u /* tile counts and tile lists disagree (bug)  */
+#define HDSR_DEV_BAD_ENTRY  0x10u /* an entry or order index >= N was skipped (bug) */
 
 /* planTileSplatCompositor input — gpuTileSplatCompositor.ts:109-116. */
 typedef struct hdsr_plan_input {
@@ -275,9 +276,13 @@ typedef struct hdsr_server_stats {
 hdsr_status hdsr_server_create(const hdsr_server_config* cfg, hdsr_server** out);
 void hdsr_server_destroy(hdsr_server* s);
 /* Registers resident device arrays (borrowed; the caller keeps them alive
- * and unchanged while the server uses them). Counted against the budget. */
+ * and unchanged while the server uses them). Counted against the budget.
+ * Synchronises the legacy default stream first (uploads still in flight). */
 hdsr_status hdsr_server_add_scene(hdsr_server* s, uint32_t scene_id, const hdsr_scene_views* scene);
-/* Queues a request; returns at once with a ticket. */
+/* Queues a request; returns at once with a ticket. Its frame starts after
+ * all work issued to the legacy default stream before the call (e.g. the
+ * allocation and clearing of its outputs); work on other streams that writes
+ * its outputs or scene must be complete. */
 hdsr_status hdsr_server_submit(hdsr_server* s, const hdsr_request* req, uint64_t* ticket);
 /* Blocks until the ticket's frame is complete on the device. */
 hdsr_status hdsr_server_wait(hdsr_server* s, uint64_t ticket, hdsr_request_result* result);
