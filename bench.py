@@ -48,6 +48,22 @@ def log(msg: str) -> None:
     print(f"[bench] {msg}", file=sys.stderr, flush=True)
 
 
+def slowest_rank_seconds(seconds: float, world: int, device) -> float:
+    """The timed region of the slowest rank (MAX all-reduce; one rank: itself)."""
+    if world <= 1:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(steps: int, world: int, slowest_s: float) -> float:
+    """Frames of all replicas per second of the slowest replica (weak scaling)."""
+    return steps * world / slowest_s
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
         os.environ.get("LOCAL_RANK", "0"))
@@ -398,12 +414,8 @@ def run_ours(args, rank, world, local):
     launches = res.launch_count() - launches0
     st = res.check_frame()
     res.set_profiling(False)
-    total_s = sum(times) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = args.steps * world / total_s
+    total_s = slowest_rank_seconds(sum(times) / 1000.0, world, dev)
+    value = replicas_value(args.steps, world, total_s)
 
     # end to end through the C ABI with host buffers
     log(f"frames timed: {value:.1f} frames/s")
@@ -493,12 +505,8 @@ def run_e2e(pkg, F, args, stream, world, dev):
         step()
     e.record(stream)
     e.synchronize()
-    total_s = s.elapsed_time(e) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    return {"value": round(args.steps * world / total_s, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+    total_s = slowest_rank_seconds(s.elapsed_time(e) / 1000.0, world, dev)
+    return {"value": round(replicas_value(args.steps, world, total_s), 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h)}
 
 
