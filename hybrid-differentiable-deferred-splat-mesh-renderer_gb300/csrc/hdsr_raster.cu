@@ -214,6 +214,44 @@ __device__ __forceinline__ void stage_row(float (*s)[32], const Row& w, uint32_t
   s[F_EB][lane] = lo16(w.gb.w);
 }
 
+// Can the entry reach any pixel centre of the rectangle [x0, x1] x [y0, y1]
+// with power > -4 and alpha > 1/255? The power, -0.5 ia dx^2 - ib dx dy -
+// 0.5 ic dy^2 (d = p - c), is concave: its maximum over the rectangle is 0
+// when the centre lies inside, else the best point of one of the four edges
+// (each a 1D parabola, vertex clamped to the edge). Conservative: the
+// continuous rectangle contains every pixel centre, the alpha limit uses a
+// fast log with margin, and the margin grows with the size of the terms, far
+// above the rounding of this test or of the rasteriser's own power. An entry
+// that fails the test changes no pixel of the rectangle (every pixel is
+// invalid for it), so skipping it is exact.
+__device__ __forceinline__ bool touches_rect(float cx, float cy, float ia, float ib, float ic, float op, float x0,
+                                             float x1, float y0, float y1) {
+  const float xa = x0 - cx, xb = x1 - cx, ya = y0 - cy, yb = y1 - cy;
+  const float xm = mx(fabsf(xa), fabsf(xb)), ym = mx(fabsf(ya), fabsf(yb));
+  const float mag = 0.5f * ia * xm * xm + fabsf(ib) * xm * ym + 0.5f * ic * ym * ym;
+  const float margin = 1e-3f + 1e-5f * mag;
+  float best;
+  if (xa <= 0.0f && xb >= 0.0f && ya <= 0.0f && yb >= 0.0f) {
+    best = 0.0f;
+  } else {
+    float e = -3.4e38f;
+    const float xs[2] = {xa, xb}, ys[2] = {ya, yb};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const float x = xs[k];
+      const float dy = clampf(-ib * x / ic, ya, yb);
+      e = mx(e, -0.5f * ia * x * x - ib * x * dy - 0.5f * ic * dy * dy);
+      const float y = ys[k];
+      const float dx = clampf(-ib * y / ia, xa, xb);
+      e = mx(e, -0.5f * ia * dx * dx - ib * dx * y - 0.5f * ic * y * y);
+    }
+    best = e;
+  }
+  // alpha = min(0.99, op exp(power)) > 1/255 needs power > -log(255 op)
+  const float lim = mx(-4.0f, -__logf(255.0f * op));
+  return best > lim - margin - 1e-3f;
+}
+
 // Resident blocks per SM the register budget is fitted to.
 #ifndef HDSR_RASTER_MIN_BLOCKS
 #define HDSR_RASTER_MIN_BLOCKS 4
@@ -238,16 +276,24 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
     const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
     const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
     const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
+    // pixel centres of this half tile
+    const float rx0 = (float)(tx * 16u) + 0.5f, ry0 = (float)(ty * 16u + 8u * half) + 0.5f;
+    const uint32_t lt = (1u << lane) - 1u;
     Quad q;
     quad_init(q);
     Row next;
     if (lane < count) next = load_row(a, start + lane);
     for (uint32_t b = 0; b < count; b += 32u) {
       const uint32_t n = count - b < 32u ? count - b : 32u;
-      if (lane < n) stage_row(s, next, lane);
+      // keep, in order, the batch's entries that can reach this half tile
+      const bool keep = lane < n && touches_rect(next.g.x, next.g.y, next.g.z, next.g.w, u2f(next.ap.x),
+                                                 hi16(next.ap.y), rx0, rx0 + 15.0f, ry0, ry0 + 7.0f);
+      const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
+      if (keep) stage_row(s, next, __popc(kept & lt));
       __syncwarp();
       if (b + 32u + lane < count) next = load_row(a, start + b + 32u + lane);  // in flight during the batch
-      for (uint32_t i = 0; i < n; ++i)
+      const uint32_t nk = __popc(kept);
+      for (uint32_t i = 0; i < nk; ++i)
         if (!q.done) quad_splat(q, p00x, p00y, s, (int)i);
       __syncwarp();
       if (__all_sync(0xFFFFFFFFu, q.done)) break;
