@@ -26,230 +26,104 @@
 //   3. k_project_bwd: per sortRank, recompute the projection in fp32 and apply
 //      the chain rule back to the scene arrays (atomic adds: a splat id may
 //      appear in sortedIndices more than once).
-#include "hdsr_internal.cuh"
+#define HDSR_BWD_REAL double
+#include "hdsr_proj_adjoint.cuh"
 
 namespace hdsr {
 
 namespace {
 
-// Scalar type of the projection recompute and its adjoint (per splat, not
-// per pixel): fp64. For splats seen nearly edge-on the conic's adjoint
-// combines large terms that cancel; at fp32 a few of them land 1e-3 to 1e-2
-// away from the FP64 gradient, at fp64 they agree to the fp32 raster's
-// precision. -DHDSR_BWD_REAL=float builds the fp32 variant.
-#ifndef HDSR_BWD_REAL
-#define HDSR_BWD_REAL double
-#endif
-using real = HDSR_BWD_REAL;
-__device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
-__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
-__device__ __forceinline__ float rexp_(float x) { return hx_expf(x); }
-__device__ __forceinline__ double rexp_(double x) { return exp(x); }
-__device__ __forceinline__ real rmax_(real a, real b) { return a > b ? a : b; }
-__device__ __forceinline__ real rmin_(real a, real b) { return a < b ? a : b; }
-__device__ __forceinline__ real rclamp_(real x, real lo, real hi) { return rmin_(rmax_(x, lo), hi); }
-
-struct F3 { real x, y, z; };
-__device__ __forceinline__ F3 f3(real x, real y, real z) { return F3{x, y, z}; }
-__device__ __forceinline__ real dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ F3 mul(F3 a, real s) { return f3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ F3 cross(F3 a, F3 b) {
-  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-
-constexpr real kBgR = 0.02f, kBgG = 0.02f, kBgB = 0.04f;  // composite background (T-weighted)
-
-// Projection of one splat, recomputed in fp32 with every intermediate the
-// adjoint needs (gpu_project_splats.wgsl:112-358, colour part and 2D conic).
-struct Proj {
-  F3 p;
-  real clip[4], safeW;
-  bool w_free;          // safeW == clip[3] (not clamped to 1e-4)
-  real vc[3], vz;
-  bool vz_free;         // vz == vc[2]
-  real fx, fy, J1x, J1y, J2x, J2y;
-  F3 w0, w1, w2, tt0, tt1;
-  real qn[4], qlen;    // normalised quaternion (w, x, y, z), its length
-  F3 R[3];              // rotated unit axes (columns of R)
-  real s[3];           // axis scales exp(logScale) * splatScale
-  F3 ax[3];
-  F3 b0, b1, cr;         // b0_i = ax_i . tt0, b1_i = ax_i . tt1, cr = b0 x b1
-  real XXr, XY, YYr, detOrig, cXX, cYY, D, ratio, aa;
-  real cx, cy;
-  real op_in, op_aa;   // input opacity, opacity * aa (before the clamp)
-  F3 cam, dir;
-  real dlen;
-  real craw[3];        // SH colour before the clamp
-};
-
-__device__ __forceinline__ real ld(const float* p) { return (real)__ldg(p); }
-
-__device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
-  const float* U = a.U;
-  const float* pp = a.pos + (uint64_t)id * 3;
-  P.p = f3(ld(pp), ld(pp + 1), ld(pp + 2));
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    P.clip[k] = ((ld(U + k) * P.p.x + ld(U + 4 + k) * P.p.y) + ld(U + 8 + k) * P.p.z) + ld(U + 12 + k);
-  P.safeW = rmax_(P.clip[3], 0.0001f);
-  P.w_free = P.clip[3] > 0.0001f;
-  P.cx = (P.clip[0] / P.safeW * 0.5f + 0.5f) * ld(U + 16);
-  P.cy = (1.0f - (P.clip[1] / P.safeW * 0.5f + 0.5f)) * ld(U + 17);
-  // axes
-  const float4 q = __ldg(reinterpret_cast<const float4*>(a.rot) + id);
-  P.qlen = rsqrt_(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
-  const real d = rmax_(P.qlen, 0.000001f);
-  P.qn[0] = q.x / d; P.qn[1] = q.y / d; P.qn[2] = q.z / d; P.qn[3] = q.w / d;
-  const real w = P.qn[0], x = P.qn[1], y = P.qn[2], z = P.qn[3];
-  P.R[0] = f3(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + w * z), 2.0f * (x * z - w * y));
-  P.R[1] = f3(2.0f * (x * y - w * z), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + w * x));
-  P.R[2] = f3(2.0f * (x * z + w * y), 2.0f * (y * z - w * x), 1.0f - 2.0f * (x * x + y * y));
-  const float* sl = a.scl + (uint64_t)id * 3;
-  const real ss = ld(U + 24);
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    P.s[i] = rexp_(ld(sl + i)) * ss;
-    P.ax[i] = mul(P.R[i], P.s[i]);
-  }
-  // Jacobian of the perspective projection in view space
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    P.vc[k] = ((ld(U + 32 + k) * P.p.x + ld(U + 36 + k) * P.p.y) + ld(U + 40 + k) * P.p.z) + ld(U + 44 + k);
-  P.vz = rmin_(P.vc[2], -0.001f);
-  P.vz_free = P.vc[2] < -0.001f;
-  P.fx = ld(U + 48);
-  P.fy = ld(U + 49);
-  P.J1x = P.fx / P.vz;
-  P.J1y = P.fy / P.vz;
-  P.J2x = (-P.J1x / P.vz) * P.vc[0];
-  P.J2y = (-P.J1y / P.vz) * P.vc[1];
-  P.w0 = f3(ld(U + 32), ld(U + 36), ld(U + 40));
-  P.w1 = f3(ld(U + 33), ld(U + 37), ld(U + 41));
-  P.w2 = f3(ld(U + 34), ld(U + 38), ld(U + 42));
-  P.tt0 = add(mul(P.w0, P.J1x), mul(P.w2, P.J2x));
-  P.tt1 = add(mul(P.w1, P.J1y), mul(P.w2, P.J2y));
-  P.b0 = f3(dot(P.ax[0], P.tt0), dot(P.ax[1], P.tt0), dot(P.ax[2], P.tt0));
-  P.b1 = f3(dot(P.ax[0], P.tt1), dot(P.ax[1], P.tt1), dot(P.ax[2], P.tt1));
-  P.XXr = dot(P.b0, P.b0);
-  P.XY = dot(P.b0, P.b1);
-  P.YYr = dot(P.b1, P.b1);
-  P.cr = cross(P.b0, P.b1);
-  P.detOrig = dot(P.cr, P.cr);
-  P.cXX = P.XXr + 0.3f;
-  P.cYY = P.YYr + 0.3f;
-  P.D = P.detOrig + 0.3f * (P.XXr + P.YYr) + 0.09f;  // >= 0.09: never below the 1e-6 floor
-  P.ratio = P.detOrig / P.D;
-  P.aa = rsqrt_(P.ratio);
-  P.op_in = ld(a.opa + id);
-  P.op_aa = P.op_in * P.aa;
-  // SH colour (WGSL basis and signs)
-  P.cam = f3(ld(U + 28), ld(U + 29), ld(U + 30));
-  const F3 dv = sub(P.cam, P.p);
-  P.dlen = rsqrt_(dot(dv, dv));
-  P.dir = f3(dv.x / P.dlen, dv.y / P.dlen, dv.z / P.dlen);
-  const uint32_t deg = f2u(ld(U + 25));
-  const uint32_t shStride = ((deg + 1) * (deg + 1) - 1) * 3;
-  const float* sh = a.sh + (uint64_t)id * (3 + shStride + 3);
-  real basis[15];
-  const real vx = P.dir.x, vy = P.dir.y, vzz = P.dir.z;
-  const real xx = vx * vx, yy = vy * vy, zz = vzz * vzz;
-  basis[0] = 0.4886025119029199f * vy;
-  basis[1] = 0.4886025119029199f * vzz;
-  basis[2] = 0.4886025119029199f * vx;
-  basis[3] = 1.0925484305920792f * vx * vy;
-  basis[4] = 1.0925484305920792f * vy * vzz;
-  basis[5] = 0.31539156525252005f * ((2.0f * zz - xx) - yy);
-  basis[6] = 1.0925484305920792f * vx * vzz;
-  basis[7] = 0.5462742152960396f * (xx - yy);
-  basis[8] = 0.5900435899266435f * vy * (3.0f * xx - yy);
-  basis[9] = 2.890611442640554f * vx * vy * vzz;
-  basis[10] = 0.4570457994644658f * vy * ((4.0f * zz - xx) - yy);
-  basis[11] = 0.3731763325901154f * vzz * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
-  basis[12] = 0.4570457994644658f * vx * ((4.0f * zz - xx) - yy);
-  basis[13] = 1.445305721320277f * vzz * (xx - yy);
-  basis[14] = 0.5900435899266435f * vx * (xx - 3.0f * yy);
-  const uint32_t nb = (deg + 1) * (deg + 1) - 1;
-#pragma unroll
-  for (int ch = 0; ch < 3; ++ch) {
-    real c = ld(sh + ch);
-    for (uint32_t k = 0; k < nb && k < 15u; ++k) c += ld(sh + 3 + 3 * k + ch) * basis[k];
-    P.craw[ch] = c;
-  }
-}
-
-// d(basis_k)/d(dir), k < 15 (same order as proj_recompute)
-__device__ __forceinline__ F3 dbasis(int k, F3 v) {
-  const real vx = v.x, vy = v.y, vz = v.z, xx = vx * vx, yy = vy * vy, zz = vz * vz;
-  const real C1 = 0.4886025119029199f, A = 1.0925484305920792f, B = 0.31539156525252005f;
-  const real Cc = 0.5462742152960396f, Dd = 0.5900435899266435f, E = 2.890611442640554f;
-  const real Ff = 0.4570457994644658f, G = 0.3731763325901154f, Hh = 1.445305721320277f;
-  switch (k) {
-    case 0: return f3(0.0f, C1, 0.0f);
-    case 1: return f3(0.0f, 0.0f, C1);
-    case 2: return f3(C1, 0.0f, 0.0f);
-    case 3: return f3(A * vy, A * vx, 0.0f);
-    case 4: return f3(0.0f, A * vz, A * vy);
-    case 5: return f3(-2.0f * B * vx, -2.0f * B * vy, 4.0f * B * vz);
-    case 6: return f3(A * vz, 0.0f, A * vx);
-    case 7: return f3(2.0f * Cc * vx, -2.0f * Cc * vy, 0.0f);
-    case 8: return f3(6.0f * Dd * vx * vy, Dd * (3.0f * xx - 3.0f * yy), 0.0f);
-    case 9: return f3(E * vy * vz, E * vx * vz, E * vx * vy);
-    case 10: return f3(-2.0f * Ff * vx * vy, Ff * (4.0f * zz - xx - 3.0f * yy), 8.0f * Ff * vy * vz);
-    case 11: return f3(-6.0f * G * vx * vz, -6.0f * G * vy * vz, G * (6.0f * zz - 3.0f * xx - 3.0f * yy));
-    case 12: return f3(Ff * (4.0f * zz - 3.0f * xx - yy), -2.0f * Ff * vx * vy, 8.0f * Ff * vx * vz);
-    case 13: return f3(2.0f * Hh * vx * vz, -2.0f * Hh * vy * vz, Hh * (xx - yy));
-    default: return f3(Dd * (3.0f * xx - 3.0f * yy), -6.0f * Dd * vx * vy, 0.0f);
-  }
-}
-
-__global__ void __launch_bounds__(256) k_bwd_prep(BwdArgs b) {
-  const FrameArgs& a = b.f;
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.N) return;
-#pragma unroll
-  for (uint32_t j = 0; j < kG2d; ++j) b.g2d[(size_t)r * kG2d + j] = 0.0f;
-  float4* par = b.par + (size_t)r * 3;
-  if (a.aux[r].x == kSentinel) {
-    par[0] = par[1] = par[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    return;
-  }
-  Proj P;
-  proj_recompute(a, __ldg(a.sorted + r), P);
-  const real Di = 1.0f / P.D;
-  par[0] = make_float4(P.cx, P.cy, P.cYY * Di, -P.XY * Di);
-  par[1] = make_float4(P.cXX * Di, rclamp_(P.op_aa, 0.0f, 0.99f), rclamp_(P.craw[0], 0.0f, 1.0f),
-                       rclamp_(P.craw[1], 0.0f, 1.0f));
-  par[2] = make_float4(rclamp_(P.craw[2], 0.0f, 1.0f), 0.0f, 0.0f, 0.0f);
-}
+constexpr float kBgR = 0.02f, kBgG = 0.02f, kBgB = 0.04f;  // composite background (T-weighted)
 
 constexpr int kBwdWarps = 4;
 enum BField { B_CX, B_CY, B_KA, B_KB, B_KC, B_OP, B_R, B_G, B_B, B_IA, B_IB, B_IC, B_RANK, kBFields };
 
-__device__ __forceinline__ void bwd_stage(const BwdArgs& b, float (*s)[32], uint32_t e, uint32_t lane) {
-  const FrameArgs& a = b.f;
-  const uint32_t r = checked_rank(__ldg(a.entries + e), a.N, a.ctl);
-  const float4 p0 = b.par[(size_t)r * 3], p1 = b.par[(size_t)r * 3 + 1], p2 = b.par[(size_t)r * 3 + 2];
-  s[B_CX][lane] = p0.x;
-  s[B_CY][lane] = p0.y;
-  s[B_KA][lane] = p0.z * -0.5f;
-  s[B_KB][lane] = -p0.w;
-  s[B_KC][lane] = p1.x * -0.5f;
-  s[B_OP][lane] = p1.y;
-  s[B_R][lane] = p1.z;
-  s[B_G][lane] = p1.w;
-  s[B_B][lane] = p2.x;
-  s[B_IA][lane] = p0.z;
-  s[B_IB][lane] = p0.w;
-  s[B_IC][lane] = p1.x;
-  s[B_RANK][lane] = u2f(r);
+// Same test as the rasteriser's (hdsr_raster.cu): can the entry reach a
+// pixel centre of [x0, x1] x [y0, y1] with power > -4 and alpha > 1/255?
+__device__ __forceinline__ bool bwd_touches(float cx, float cy, float ia, float ib, float ic, float op, float x0,
+                                            float x1, float y0, float y1) {
+  const float xa = x0 - cx, xb = x1 - cx, ya = y0 - cy, yb = y1 - cy;
+  const float xm = fmaxf(fabsf(xa), fabsf(xb)), ym = fmaxf(fabsf(ya), fabsf(yb));
+  const float mag = 0.5f * ia * xm * xm + fabsf(ib) * xm * ym + 0.5f * ic * ym * ym;
+  const float margin = 1e-3f + 1e-5f * mag;
+  float best;
+  if (xa <= 0.0f && xb >= 0.0f && ya <= 0.0f && yb >= 0.0f) {
+    best = 0.0f;
+  } else {
+    float e = -3.4e38f;
+    const float xs[2] = {xa, xb}, ys[2] = {ya, yb};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const float x = xs[k];
+      const float dy = fminf(fmaxf(-ib * x / ic, ya), yb);
+      e = fmaxf(e, -0.5f * ia * x * x - ib * x * dy - 0.5f * ic * dy * dy);
+      const float y = ys[k];
+      const float dx = fminf(fmaxf(-ib * y / ia, xa), xb);
+      e = fmaxf(e, -0.5f * ia * dx * dx - ib * dx * y - 0.5f * ic * y * y);
+    }
+    best = e;
+  }
+  const float lim = fmaxf(-4.0f, -__logf(255.0f * op));
+  return best > lim - margin - 1e-3f;
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
+// Stages entry e into slot `slot` of the batch if it can reach the half tile
+// [x0, x0 + 15] x [y0, y0 + 7]; returns whether it was kept (warp-collective:
+// every lane calls it, lanes without an entry pass valid = false).
+__device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float (*s)[32], uint32_t e, bool valid,
+                                                   uint32_t lane, float x0, float y0) {
+  const FrameArgs& a = b.f;
+  bool keep = false;
+  uint32_t r = 0;
+  float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
+  if (valid) {
+    r = checked_rank(__ldg(a.entries + e), a.N, a.ctl);
+    p0 = b.par[(size_t)r * 3];
+    p1 = b.par[(size_t)r * 3 + 1];
+    p2 = b.par[(size_t)r * 3 + 2];
+    keep = bwd_touches(p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, x0, x0 + 15.0f, y0, y0 + 7.0f);
+  }
+  const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
+  if (keep) {
+    const uint32_t k = __popc(kept & ((1u << lane) - 1u));
+    s[B_CX][k] = p0.x;
+    s[B_CY][k] = p0.y;
+    s[B_KA][k] = p0.z * -0.5f;
+    s[B_KB][k] = -p0.w;
+    s[B_KC][k] = p1.x * -0.5f;
+    s[B_OP][k] = p1.y;
+    s[B_R][k] = p1.z;
+    s[B_G][k] = p1.w;
+    s[B_B][k] = p2.x;
+    s[B_IA][k] = p0.z;
+    s[B_IB][k] = p0.w;
+    s[B_IC][k] = p1.x;
+    s[B_RANK][k] = u2f(r);
+  }
+  return __popc(kept);
+}
+
+// Warp sums of 9 values (padded to 16) by recursive halving: at each step a
+// lane keeps half of its values, receives its partner's partial sums of that
+// half and sends the other half (8 + 4 + 2 + 1 shuffles, then 1 to finish).
+// On return lanes 2k and 2k+1 hold the sum of value k' = bits 4..1 of the
+// lane; returns that index (>= 9: padding).
+__device__ __forceinline__ uint32_t warp_sum9(const float (&g)[9], uint32_t lane, float& out) {
+  float v[16];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-  return v;
+  for (int j = 0; j < 16; ++j) v[j] = j < 9 ? g[j] : 0.0f;
+#pragma unroll
+  for (int h = 8; h >= 1; h >>= 1) {
+    const bool upper = (lane & (uint32_t)(2 * h)) != 0u;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const float send = upper ? v[j] : v[j + h];
+      const float keep = upper ? v[j + h] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 2 * h);
+    }
+  }
+  out = v[0] + __shfl_xor_sync(0xFFFFFFFFu, v[0], 1);
+  return ((lane >> 1) & 1u) | (((lane >> 2) & 1u) << 1) | (((lane >> 3) & 1u) << 2) | (((lane >> 4) & 1u) << 3);
 }
 
 __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
@@ -283,9 +157,10 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     for (int k = 0; k < 4; ++k) { T[k] = 1.0f; C[k][0] = C[k][1] = C[k][2] = 0.0f; }
     bool done = false;
     uint32_t n_end = 0;
+    const float rx0 = (float)(tx * 16u) + 0.5f, ry0 = (float)(ty * 16u + 8u * half) + 0.5f;
     for (uint32_t b0 = 0; b0 < count; b0 += 32u) {
-      const uint32_t n = count - b0 < 32u ? count - b0 : 32u;
-      if (lane < n) bwd_stage(b, s, start + b0 + lane, lane);
+      const uint32_t nb = count - b0 < 32u ? count - b0 : 32u;
+      const uint32_t n = bwd_stage_kept(b, s, start + b0 + lane, lane < nb, lane, rx0, ry0);
       __syncwarp();
       for (uint32_t i = 0; i < n && !done; ++i) {
         const float cx = s[B_CX][i], cy = s[B_CY][i], ka = s[B_KA][i], kb = s[B_KB][i], kc = s[B_KC][i];
@@ -307,7 +182,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
         done = T[0] < 0.001f && T[1] < 0.001f && T[2] < 0.001f && T[3] < 0.001f;
       }
       __syncwarp();
-      n_end = b0 + n;
+      n_end = b0 + nb;
       if (__all_sync(0xFFFFFFFFu, done)) break;
     }
     // outputs and their incoming gradients (pixels outside the image: none)
@@ -328,8 +203,8 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     }
     // pass B: gradients, same entries in the same order
     for (uint32_t b0 = 0; b0 < n_end; b0 += 32u) {
-      const uint32_t n = n_end - b0 < 32u ? n_end - b0 : 32u;
-      if (lane < n) bwd_stage(b, s, start + b0 + lane, lane);
+      const uint32_t nb = n_end - b0 < 32u ? n_end - b0 : 32u;
+      const uint32_t n = bwd_stage_kept(b, s, start + b0 + lane, lane < nb, lane, rx0, ry0);
       __syncwarp();
       for (uint32_t i = 0; i < n; ++i) {
         const float cx = s[B_CX][i], cy = s[B_CY][i], ka = s[B_KA][i], kb = s[B_KB][i], kc = s[B_KC][i];
@@ -370,12 +245,9 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
           T[k] = T[k] * (1.0f - al);
         }
         if (__any_sync(0xFFFFFFFFu, any)) {
-          float* dst = b.g2d + (size_t)f2u(s[B_RANK][i]) * kG2d;
-#pragma unroll
-          for (int j = 0; j < 9; ++j) {
-            const float v = warp_sum(g[j]);
-            if (lane == (uint32_t)j && v != 0.0f) atomicAdd(dst + j, v);
-          }
+          float v;
+          const uint32_t j = warp_sum9(g, lane, v);
+          if (!(lane & 1u) && j < 9u && v != 0.0f) atomicAdd(b.g2d + (size_t)f2u(s[B_RANK][i]) * kG2d + j, v);
         }
       }
       __syncwarp();
@@ -541,7 +413,8 @@ __global__ void __launch_bounds__(128) k_project_bwd(BwdArgs b) {
 
 cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s) {
   const FrameArgs& a = b.f;
-  if (a.N) k_bwd_prep<<<(a.N + 255) / 256, 256, 0, s>>>(b);
+  cudaError_t e = launch_bwd_prep(b, s);
+  if (e != cudaSuccess) return e;
   if (a.tile_count) {
     const uint32_t want = (2u * a.tile_count + kBwdWarps - 1) / kBwdWarps;
     const uint32_t cap = (uint32_t)a.num_sms * 8u;

@@ -178,6 +178,7 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s);  // 3 launches
+cudaError_t launch_bwd_prep(const BwdArgs& b, cudaStream_t s);  // hdsr_backward_prep.cu
 
 // internal entry points of one compositor handle for the serving loop
 // (hdsr_api.cu); C++ linkage, not part of the C ABI
