@@ -45,6 +45,16 @@ struct hdsr_compositor {
   uint64_t launches = 0;           // kernels queued by this handle
   bool profiling = false;
   cudaEvent_t ev[kMaxProfiledPasses + 1] = {};
+  // uniform upload: a ring of pinned staging slots (an async copy from
+  // pageable memory may synchronise the stream), each reused only after its
+  // copy has run; no upload when the block equals the device's copy
+  static constexpr uint32_t kUniformSlots = 8;
+  float* pinned_u = nullptr;
+  cudaEvent_t ev_u[kUniformSlots] = {};
+  bool ev_u_pending[kUniformSlots] = {};
+  uint32_t next_u = 0;
+  float device_u[64] = {};
+  bool device_u_valid = false;
   uint32_t ev_used = 0;
   uint32_t pass_id[kMaxProfiledPasses] = {};
   char err[256] = {0};
@@ -221,7 +231,18 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   if (e == cudaSuccess) e = cudaMemsetAsync(a.ctl, 0, kCtlWords * 4, cudaStreamLegacy);
   if (e == cudaSuccess) e = cudaMemsetAsync(U, 0, 256, cudaStreamLegacy);
   if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
-  if (e != cudaSuccess) { s = cuda_fail(h, e, "clear handle state"); free_all(h); delete h; return s; }
+  if (e == cudaSuccess) e = cudaMallocHost(&h->pinned_u, hdsr_compositor::kUniformSlots * 256);
+  for (uint32_t i = 0; e == cudaSuccess && i < hdsr_compositor::kUniformSlots; ++i)
+    e = cudaEventCreateWithFlags(&h->ev_u[i], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    s = cuda_fail(h, e, "clear handle state");
+    for (cudaEvent_t& ev : h->ev_u)
+      if (ev) cudaEventDestroy(ev);
+    if (h->pinned_u) cudaFreeHost(h->pinned_u);
+    free_all(h);
+    delete h;
+    return s;
+  }
   *out = h;
   return HDSR_OK;
 }
@@ -234,6 +255,9 @@ void hdsr_destroy_tile_splat_compositor(hdsr_compositor* h) {
   cudaDeviceSynchronize();
   for (cudaEvent_t& e : h->ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t& e : h->ev_u)
+    if (e) cudaEventDestroy(e);
+  if (h->pinned_u) cudaFreeHost(h->pinned_u);
   free_all(h);
   cudaSetDevice(prev);
   delete h;
@@ -448,8 +472,21 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
   FrameArgs& a = h->args;
   h->ev_used = 0;
   if (h->profiling) cudaEventRecord(h->ev[0], s);
-  cudaError_t e = cudaMemcpyAsync(const_cast<float*>(a.U), h->uniforms, 256, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(h, e, "upload uniforms");
+  if (!h->device_u_valid || std::memcmp(h->device_u, h->uniforms, 256) != 0) {
+    const uint32_t k = h->next_u;
+    h->next_u = (k + 1) % hdsr_compositor::kUniformSlots;
+    cudaError_t e = h->ev_u_pending[k] ? cudaEventSynchronize(h->ev_u[k]) : cudaSuccess;
+    float* slot = h->pinned_u + 64 * k;
+    if (e == cudaSuccess) {
+      std::memcpy(slot, h->uniforms, 256);
+      e = cudaMemcpyAsync(const_cast<float*>(a.U), slot, 256, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev_u[k], s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload uniforms");
+    h->ev_u_pending[k] = true;
+    std::memcpy(h->device_u, h->uniforms, 256);
+    h->device_u_valid = true;
+  }
   mark(h, s, 0);
   if (full && (st = encode_pre_raster(h, s)) != HDSR_OK) return st;
   return encode_raster(h, s, full);
@@ -601,6 +638,7 @@ const FrameArgs* handle_args(const hdsr_compositor* h) { return h ? &h->args : n
 int handle_frame_checks(hdsr_compositor* h) { return encode_checks(h, true); }
 
 int handle_upload_uniforms(hdsr_compositor* h, const float* pinned_uniforms, cudaStream_t s) {
+  h->device_u_valid = false;  // the caller's staging, not the handle's record
   cudaError_t e = cudaMemcpyAsync(const_cast<float*>(h->args.U), pinned_uniforms, 256, cudaMemcpyHostToDevice, s);
   return e == cudaSuccess ? HDSR_OK : cuda_fail(h, e, "upload uniforms");
 }

@@ -238,24 +238,39 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
 //   k_seg_scan:    per superblock and tile, an exclusive scan over the
 //                  segments plus the tile's offset: every segment's first
 //                  entry position in every tile;
-//   k_seg_scatter: per segment, in list order, every entry appended to every
-//                  tile it covers: one ballot per covered tile gives the
-//                  entries' ranks, the tile's running position lives in
-//                  lane (tile & 31) of the warp.
+//   k_seg_scatter: per segment (two warps, four tile rows each), in list
+//                  order, every entry appended to every tile it covers: one
+//                  ballot per covered tile gives the entries' ranks, the
+//                  tile's running position lives in lane (tile & 31).
 // Tile j of a superblock is (j & 7, j >> 3) in its local coordinates.
 
+// The per-superblock segment tables, staged in shared memory once per block
+// (every warp item binary-searches them).
+struct SegTables {
+  uint32_t first[kMaxSuperblocks + 1];
+  uint32_t start[kMaxSuperblocks + 1];
+};
+
+__device__ __forceinline__ void seg_tables_load(const FrameArgs& a, SegTables& t) {
+  for (uint32_t i = threadIdx.x; i <= a.num_sb; i += blockDim.x) {
+    t.first[i] = a.seg_first[i];
+    t.start[i] = a.sb_start[i];
+  }
+  __syncthreads();
+}
+
 // Segment s: its superblock and its [beg, end) in the sorted list entries.
-__device__ __forceinline__ void seg_locate(const FrameArgs& a, uint32_t s, uint32_t& sb, uint32_t& beg,
-                                           uint32_t& end) {
-  uint32_t lo = 0u, hi = a.num_sb;  // seg_first[lo] <= s < seg_first[hi]
+__device__ __forceinline__ void seg_locate(const FrameArgs& a, const SegTables& t, uint32_t s, uint32_t& sb,
+                                           uint32_t& beg, uint32_t& end) {
+  uint32_t lo = 0u, hi = a.num_sb;  // first[lo] <= s < first[hi]
   while (hi - lo > 1u) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (a.seg_first[mid] <= s) lo = mid;
+    if (t.first[mid] <= s) lo = mid;
     else hi = mid;
   }
   sb = lo;
-  beg = a.sb_start[sb] + (s - a.seg_first[sb]) * kSegEntries;
-  const uint32_t lim = a.sb_start[sb + 1u];
+  beg = t.start[sb] + (s - t.first[sb]) * kSegEntries;
+  const uint32_t lim = t.start[sb + 1u];
   end = lim - beg < kSegEntries ? lim : beg + kSegEntries;
 }
 
@@ -264,14 +279,16 @@ __device__ __forceinline__ uint32_t local_rect(unsigned long long k) { return (u
 __global__ void __launch_bounds__(256) k_seg_count(FrameArgs a) {
   constexpr uint32_t kGrid = 9u * 9u;
   __shared__ int s_diff[8][kGrid + 3u];
+  __shared__ SegTables tables;
   if (a.ctl[kCtlFlags] & 0x1u) return;
+  seg_tables_load(a, tables);
   const uint32_t lane = threadIdx.x & 31u;
   int* d = s_diff[threadIdx.x >> 5];
   const uint32_t total = a.ctl[kCtlSegments];
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < total; s += nw) {
     uint32_t sb, beg, end;
-    seg_locate(a, s, sb, beg, end);
+    seg_locate(a, tables, s, sb, beg, end);
     for (uint32_t i = lane; i < kGrid; i += 32u) d[i] = 0;
     __syncwarp();
     for (uint32_t i = beg + lane; i < end; i += 32u) {
@@ -338,7 +355,9 @@ __global__ void __launch_bounds__(1024) k_seg_scan(FrameArgs a) {
 // Two warps per segment: half h takes tile rows 4h..4h+3 (tiles 32h + lane).
 __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
   constexpr uint32_t C = kSegEntries / 32u;
+  __shared__ SegTables tables;
   if (a.ctl[kCtlFlags] & 0x1u) return;
+  seg_tables_load(a, tables);
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt = lanemask_lt();
   const uint32_t total = a.ctl[kCtlSegments] * 2u;
@@ -347,10 +366,10 @@ __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
     const uint32_t s = w >> 1, half = w & 1u;
     uint32_t sb, beg, end;
-    seg_locate(a, s, sb, beg, end);
+    seg_locate(a, tables, s, sb, beg, end);
     // lane t: first position of tile 32 * half + t in this segment; the
-    // chunk's appends to it collect in inc and land after the chunk (every
-    // tile is visited at most once per chunk)
+    // chunk's appends collect in inc and land after the chunk (every tile is
+    // visited at most once per chunk)
     uint32_t pos = a.seg_cnt[(size_t)s * kSbTiles + 32u * half + lane];
     unsigned long long k[C];
 #pragma unroll
