@@ -311,7 +311,7 @@ void dispatcher_main(hdsr_server* s) {
         hdsr_destroy_tile_splat_compositor(sl->h);
         sl->h = nullptr;
         char msg[160];
-        Slot* fresh = create_slot(key, scene.views, pairs + pairs / 8 + 4096, msg, sizeof(msg));
+        Slot* fresh = create_slot(key, scene.views, pairs + pairs / 4 + 65536, msg, sizeof(msg));
         hdsr_status st = HDSR_ERR_OOM;
         if (fresh) {
           // keep the slot object (its stream and staging); take the new handle
@@ -386,7 +386,9 @@ void dispatcher_main(hdsr_server* s) {
         const uint64_t learned = s->learned_pairs.count(key) ? s->learned_pairs[key] : 0;
         lock.unlock();
         char msg[160];
-        Slot* fresh = create_slot(key, scene.views, learned ? learned + learned / 8 + 4096 : 0, msg, sizeof(msg));
+        // headroom over the largest frame seen: another camera of the same
+        // key rarely needs more, and a re-run rebuilds the slot
+        Slot* fresh = create_slot(key, scene.views, learned ? learned + learned / 2 + 65536 : 0, msg, sizeof(msg));
         lock.lock();
         if (!fresh) {
           finish_ticket(s, t, HDSR_ERR_OOM);
