@@ -442,8 +442,8 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
     if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
     h->launches += 2;
   }
-  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 4 * kDepthPasses + 1 + n_splat_launch +
-                 4 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
+  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 3 * kDepthPasses + 1 + n_splat_launch +
+                 3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
   return HDSR_OK;
 }
 

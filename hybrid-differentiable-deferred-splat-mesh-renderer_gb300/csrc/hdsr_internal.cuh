@@ -174,7 +174,7 @@ cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_emit_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
-cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 4 launches
+cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 3 launches
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s);  // 3 launches

@@ -345,24 +345,42 @@ __global__ void __launch_bounds__(1024) k_tile_prefix(FrameArgs a) {
     gs = cols;
     __syncthreads();
   }
-  for (uint32_t y = threadIdx.x; y < rows; y += blockDim.x) {
-    int run = 0;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t nwarps = blockDim.x >> 5;
+  // rows, then columns: one warp per line, 32 cells per step with a carry
+  for (uint32_t y = warp; y < rows; y += nwarps) {
+    int carry = 0;
     int* row = g + y * gs;
-    for (uint32_t x = 0; x < cols; ++x) {
-      run += row[x];
-      row[x] = run;
+    for (uint32_t x0 = 0; x0 < cols; x0 += 32u) {
+      const uint32_t x = x0 + lane;
+      int v = x < cols ? row[x] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= (uint32_t)o) v += t;
+      }
+      v += carry;
+      if (x < cols) row[x] = v;
+      carry = __shfl_sync(0xFFFFFFFFu, v, 31);
     }
   }
   __syncthreads();
-  for (uint32_t x = threadIdx.x; x < cols; x += blockDim.x) {
-    int run = 0;
-    for (uint32_t y = 0; y < rows; ++y) {
-      run += g[y * gs + x];
-      a.tile_cnt[morton(x, y)] = (uint32_t)run;
+  for (uint32_t x = warp; x < cols; x += nwarps) {
+    int carry = 0;
+    for (uint32_t y0 = 0; y0 < rows; y0 += 32u) {
+      const uint32_t y = y0 + lane;
+      int v = y < rows ? g[y * gs + x] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= (uint32_t)o) v += t;
+      }
+      v += carry;
+      if (y < rows) a.tile_cnt[morton(x, y)] = (uint32_t)v;
+      carry = __shfl_sync(0xFFFFFFFFu, v, 31);
     }
   }
   // superblock list lengths
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t ss = a.sb_cols + 1u;
   if (tid < a.sb_rows) {
     int run = 0;

@@ -18,8 +18,9 @@
 //      over 256-entry segments (k_seg_*), which writes the 1-u32 tile
 //      entries (sortRank).
 // Each pass is reduce-then-scan: an upsweep counts the digits of every block
-// tile of keys, a column scan turns the counts into per-tile digit offsets,
-// a bin scan gives the digits' global bases, and a downsweep ranks the keys
+// tile of keys, a column scan turns the counts into per-tile digit offsets
+// and digit totals, and a downsweep (which scans the totals into the digits'
+// global bases) ranks the keys
 // per warp with __match_any_sync (stable: warp-striped items keep input
 // order), stages them in shared memory in digit order and writes consecutive
 // addresses of each digit bucket from consecutive threads.
@@ -65,7 +66,8 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
 }
 
 // Column scan: for every bin, exclusive prefix of its per-tile counts; the
-// bin's total goes to bin_base. One block per bin, 16 tiles per thread.
+// bin's total goes to bin_base (the downsweep scans the totals into bases).
+// One block per bin, 16 tiles per thread.
 __global__ void __launch_bounds__(256) k_radix_colscan(RadixJob j) {
   constexpr uint32_t IT = 16;
   __shared__ uint32_t s_w[8];
@@ -109,30 +111,6 @@ __global__ void __launch_bounds__(256) k_radix_colscan(RadixJob j) {
   if (tid == 0) j.bin_base[bin] = s_carry;
 }
 
-// Bin scan: bin totals -> exclusive global bases (256 threads, 2 bins each).
-__global__ void __launch_bounds__(256) k_radix_binscan(RadixJob j) {
-  __shared__ uint32_t s_w[8];
-  if (skipped(j)) return;
-  const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
-  const uint32_t nb = 1u << j.bits;
-  uint32_t* h = j.bin_base;
-  const uint32_t v0 = 2 * t < nb ? h[2 * t] : 0u, v1 = 2 * t + 1 < nb ? h[2 * t + 1] : 0u;
-  const uint32_t v = v0 + v1;
-  uint32_t inc = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t x = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-    if (lane >= (uint32_t)o) inc += x;
-  }
-  if (lane == 31) s_w[w] = inc;
-  __syncthreads();
-  uint32_t off = 0;
-  for (uint32_t k = 0; k < w; ++k) off += s_w[k];
-  const uint32_t ex = off + inc - v;
-  if (2 * t < nb) h[2 * t] = ex;
-  if (2 * t + 1 < nb) h[2 * t + 1] = ex + v0;
-}
-
 // Shared memory of one downsweep block (dynamic).
 struct SweepSmem {
   unsigned long long keys[kRadixTile];
@@ -156,6 +134,24 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t lt = lanemask_lt();
   static_assert(kRadixBins == kRadixThreads, "one digit per thread in the bookkeeping");
+  // global base of digit `tid`: exclusive scan of the bin totals (each block
+  // computes it; 256 values)
+  uint32_t digit_base;
+  {
+    const uint32_t tot = tid <= dmask ? j.bin_base[tid] : 0u;
+    uint32_t inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += t;
+    }
+    if (lane == 31) S.wsum[warp] = inc;
+    __syncthreads();
+    uint32_t off = 0;
+    for (uint32_t w = 0; w < warp; ++w) off += S.wsum[w];
+    digit_base = off + inc - tot;
+    __syncthreads();
+  }
   for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
     for (uint32_t i = tid; i < W * kRadixBins; i += kRadixThreads) (&S.whist[0][0])[i] = 0u;
     const uint32_t d = tid;
@@ -197,7 +193,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
       uint32_t woff = 0;
       for (uint32_t w = 0; w < warp; ++w) woff += S.wsum[w];
       uint32_t e = woff + inc - run;
-      if (d <= dmask) S.excl[d] = j.bin_base[d] + j.tile_digits[(size_t)d * j.tiles_cap + tile] - e;
+      if (d <= dmask) S.excl[d] = digit_base + j.tile_digits[(size_t)d * j.tiles_cap + tile] - e;
 #pragma unroll
       for (uint32_t w = 0; w < W; ++w) {
         const uint32_t c = S.whist[w][d];
@@ -462,7 +458,6 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
   }
   k_radix_upsweep<<<num_sms * 8, kRadixThreads, 0, s>>>(j);
   k_radix_colscan<<<1u << j.bits, 256, 0, s>>>(j);
-  k_radix_binscan<<<1, 256, 0, s>>>(j);
   if (last) k_radix_downsweep<true><<<grid_last, kRadixThreads, smem, s>>>(j);
   else k_radix_downsweep<false><<<grid_mid, kRadixThreads, smem, s>>>(j);
   return cudaGetLastError();
