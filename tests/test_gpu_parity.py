@@ -15,11 +15,25 @@ from gpu_helpers import assert_frame_parity, read_gpu, render_gpu
 pytestmark = pytest.mark.gpu
 
 
+def _fp64_error(orc, g, gpu, ref):
+    """Max |err| and PSNR of the GPU colour against the FP64 twin (same entry
+    lists, double arithmetic, no f16 quantisation)."""
+    f64 = orc.render_frame_f64(g["u"], g["packed"], g["order"], ref)
+    got = gpu["color"].astype(np.float64)
+    err = np.abs(got - f64)
+    mse = float(np.mean((got[..., :3] - f64[..., :3]) ** 2))
+    psnr = 10.0 * math.log10(1.0 / max(mse, 1e-30))
+    return float(err.max()), psnr
+
+
 def test_plain50k_800x600_parity(cuda, pkg, orc):
     wl = pkg.workloads.plain50k()
     g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height)
     gpu, ref = assert_frame_parity(orc, g)
     assert ref["total_pairs"] > 50_000
+    # accuracy against FP64: PSNR >= 50 dB (the image is the f16 output)
+    err, psnr = _fp64_error(orc, g, gpu, ref)
+    assert psnr >= 50.0, (err, psnr)
     g["res"].destroy()
 
 
@@ -232,4 +246,6 @@ def test_hot760k_full_frame_parity(cuda, pkg, orc):
     R = np.uint64(gpu["rank_bits"])
     tiles = (gk >> (R + np.uint64(20))).astype(np.int64)
     assert np.array_equal(np.bincount(tiles, minlength=len(ref["tile_counts"])), ref["tile_counts"].astype(np.int64))
+    err, psnr = _fp64_error(orc, g, gpu, ref)
+    assert psnr >= 50.0, (err, psnr)
     g["res"].destroy()
