@@ -398,12 +398,11 @@ def run_ours(args, rank, world, local):
     for _ in range(args.warmup):
         frame()
     torch.cuda.synchronize()
-    res.set_profiling(True)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = res.launch_count()
-    times, passes = [], {}
+    times = []
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush.zero_()
@@ -411,13 +410,19 @@ def run_ours(args, rank, world, local):
             s.record(stream)
             frame()
             e.record(stream)
-            for name, ms in res.pass_times():
-                passes.setdefault(name, []).append(ms)
             e.synchronize()
             times.append(s.elapsed_time(e))
         torch.cuda.synchronize()
     launches = res.launch_count() - launches0
     st = res.check_frame()
+    # per-pass times: the same frames again with profiling events (one stream)
+    res.set_profiling(True)
+    passes = {}
+    for _ in range(args.steps):
+        flush.zero_()
+        frame()
+        for name, ms in res.pass_times():
+            passes.setdefault(name, []).append(ms)
     res.set_profiling(False)
     total_s = slowest_rank_seconds(sum(times) / 1000.0, world, dev)
     value = replicas_value(args.steps, world, total_s)

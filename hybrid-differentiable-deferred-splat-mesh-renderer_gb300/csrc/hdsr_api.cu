@@ -55,6 +55,11 @@ struct hdsr_compositor {
   uint32_t next_u = 0;
   float device_u[64] = {};
   bool device_u_valid = false;
+  // second stream of a frame: tile counts and the tile scan run there,
+  // forked after projection and joined before the superblock lists, beside
+  // the depth sort (none when profiling: per-pass times need one stream)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   uint32_t ev_used = 0;
   uint32_t pass_id[kMaxProfiledPasses] = {};
   char err[256] = {0};
@@ -234,10 +239,16 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   if (e == cudaSuccess) e = cudaMallocHost(&h->pinned_u, hdsr_compositor::kUniformSlots * 256);
   for (uint32_t i = 0; e == cudaSuccess && i < hdsr_compositor::kUniformSlots; ++i)
     e = cudaEventCreateWithFlags(&h->ev_u[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     s = cuda_fail(h, e, "clear handle state");
     for (cudaEvent_t& ev : h->ev_u)
       if (ev) cudaEventDestroy(ev);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->pinned_u) cudaFreeHost(h->pinned_u);
     free_all(h);
     delete h;
@@ -258,6 +269,9 @@ void hdsr_destroy_tile_splat_compositor(hdsr_compositor* h) {
   for (cudaEvent_t& e : h->ev_u)
     if (e) cudaEventDestroy(e);
   if (h->pinned_u) cudaFreeHost(h->pinned_u);
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->join_ev) cudaEventDestroy(h->join_ev);
+  if (h->side) cudaStreamDestroy(h->side);
   free_all(h);
   cudaSetDevice(prev);
   delete h;
@@ -396,11 +410,19 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   mark(h, s, 1);
   if ((e = launch_project(a, s)) != cudaSuccess) return cuda_fail(h, e, "project");
   mark(h, s, 2);
-  if ((e = launch_tile_counts(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_counts");
-  if (a.log_keys && (e = launch_depth_range(a, s)) != cudaSuccess) return cuda_fail(h, e, "depth_range");
+  // tile counts and the tile scan: beside the depth sort on the side stream
+  // (they share no buffer with it), or in line when profiling
+  const bool fork = !h->profiling && h->side;
+  cudaStream_t ts = fork ? h->side : s;
+  if (fork && ((e = cudaEventRecord(h->fork_ev, s)) != cudaSuccess ||
+               (e = cudaStreamWaitEvent(ts, h->fork_ev, 0)) != cudaSuccess))
+    return cuda_fail(h, e, "fork");
+  if ((e = launch_tile_counts(a, ts)) != cudaSuccess) return cuda_fail(h, e, "tile_counts");
+  if (a.log_keys && (e = launch_depth_range(a, ts)) != cudaSuccess) return cuda_fail(h, e, "depth_range");
   mark(h, s, 3);
-  if ((e = launch_scan_tiles(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
+  if ((e = launch_scan_tiles(a, ts)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
   mark(h, s, 5);
+  if (fork && (e = cudaEventRecord(h->join_ev, ts)) != cudaSuccess) return cuda_fail(h, e, "fork");
   // splats: 4 passes over the 32 depth bits -> order (sortRanks by depth)
   RadixJob dj{};
   dj.count = a.ctl + kCtlSplats;
@@ -419,6 +441,8 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
       return cuda_fail(h, e, "depth_sort");
   }
   mark(h, s, 6);
+  // the superblock lists need the tile scan's totals and overflow flag
+  if (fork && (e = cudaStreamWaitEvent(s, h->join_ev, 0)) != cudaSuccess) return cuda_fail(h, e, "join");
   // superblock lists in depth order, sorted by superblock (stable)
   if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
   if ((e = launch_emit_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit_superblocks");
