@@ -71,9 +71,10 @@ __device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
   P.cy = (1.0f - (P.clip[1] / P.safeW * 0.5f + 0.5f)) * ld(U + 17);
   // axes
   const float4 q = __ldg(reinterpret_cast<const float4*>(a.rot) + id);
-  P.qlen = rsqrt_(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
-  const real d = rmax_(P.qlen, 0.000001f);
-  P.qn[0] = q.x / d; P.qn[1] = q.y / d; P.qn[2] = q.z / d; P.qn[3] = q.w / d;
+  const real qx = q.x, qy = q.y, qz = q.z, qw = q.w;
+  P.qlen = rsqrt_(qx * qx + qy * qy + qz * qz + qw * qw);
+  const real iq = real(1) / rmax_(P.qlen, 0.000001f);
+  P.qn[0] = qx * iq; P.qn[1] = qy * iq; P.qn[2] = qz * iq; P.qn[3] = qw * iq;
   const real w = P.qn[0], x = P.qn[1], y = P.qn[2], z = P.qn[3];
   P.R[0] = f3(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + w * z), 2.0f * (x * z - w * y));
   P.R[1] = f3(2.0f * (x * y - w * z), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + w * x));
@@ -82,7 +83,9 @@ __device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
   const real ss = ld(U + 24);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    P.s[i] = rexp_(ld(sl + i)) * ss;
+    // exp at fp32: an error in s_i scales b0_i and b1_i alike, so the
+    // near-parallel cancellation of the conic does not amplify it
+    P.s[i] = (real)hx_expf(__ldg(sl + i)) * ss;
     P.ax[i] = mul(P.R[i], P.s[i]);
   }
   // Jacobian of the perspective projection in view space
@@ -93,10 +96,11 @@ __device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
   P.vz_free = P.vc[2] < -0.001f;
   P.fx = ld(U + 48);
   P.fy = ld(U + 49);
-  P.J1x = P.fx / P.vz;
-  P.J1y = P.fy / P.vz;
-  P.J2x = (-P.J1x / P.vz) * P.vc[0];
-  P.J2y = (-P.J1y / P.vz) * P.vc[1];
+  const real ivz = real(1) / P.vz;
+  P.J1x = P.fx * ivz;
+  P.J1y = P.fy * ivz;
+  P.J2x = (-P.J1x * ivz) * P.vc[0];
+  P.J2y = (-P.J1y * ivz) * P.vc[1];
   P.w0 = f3(ld(U + 32), ld(U + 36), ld(U + 40));
   P.w1 = f3(ld(U + 33), ld(U + 37), ld(U + 41));
   P.w2 = f3(ld(U + 34), ld(U + 38), ld(U + 42));
@@ -120,7 +124,8 @@ __device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
   P.cam = f3(ld(U + 28), ld(U + 29), ld(U + 30));
   const F3 dv = sub(P.cam, P.p);
   P.dlen = rsqrt_(dot(dv, dv));
-  P.dir = f3(dv.x / P.dlen, dv.y / P.dlen, dv.z / P.dlen);
+  const real idl = real(1) / P.dlen;
+  P.dir = f3(dv.x * idl, dv.y * idl, dv.z * idl);
   const uint32_t deg = f2u(ld(U + 25));
   const uint32_t shStride = ((deg + 1) * (deg + 1) - 1) * 3;
   const float* sh = a.sh + (uint64_t)id * (3 + shStride + 3);

@@ -37,6 +37,30 @@ def test_plain50k_800x600_parity(cuda, pkg, orc):
     g["res"].destroy()
 
 
+def test_profiled_and_forked_frames_are_identical(cuda, pkg, orc):
+    # with profiling the frame runs on one stream; without it the tile counts
+    # and tile scan run beside the depth sort on the handle's second stream
+    import torch
+
+    wl = pkg.workloads.plain50k()
+    g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height)
+    res = g["res"]
+    snap = lambda: [t.clone() for t in (g["color"], g["gb"]["depth"], g["gb"]["normal"], g["gb"]["material"],
+                                         res.buffer("tile_entries", count=int(res.query_status()["total_pairs"])))]
+    forked = snap()
+    res.set_profiling(True)
+    pkg.encode_full_compute_compositor_pipeline(None, res)
+    torch.cuda.synchronize()
+    names = [n for n, _ in res.pass_times()]
+    res.set_profiling(False)
+    serial = snap()
+    assert "tile_counts" in names and "raster" in names
+    for a, b in zip(forked, serial):
+        assert torch.equal(a.view(torch.int16) if a.dtype == torch.float16 else a, b.view(torch.int16) if b.dtype == torch.float16 else b)
+    assert_frame_parity(orc, g)
+    res.destroy()
+
+
 def test_one_splat(cuda, pkg, orc):
     scene = pkg.splats.SplatAttributes(
         positions=np.array([[0.1, -0.2, 0.0]], np.float32), scales=np.full((1, 3), -2.0, np.float32),
