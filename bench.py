@@ -426,6 +426,19 @@ def run_ours(args, rank, world, local):
     res.set_profiling(False)
     total_s = slowest_rank_seconds(sum(times) / 1000.0, world, dev)
     value = replicas_value(args.steps, world, total_s)
+    # sortedIndices on the device for the same camera (the reference sorts on
+    # the host: cpu_baseline's cpu_depth_sort_ms)
+    sorted_tmp = torch.empty(N, dtype=torch.int32, device=dev)
+    view = np.asarray(wl.cameras[0].frame(wl.width, wl.height)["view"], np.float32).reshape(-1)
+    for _ in range(3):
+        pkg.sort_back_to_front(stream, res, view, sorted_tmp)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(args.steps):
+        pkg.sort_back_to_front(stream, res, view, sorted_tmp)
+    e.record(stream)
+    e.synchronize()
+    sort_ms = s.elapsed_time(e) / args.steps
 
     # end to end through the C ABI with host buffers
     log(f"frames timed: {value:.1f} frames/s")
@@ -460,6 +473,7 @@ def run_ours(args, rank, world, local):
         "passes_ms": {k: round(v, 4) for k, v in mean_pass.items()},
         "pass_share": {k: round(v / frame_ms, 4) for k, v in mean_pass.items()},
         "roofline": roofline, "clocks": clocks.summary(),
+        "gpu_back_to_front_sort_ms": round(sort_ms, 4),
     }
     if rank == 0 and not args.no_train:
         log("training leg")

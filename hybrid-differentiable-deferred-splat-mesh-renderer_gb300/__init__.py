@@ -16,6 +16,7 @@ from .compositor import (
     encode_full_compute_compositor_pipeline,
     frame_uniforms_for,
     plan_tile_splat_compositor,
+    sort_back_to_front,
     write_frame_uniform_buffer,
     write_tile_splat_frame_uniforms,
 )
@@ -39,6 +40,7 @@ __all__ = [
     "frame_uniforms_for",
     "load_library",
     "plan_tile_splat_compositor",
+    "sort_back_to_front",
     "splats",
     "workloads",
     "write_frame_uniform_buffer",

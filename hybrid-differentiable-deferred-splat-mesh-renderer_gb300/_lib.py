@@ -133,6 +133,7 @@ SIGNATURES = {
     "hdsr_bind_scene": (c_int, [c_void_p, POINTER(SceneViews)]),
     "hdsr_bind_outputs": (c_int, [c_void_p, POINTER(OutputViews)]),
     "hdsr_encode_backward": (c_int, [c_void_p, POINTER(GradViews), c_void_p]),
+    "hdsr_sort_back_to_front": (c_int, [c_void_p, POINTER(c_float), c_void_p, c_void_p]),
     "hdsr_server_create": (c_int, [POINTER(ServerConfig), POINTER(c_void_p)]),
     "hdsr_server_destroy": (None, [c_void_p]),
     "hdsr_server_add_scene": (c_int, [c_void_p, c_uint32, POINTER(SceneViews)]),

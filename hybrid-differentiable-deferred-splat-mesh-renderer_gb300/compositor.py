@@ -172,6 +172,18 @@ def create_tile_splat_compositor(plan: TileSplatCompositorPlan, pair_capacity: i
     return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys, backward)
 
 
+def sort_back_to_front(stream, resources: TileSplatCompositorResources, view, out) -> None:
+    """sortedIndices on the device (hdsr_sort_back_to_front): the back-to-front
+    order of the bound positions for `view` (16 floats, column-major) into
+    `out` (int32/uint32 CUDA tensor of splat_count), as back_to_front_order
+    computes it on the host."""
+    v = np.ascontiguousarray(np.asarray(view, np.float32).reshape(-1))
+    assert v.size == 16
+    st = resources._lib.hdsr_sort_back_to_front(resources.handle, v.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                ctypes.c_void_p(_ptr(out)), _stream_handle(stream))
+    _lib.check(st, resources.handle, "sort_back_to_front")
+
+
 def encode_backward(stream, resources: TileSplatCompositorResources, d_color, grads: dict) -> None:
     """Adjoint of the last full encode (hdsr_encode_backward).
 

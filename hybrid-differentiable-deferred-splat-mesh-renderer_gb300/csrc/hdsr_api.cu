@@ -518,6 +518,18 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
 
 hdsr_status hdsr_encode_full(hdsr_compositor* h, void* stream) { return encode(h, stream, true); }
 
+hdsr_status hdsr_sort_back_to_front(hdsr_compositor* h, const float view[16], uint32_t* sorted_out, void* stream) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  if (!view) return fail(h, HDSR_ERR_INVALID_ARG, "view matrix is NULL");
+  if (!h->scene_bound) return fail(h, HDSR_ERR_NOT_BOUND, "bind the scene first");
+  if (h->args.N && !sorted_out) return fail(h, HDSR_ERR_INVALID_ARG, "output is NULL");
+  const double vrow[4] = {view[2], view[6], view[10], view[14]};
+  cudaError_t e = launch_sort_back_to_front(h->args, vrow, sorted_out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(h, e, "sort_back_to_front");
+  if (h->args.N) h->launches += 1 + 3 * 4;
+  return HDSR_OK;
+}
+
 hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* g, void* stream) {
   if (!h) return HDSR_ERR_INVALID_ARG;
   if (!(h->cfg.flags & HDSR_CFG_BACKWARD)) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_BACKWARD");

@@ -24,6 +24,8 @@ enum Ctl : int {
   kCtlScanMTile = 9,
   kCtlRasterTile = 19, // dynamic tile counter of the rasteriser
   kCtlBwdTile = 20,    // dynamic tile counter of the adjoint rasteriser
+  kCtlSortCount = 21,  // key count of the back-to-front sort (hdsr_sort_back_to_front)
+  kCtlSortFlags = 22,  // its skip flags (always 0: the sort never skips)
   kCtlWords = 64
 };
 
@@ -176,6 +178,9 @@ cudaError_t launch_emit_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
 cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 3 launches
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
+// back-to-front order of the bound positions for a view matrix (row 2 of the
+// view transform: view[2], view[6], view[10], view[14]) into `out`
+cudaError_t launch_sort_back_to_front(const FrameArgs& a, const double vrow[4], uint32_t* out, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s);  // 3 launches
 cudaError_t launch_bwd_prep(const BwdArgs& b, cudaStream_t s);  // hdsr_backward_prep.cu

@@ -471,6 +471,55 @@ cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+namespace {
+
+// Keys of the back-to-front sort (gpuSortPrototype.ts:120-163, the view
+// depth of viewSpaceDepthUnchecked :308-320 in double, left to right, stored
+// as f32 of its negation): ascending u64 order = descending key, ties by
+// ascending splat id. -0 sorts as +0 (the reference compares keys with ==);
+// NaN keys sort after every other key.
+__global__ void __launch_bounds__(256) k_view_keys(const float* pos, uint32_t N, double v2, double v6, double v10,
+                                                   double v14, unsigned long long* keys, uint32_t* ctl) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    ctl[kCtlSortCount] = N;
+    ctl[kCtlSortFlags] = 0u;
+  }
+  if (i >= N) return;
+  const double x = pos[(uint64_t)i * 3], y = pos[(uint64_t)i * 3 + 1], z = pos[(uint64_t)i * 3 + 2];
+  const double d = ((v2 * x + v6 * y) + v10 * z) + v14;
+  float k = (float)(-d);
+  if (k == 0.0f) k = 0.0f;
+  const uint32_t u = f2u(k);
+  uint32_t ord = (u & 0x80000000u) ? ~u : (u | 0x80000000u);  // increasing with k
+  if (k != k) ord = 0u;
+  keys[i] = ((unsigned long long)(~ord) << 32) | i;
+}
+
+}  // namespace
+
+cudaError_t launch_sort_back_to_front(const FrameArgs& a, const double vrow[4], uint32_t* out, cudaStream_t s) {
+  if (!a.N) return cudaSuccess;
+  k_view_keys<<<(a.N + 255) / 256, 256, 0, s>>>(a.pos, a.N, vrow[0], vrow[1], vrow[2], vrow[3], a.dkeys_a, a.ctl);
+  RadixJob j{};
+  j.count = a.ctl + kCtlSortCount;
+  j.flags = a.ctl + kCtlSortFlags;
+  j.tile_digits = a.tile_digits;
+  j.bin_base = a.bin_base;
+  j.tiles_cap = a.radix_tiles_cap;
+  j.low_mask = 0xFFFFFFFFull;
+  for (uint32_t p = 0; p < 4; ++p) {
+    j.in = (p & 1u) ? a.dkeys_b : a.dkeys_a;
+    j.out = (p & 1u) ? a.dkeys_a : a.dkeys_b;
+    j.out_low = out;
+    j.shift = 32u + 8u * p;
+    j.bits = 8u;
+    cudaError_t e = launch_radix_pass(j, p == 3, a.num_sms, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s) {
   if (a.sorted_keys) k_log_depth_keys<<<a.num_sms * 4, 256, 0, s>>>(a);
   return cudaGetLastError();

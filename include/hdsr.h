@@ -233,6 +233,16 @@ typedef struct hdsr_grad_views {
  * bitwise reproducible from run to run. */
 hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* grads, void* stream);
 
+/* sortedIndices on the device: the back-to-front order of the bound scene's
+ * positions for a view matrix (column-major, as in the frame uniforms), as
+ * gpuSortPrototype.ts:120-163 defines it (simulateGpuViewDepthSortPrototype):
+ * key = f32(-(view[2] x + view[6] y + view[10] z + view[14])) with the sum in
+ * double, descending, ties by ascending splat id (-0 equal to +0; NaN keys
+ * last). Writes splat_count u32 to `sorted_out` (device; it may be the bound
+ * sortedIndices buffer) on `stream`; uses the handle's depth-sort scratch, so
+ * it is ordered with the handle's frames on one stream. */
+hdsr_status hdsr_sort_back_to_front(hdsr_compositor* h, const float view[16], uint32_t* sorted_out, void* stream);
+
 /* ---- Serving loop ---------------------------------------------------------
  * No reference counterpart: the reference renders one scene per page
  * (splatRenderer.ts loadScene :866-961, renderFrame :1024-1140). A server
