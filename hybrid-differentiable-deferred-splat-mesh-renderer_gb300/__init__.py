@@ -4,7 +4,7 @@ The compute path is libhdsr.so (hand-written sm_103a CUDA behind the C ABI in
 include/hdsr.h); this package is the host-side mirror of the reference's
 operator API plus scene packing, camera conventions and synthetic workloads.
 """
-from . import _build, _lib, camera, differentiable, serving, splats, workloads
+from . import _build, _lib, assets, camera, differentiable, serving, splats, workloads
 from .compositor import (
     TileSplatCompositorPlan,
     TileSplatCompositorResources,
@@ -27,6 +27,7 @@ load_library = _lib.load
 __all__ = [
     "TileSplatCompositorPlan",
     "TileSplatCompositorResources",
+    "assets",
     "build",
     "camera",
     "create_output_textures",
