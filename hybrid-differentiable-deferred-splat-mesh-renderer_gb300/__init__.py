@@ -4,7 +4,7 @@ The compute path is libhdsr.so (hand-written sm_103a CUDA behind the C ABI in
 include/hdsr.h); this package is the host-side mirror of the reference's
 operator API plus scene packing, camera conventions and synthetic workloads.
 """
-from . import _build, _lib, assets, camera, differentiable, serving, splats, workloads
+from . import _build, _lib, assets, camera, differentiable, ply, serving, splats, workloads
 from .compositor import (
     TileSplatCompositorPlan,
     TileSplatCompositorResources,
@@ -41,6 +41,7 @@ __all__ = [
     "frame_uniforms_for",
     "load_library",
     "plan_tile_splat_compositor",
+    "ply",
     "sort_back_to_front",
     "splats",
     "workloads",

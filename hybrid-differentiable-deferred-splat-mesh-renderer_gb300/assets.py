@@ -54,7 +54,7 @@ class SplatBounds:
 
 
 @dataclass
-class FirstSmokeScene:
+class SplatScene:
     """A decoded asset: the compositor's attributes plus what the reference
     keeps beside them (per-row radii, original ids, bounds, source kind)."""
 
@@ -297,7 +297,7 @@ def _first_bad_row(opacity: np.ndarray, radius: np.ndarray, op_path: str, rad_pa
 
 def decode_first_smoke_manifest(manifest, payload: bytes, ids: bytes | None = None, scales: bytes | None = None,
                                 rotations: bytes | None = None, sh: bytes | None = None,
-                                roughness: bytes | None = None, metalness: bytes | None = None) -> FirstSmokeScene:
+                                roughness: bytes | None = None, metalness: bytes | None = None) -> SplatScene:
     """The manifest dict and the sidecars' bytes (None where absent)."""
     root = _record(manifest, "manifest")
     count = _positive_int(_first(root.get("splat_count"), root.get("count")), "splat_count")
@@ -327,10 +327,10 @@ def decode_first_smoke_manifest(manifest, payload: bytes, ids: bytes | None = No
     original = decode_original_ids(None, count) if ids is None else decode_original_id_bytes(ids, count)
     attrs = SplatAttributes(positions=positions, scales=log_scales, rotations=rot, opacities=opacity, colors=colors,
                             sh=coeffs, sh_degree=degree, roughness=rough, metalness=metal)
-    return FirstSmokeScene(attributes=attrs, radii=radius, original_ids=original, bounds=bounds, source_kind=kind)
+    return SplatScene(attributes=attrs, radii=radius, original_ids=original, bounds=bounds, source_kind=kind)
 
 
-def decode_first_smoke_payload(payload) -> FirstSmokeScene:
+def decode_first_smoke_payload(payload) -> SplatScene:
     """Inline JSON: {metadata?, splats: [rows]} or {metadata?, attributes: {planar arrays}}."""
     root = _record(payload, "payload")
     meta = root if root.get("metadata") is None else _record(root["metadata"], "metadata")
@@ -371,7 +371,7 @@ def decode_first_smoke_payload(payload) -> FirstSmokeScene:
     kind = _string(_first(meta.get("sourceKind"), "real_scaniverse_ply"), "sourceKind")
     original = decode_original_ids(root.get("originalIds"), count)
     attrs = SplatAttributes(positions=positions, scales=log_scales, rotations=rot, opacities=opacity, colors=colors)
-    return FirstSmokeScene(attributes=attrs, radii=radius, original_ids=original, bounds=bounds, source_kind=kind)
+    return SplatScene(attributes=attrs, radii=radius, original_ids=original, bounds=bounds, source_kind=kind)
 
 
 def _is_sidecar_manifest(doc) -> bool:
@@ -398,7 +398,7 @@ def _sidecar_shape_path(root: dict, key: str):
     return None if shape.get(key) is None else _string(shape[key], f"shape.{key}")
 
 
-def load_first_smoke(path) -> FirstSmokeScene:
+def load_first_smoke(path) -> SplatScene:
     """A manifest (sidecars read beside it) or an inline JSON payload."""
     mpath = Path(path)
     doc = json.loads(mpath.read_text())
