@@ -4,7 +4,7 @@ The compute path is libhdsr.so (hand-written sm_103a CUDA behind the C ABI in
 include/hdsr.h); this package is the host-side mirror of the reference's
 operator API plus scene packing, camera conventions and synthetic workloads.
 """
-from . import _build, _lib, assets, camera, differentiable, ply, serving, splats, workloads
+from . import _build, _lib, assets, camera, deferred, differentiable, ply, serving, splats, workloads
 from .compositor import (
     TileSplatCompositorPlan,
     TileSplatCompositorResources,
@@ -33,6 +33,7 @@ __all__ = [
     "create_output_textures",
     "create_tile_splat_bind_groups",
     "create_tile_splat_compositor",
+    "deferred",
     "differentiable",
     "encode_backward",
     "serving",

@@ -112,6 +112,36 @@ class ServerStats(ctypes.Structure):
 SERVER_NO_GRAPH = 0x1
 
 
+class PostInputs(ctypes.Structure):
+    _fields_ = [("color", c_void_p), ("color_pitch", c_uint64), ("color_format", c_uint32), ("_pad", c_uint32),
+                ("depth", c_void_p), ("depth_pitch", c_uint64), ("normal", c_void_p), ("normal_pitch", c_uint64),
+                ("material", c_void_p), ("material_pitch", c_uint64)]
+
+
+class PostParams(ctypes.Structure):
+    """hdsr_post_params; the oracle's orp_params has the same layout."""
+
+    _fields_ = [("view_proj_inverse", c_float * 16), ("camera_pos", c_float * 3), ("normal_recovery_mode", c_uint32),
+                ("grazing_start", c_float), ("grazing_end", c_float), ("bilateral_spatial_sigma", c_float),
+                ("bilateral_depth_sigma", c_float), ("bilateral_normal_sigma", c_float),
+                ("bilateral_radius", c_uint32), ("proj", c_float * 16), ("view", c_float * 16),
+                ("near_plane", c_float), ("far_plane", c_float), ("ao_radius_world", c_float),
+                ("ao_falloff_end", c_float), ("ao_intensity", c_float), ("ao_thickness", c_float),
+                ("ao_slices", c_uint32), ("ao_steps", c_uint32), ("frame_counter", c_uint32),
+                ("ao_denoise_strength", c_float), ("bloom_threshold", c_float), ("bloom_soft_knee", c_float),
+                ("light_dir", c_float * 3), ("light_intensity", c_float), ("ambient_intensity", c_float),
+                ("specular_only", c_uint32), ("emissive_intensity", c_float), ("emissive_threshold", c_float),
+                ("env_intensity", c_float), ("env_rotation", c_float), ("exposure", c_float),
+                ("fallback_roughness", c_float), ("fallback_metallic", c_float)]
+
+
+POST_BUFFER_IDS = {
+    "screen_normals": 0, "normals": 1, "depth_mip0": 2, "depth_mip1": 3, "depth_mip2": 4, "ao_raw": 5, "ao": 6,
+    "bloom": 7, "bloom_h": 8, "brdf_lut": 9, "env": 10, "curves": 11,
+}
+POST_PASSES = ("ss_normals", "bilateral", "gtao_prefilter", "gtao_main", "gtao_denoise", "bloom", "lighting")
+
+
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_pairs", c_uint64), ("pair_capacity", c_uint64), ("visible_splats", c_uint32),
                 ("superblock_entries", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
@@ -155,6 +185,16 @@ SIGNATURES = {
     "hdsr_pass_times": (c_int, [c_void_p, POINTER(c_float), POINTER(c_uint32), c_uint32, POINTER(c_uint32)]),
     "hdsr_pass_name": (c_char_p, [c_uint32]),
     "hdsr_launch_count": (c_uint64, [c_void_p]),
+    "hdsr_post_create": (c_int, [c_uint32, c_uint32, POINTER(c_void_p)]),
+    "hdsr_post_destroy": (None, [c_void_p]),
+    "hdsr_post_default_params": (None, [POINTER(PostParams)]),
+    "hdsr_post_set_environment": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p]),
+    "hdsr_post_set_material_curves": (c_int, [c_void_p, POINTER(c_float)]),
+    "hdsr_post_encode": (c_int, [c_void_p, POINTER(PostInputs), POINTER(PostParams), c_void_p, c_uint64, c_void_p]),
+    "hdsr_post_get_buffer": (c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(c_uint64)]),
+    "hdsr_post_set_profiling": (c_int, [c_void_p, c_int]),
+    "hdsr_post_pass_times": (c_int, [c_void_p, POINTER(c_float)]),
+    "hdsr_post_last_error": (c_char_p, [c_void_p]),
     "hdsr_count_tile_refs_static": (c_int, [c_void_p, c_uint32, c_uint64, c_uint32, c_uint32, c_void_p, c_uint64,
                                             c_void_p]),
 }

@@ -317,6 +317,95 @@ hdsr_status hdsr_count_tile_refs_static(const uint32_t* tile_boxes, uint32_t box
                                         uint64_t splat_count, uint32_t tile_columns, uint32_t tile_rows,
                                         uint32_t* tile_counts, uint64_t tile_counts_len, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Deferred passes over the G-buffer: the frame tail that
+ * splatRenderer.ts:1042-1139 encodes after the compositor — screen-space
+ * normal reconstruction (createScreenSpaceNormalsPass :317-385), the
+ * bilateral normal filter (createBilateralNormalFilter :387-440), GTAO
+ * (gtao.ts createGTAO: depth prefilter, main, denoise), bloom (bloom.ts
+ * createBloom: threshold, horizontal and vertical blur), material curve LUTs
+ * (materialCurves.ts), IBL (ibl.ts: BRDF LUT, equirect mip chain) and
+ * deferred lighting (createDeferredLightingPass :442-556).
+ * One hdsr_post per viewport size; its intermediate images live in the
+ * handle, the inputs are the compositor's output views. */
+typedef struct hdsr_post hdsr_post;
+
+typedef struct hdsr_post_inputs {
+  const void* color;        uint64_t color_pitch;     /* compositor colour, rgba16f or rgba32f */
+  uint32_t color_format;    uint32_t _pad;            /* HDSR_COLOR_* */
+  const float* depth;       uint64_t depth_pitch;     /* r32f NDC depth */
+  const uint32_t* normal;   uint64_t normal_pitch;    /* r32u oct normal (source normals) */
+  const uint32_t* material; uint64_t material_pitch;  /* rgba32u */
+} hdsr_post_inputs;
+
+/* Per-frame parameters; hdsr_post_default_params() fills the reference's
+ * defaults (main.ts DEFAULT_SETTINGS :144-169, DEFAULT_GTAO_PARAMS,
+ * DEFAULT_BLOOM_PARAMS, the constants of each pass's encode()). */
+typedef struct hdsr_post_params {
+  float view_proj_inverse[16];  /* mat4Inverse(lightingViewProj), column-major */
+  float camera_pos[3];
+  uint32_t normal_recovery_mode;/* 0 screen-space, 1 grazing recovery, 2 source normals */
+  float grazing_start, grazing_end;   /* 0.45, 0.80 */
+  float bilateral_spatial_sigma, bilateral_depth_sigma, bilateral_normal_sigma;  /* 3, 0.05, 1.5 */
+  uint32_t bilateral_radius;          /* 3 (at most 8) */
+  float proj[16];               /* projMatrix: GTAO projInfo */
+  float view[16];               /* lightingViewMatrix: GTAO normal transform */
+  float near_plane, far_plane;  /* 0.01, 100 */
+  float ao_radius_world, ao_falloff_end, ao_intensity, ao_thickness;   /* 0.15, 1, 1.5, 1.81 */
+  uint32_t ao_slices, ao_steps, frame_counter;                         /* 3, 4, 0 */
+  float ao_denoise_strength;                                           /* 60 */
+  float bloom_threshold, bloom_soft_knee;                              /* 0.8, 0.5 */
+  float light_dir[3];
+  float light_intensity, ambient_intensity;                            /* 3, 0.12 */
+  uint32_t specular_only;
+  float emissive_intensity, emissive_threshold;                        /* 3, 0.05 */
+  float env_intensity, env_rotation, exposure;                         /* 1, 0, 1 */
+  float fallback_roughness, fallback_metallic;                         /* 0.65, 0 (unused by the shader) */
+} hdsr_post_params;
+
+/* Intermediate images, readable with hdsr_post_get_buffer (dense rows). */
+typedef enum hdsr_post_buffer_id {
+  HDSR_POST_SCREEN_NORMALS = 0, /* u32 W*H: pack2x16float(oct), screen-space pass */
+  HDSR_POST_NORMALS = 1,        /* u32 W*H: bilateral output (what GTAO and lighting read) */
+  HDSR_POST_DEPTH_MIP0 = 2,     /* f32 W*H linear view depth */
+  HDSR_POST_DEPTH_MIP1 = 3,     /* f32 ceil(W/2)*ceil(H/2), 2x2 min */
+  HDSR_POST_DEPTH_MIP2 = 4,     /* f32 ceil(W/4)*ceil(H/4) */
+  HDSR_POST_AO_RAW = 5,         /* rgba16f W*H: ao, bent-normal oct, 0 */
+  HDSR_POST_AO = 6,             /* rgba16f W*H: denoised */
+  HDSR_POST_BLOOM = 7,          /* rgba16f ceil(W/2)*ceil(H/2): after both blurs */
+  HDSR_POST_BLOOM_H = 8,        /* rgba16f: after the horizontal blur */
+  HDSR_POST_BRDF_LUT = 9,       /* u32 256*256: pack2x16float(scale, bias) */
+  HDSR_POST_ENV = 10,           /* rgba16f equirect mip chain, level 0 first */
+  HDSR_POST_CURVES = 11         /* u16 3*256: roughness, metalness, albedo LUTs (f16) */
+} hdsr_post_buffer_id;
+
+/* createGTAO / createBloom / createIBL / createMaterialCurves for one viewport.
+ * Generates the BRDF LUT (ibl_brdf_lut.wgsl), the identity curves and the 1x1
+ * placeholder environment (no IBL until hdsr_post_set_environment). */
+hdsr_status hdsr_post_create(uint32_t width, uint32_t height, hdsr_post** out);
+void hdsr_post_destroy(hdsr_post* p);
+void hdsr_post_default_params(hdsr_post_params* params);
+/* IBLResources.loadEquirectRGBA (ibl.ts:107-149): level 0 as rgba16f texels
+ * (host memory, w*h*4 halves), the mip chain by 2x2 box filter
+ * (ibl_mipgen.wgsl). width or height 0 restores the placeholder. */
+hdsr_status hdsr_post_set_environment(hdsr_post* p, const uint16_t* rgba16f, uint32_t width, uint32_t height,
+                                      void* stream);
+/* MaterialCurves.update (materialCurves.ts:100-104): (contrast, brightness,
+ * gamma) for roughness, metalness and albedo, generated on the host. */
+hdsr_status hdsr_post_set_material_curves(hdsr_post* p, const float curves[9]);
+/* The frame tail: normals -> bilateral -> GTAO (prefilter, main, denoise),
+ * bloom on the handle's side stream, then lighting into `lit` (rgba16f,
+ * lit_pitch bytes per row). Asynchronous on `stream`. */
+hdsr_status hdsr_post_encode(hdsr_post* p, const hdsr_post_inputs* in, const hdsr_post_params* params,
+                             void* lit, uint64_t lit_pitch, void* stream);
+hdsr_status hdsr_post_get_buffer(hdsr_post* p, hdsr_post_buffer_id id, void** device_ptr, uint64_t* bytes);
+/* With profiling on, passes run on one stream between CUDA events; times of
+ * the last encode in ms: ss_normals, bilateral, gtao_prefilter, gtao_main,
+ * gtao_denoise, bloom, lighting. */
+hdsr_status hdsr_post_set_profiling(hdsr_post* p, int enable);
+hdsr_status hdsr_post_pass_times(hdsr_post* p, float ms[7]);
+const char* hdsr_post_last_error(const hdsr_post* p);
+
 #ifdef __cplusplus
 }
 #endif

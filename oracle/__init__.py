@@ -19,6 +19,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 SRC = HERE / "hdsr_oracle.c"
+POST_SRC = HERE / "hdsr_post_oracle.c"
 CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"]
 
 FLAG_LARGE_SPLAT_CAP = 1
@@ -30,10 +31,10 @@ FLAG_BUCKET_KEY_MISMATCH = 16
 
 def build(force: bool = False) -> Path:
     """gcc recipe for liboracle.so (no -march flags: identical on x86 and Arm)."""
-    deps = [SRC, HERE / "hdsr_oracle.h"]
+    deps = [SRC, POST_SRC, HERE / "hdsr_oracle.h"]
     if force or not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in deps):
         cc = os.environ.get("CC", "gcc")
-        subprocess.run([cc, *CFLAGS, str(SRC), "-o", str(LIB), "-lm"], check=True)
+        subprocess.run([cc, *CFLAGS, str(SRC), str(POST_SRC), "-o", str(LIB), "-lm"], check=True)
     return LIB
 
 
@@ -294,3 +295,188 @@ def plan(W, H, tile, N, mult=16.0) -> np.ndarray:
     out = np.zeros(9, np.uint32)
     lib().orc_plan(W, H, tile, N, mult, _p(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# deferred frame tail (hdsr_post_oracle.c)
+# ---------------------------------------------------------------------------
+class PostInputs(ctypes.Structure):
+    _fields_ = [("W", c_int), ("H", c_int), ("color", c_void_p), ("depth", c_void_p), ("normal", c_void_p),
+                ("material", c_void_p)]
+
+
+class PostParams(ctypes.Structure):
+    """orp_params: the field layout of hdsr_post_params."""
+
+    _fields_ = [("view_proj_inverse", c_float * 16), ("camera_pos", c_float * 3), ("normal_recovery_mode", c_uint32),
+                ("grazing_start", c_float), ("grazing_end", c_float), ("bilateral_spatial_sigma", c_float),
+                ("bilateral_depth_sigma", c_float), ("bilateral_normal_sigma", c_float),
+                ("bilateral_radius", c_uint32), ("proj", c_float * 16), ("view", c_float * 16),
+                ("near_plane", c_float), ("far_plane", c_float), ("ao_radius_world", c_float),
+                ("ao_falloff_end", c_float), ("ao_intensity", c_float), ("ao_thickness", c_float),
+                ("ao_slices", c_uint32), ("ao_steps", c_uint32), ("frame_counter", c_uint32),
+                ("ao_denoise_strength", c_float), ("bloom_threshold", c_float), ("bloom_soft_knee", c_float),
+                ("light_dir", c_float * 3), ("light_intensity", c_float), ("ambient_intensity", c_float),
+                ("specular_only", c_uint32), ("emissive_intensity", c_float), ("emissive_threshold", c_float),
+                ("env_intensity", c_float), ("env_rotation", c_float), ("exposure", c_float),
+                ("fallback_roughness", c_float), ("fallback_metallic", c_float)]
+
+
+class PostEnv(ctypes.Structure):
+    _fields_ = [("texels", c_void_p), ("w", c_int), ("h", c_int), ("levels", c_int), ("lw", c_int * 16),
+                ("lh", c_int * 16), ("offset", c_uint32 * 16)]
+
+
+_post_ready = False
+
+
+def _post_lib():
+    global _post_ready
+    L = lib()
+    if not _post_ready:
+        vp = c_void_p
+        for nm, args in (("orp_ss_normals", [vp, vp, vp]), ("orp_bilateral", [vp, vp, vp, vp]),
+                         ("orp_gtao_prefilter", [vp, vp, vp, vp, vp]),
+                         ("orp_gtao_main", [vp, vp, vp, vp, vp, vp, vp]),
+                         ("orp_gtao_denoise", [vp, vp, vp, vp, vp]), ("orp_bloom_threshold", [vp, vp, vp]),
+                         ("orp_bloom_blur", [c_int, c_int, vp, vp, c_float, c_float, c_float, c_float]),
+                         ("orp_lighting", [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+                         ("orp_brdf_lut", [c_int, c_int, vp]), ("orp_env_mip", [vp, c_int, c_int, vp, c_int, c_int]),
+                         ("orp_curve_lut", [c_float, c_float, c_float, vp])):
+            getattr(L, nm).argtypes = args
+            getattr(L, nm).restype = None
+        for nm in ("orp_asin", "orp_sin", "orp_cos", "orp_log2"):
+            getattr(L, nm).argtypes = [c_float]
+            getattr(L, nm).restype = c_float
+        for nm in ("orp_atan2", "orp_pow"):
+            getattr(L, nm).argtypes = [c_float, c_float]
+            getattr(L, nm).restype = c_float
+        _post_ready = True
+    return L
+
+
+def post_inputs(color, depth, normal, material):
+    """(orp_inputs, keepalive) over host copies of the compositor's output images."""
+    keep = dict(color=np.ascontiguousarray(color, np.float32), depth=np.ascontiguousarray(depth, np.float32),
+                normal=np.ascontiguousarray(normal).view(np.uint32),
+                material=np.ascontiguousarray(material).view(np.uint32))
+    H, W = keep["depth"].shape
+    s = PostInputs(W, H, _p(keep["color"]), _p(keep["depth"]), _p(keep["normal"]), _p(keep["material"]))
+    return s, keep
+
+
+def _addr(q):
+    return ctypes.addressof(q)
+
+
+def post_ss_normals(inp, params) -> np.ndarray:
+    out = np.zeros((inp.H, inp.W), np.uint32)
+    _post_lib().orp_ss_normals(ctypes.addressof(inp), _addr(params), _p(out))
+    return out
+
+
+def post_bilateral(inp, params, ssn) -> np.ndarray:
+    ssn = np.ascontiguousarray(ssn).view(np.uint32)
+    out = np.zeros((inp.H, inp.W), np.uint32)
+    _post_lib().orp_bilateral(ctypes.addressof(inp), _addr(params), _p(ssn), _p(out))
+    return out
+
+
+def post_gtao_prefilter(inp, params):
+    W, H = inp.W, inp.H
+    m0 = np.zeros((H, W), np.float32)
+    m1 = np.zeros(((H + 1) // 2, (W + 1) // 2), np.float32)
+    m2 = np.zeros(((H + 3) // 4, (W + 3) // 4), np.float32)
+    _post_lib().orp_gtao_prefilter(ctypes.addressof(inp), _addr(params), _p(m0), _p(m1), _p(m2))
+    return m0, m1, m2
+
+
+def post_gtao_main(inp, params, mips, normals) -> np.ndarray:
+    m0, m1, m2 = (np.ascontiguousarray(m, np.float32) for m in mips)
+    nrm = np.ascontiguousarray(normals).view(np.uint32)
+    out = np.zeros((inp.H, inp.W, 4), np.uint16)
+    _post_lib().orp_gtao_main(ctypes.addressof(inp), _addr(params), _p(m0), _p(m1), _p(m2), _p(nrm), _p(out))
+    return out
+
+
+def post_gtao_denoise(inp, params, ao_raw, mip0) -> np.ndarray:
+    a = np.ascontiguousarray(ao_raw).view(np.uint16)
+    m0 = np.ascontiguousarray(mip0, np.float32)
+    out = np.zeros((inp.H, inp.W, 4), np.uint16)
+    _post_lib().orp_gtao_denoise(ctypes.addressof(inp), _addr(params), _p(a), _p(m0), _p(out))
+    return out
+
+
+def post_bloom_threshold(inp, params) -> np.ndarray:
+    out = np.zeros(((inp.H + 1) // 2, (inp.W + 1) // 2, 4), np.uint16)
+    _post_lib().orp_bloom_threshold(ctypes.addressof(inp), _addr(params), _p(out))
+    return out
+
+
+def post_bloom_blur(src, dirx: float, diry: float, tx: float, ty: float) -> np.ndarray:
+    s = np.ascontiguousarray(src).view(np.uint16)
+    hh, hw = s.shape[:2]
+    out = np.zeros_like(s)
+    _post_lib().orp_bloom_blur(hw, hh, _p(s), _p(out), dirx, diry, tx, ty)
+    return out
+
+
+def post_env_chain(level0) -> dict:
+    """ibl_mipgen.wgsl chain over level 0 (h, w, 4) rgba16f bits; the PostEnv fields."""
+    L = _post_lib()
+    l0 = np.ascontiguousarray(level0).view(np.uint16)
+    h, w = l0.shape[:2]
+    levels = 1
+    while (max(w, h) >> levels) > 0:
+        levels += 1
+    dims = [(max(1, w >> k), max(1, h >> k)) for k in range(levels)]
+    offs = np.cumsum([0] + [a * b for a, b in dims])
+    tex = np.zeros((int(offs[-1]), 4), np.uint16)
+    tex[: w * h] = l0.reshape(-1, 4)
+    for k in range(1, levels):
+        (sw, sh), (dw, dh) = dims[k - 1], dims[k]
+        src = np.ascontiguousarray(tex[offs[k - 1]:offs[k]])
+        dst = np.zeros((dh * dw, 4), np.uint16)
+        L.orp_env_mip(_p(src), sw, sh, _p(dst), dw, dh)
+        tex[offs[k]:offs[k + 1]] = dst
+    return dict(texels=tex, w=w, h=h, levels=levels, dims=dims, offsets=[int(o) for o in offs[:-1]])
+
+
+def placeholder_env() -> dict:
+    return dict(texels=np.full((1, 4), 0x3C00, np.uint16), w=1, h=1, levels=1, dims=[(1, 1)], offsets=[0])
+
+
+def _env_struct(env: dict):
+    e = PostEnv(_p(env["texels"]), env["w"], env["h"], env["levels"])
+    for k in range(16):
+        lw, lh = env["dims"][k] if k < env["levels"] else (1, 1)
+        e.lw[k], e.lh[k] = lw, lh
+        e.offset[k] = env["offsets"][k] if k < env["levels"] else 0
+    return e
+
+
+def post_lighting(inp, params, normals, ao, env: dict, brdf, bloom, curves) -> np.ndarray:
+    keep = [np.ascontiguousarray(normals).view(np.uint32), np.ascontiguousarray(ao).view(np.uint16),
+            np.ascontiguousarray(brdf).view(np.uint32), np.ascontiguousarray(bloom).view(np.uint16),
+            np.ascontiguousarray(curves).view(np.uint16)]
+    e = _env_struct(env)
+    out = np.zeros((inp.H, inp.W, 4), np.uint16)
+    _post_lib().orp_lighting(ctypes.addressof(inp), _addr(params), _p(keep[0]), _p(keep[1]), ctypes.addressof(e),
+                             _p(keep[2]), _p(keep[3]), _p(keep[4]), _p(out))
+    return out
+
+
+def post_brdf_lut(y0: int = 0, y1: int = 256) -> np.ndarray:
+    out = np.zeros((256, 256), np.uint32)
+    _post_lib().orp_brdf_lut(y0, y1, _p(out))
+    return out
+
+
+def post_curve_lut(contrast: float, brightness: float, gamma: float) -> np.ndarray:
+    out = np.zeros(256, np.uint16)
+    _post_lib().orp_curve_lut(contrast, brightness, gamma, _p(out))
+    return out
+
+
+def post_math(name: str, *args) -> float:
+    return float(getattr(_post_lib(), "orp_" + name)(*[float(a) for a in args]))

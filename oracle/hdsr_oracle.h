@@ -162,6 +162,67 @@ void orc_logf_n(const float* in, float* out, uint64_t n);
 void orc_f16_rne_n(const float* in, uint16_t* out, uint64_t n);
 void orc_f16_trunc_n(const float* in, uint16_t* out, uint64_t n);
 void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n);
+
+/* ---- deferred frame tail (hdsr_post_oracle.c) ---- */
+typedef struct orp_inputs {
+  int W, H;
+  const float* color;        /* W*H*4, rgba as f32 (the compositor's f16 decoded) */
+  const float* depth;        /* W*H */
+  const uint32_t* normal;    /* W*H source oct normals */
+  const uint32_t* material;  /* W*H*4 */
+} orp_inputs;
+
+/* the same fields, order and meaning as hdsr_post_params (include/hdsr.h) */
+typedef struct orp_params {
+  float view_proj_inverse[16];
+  float camera_pos[3];
+  uint32_t normal_recovery_mode;
+  float grazing_start, grazing_end;
+  float bilateral_spatial_sigma, bilateral_depth_sigma, bilateral_normal_sigma;
+  uint32_t bilateral_radius;
+  float proj[16];
+  float view[16];
+  float near_plane, far_plane;
+  float ao_radius_world, ao_falloff_end, ao_intensity, ao_thickness;
+  uint32_t ao_slices, ao_steps, frame_counter;
+  float ao_denoise_strength;
+  float bloom_threshold, bloom_soft_knee;
+  float light_dir[3];
+  float light_intensity, ambient_intensity;
+  uint32_t specular_only;
+  float emissive_intensity, emissive_threshold;
+  float env_intensity, env_rotation, exposure;
+  float fallback_roughness, fallback_metallic;
+} orp_params;
+
+typedef struct orp_env {
+  const uint16_t* texels;    /* rgba16f mip chain, level 0 first */
+  int w, h, levels;
+  int lw[16], lh[16];
+  uint32_t offset[16];       /* texel offset of each level */
+} orp_env;
+
+void orp_ss_normals(const orp_inputs* in, const orp_params* q, uint32_t* out);
+void orp_bilateral(const orp_inputs* in, const orp_params* q, const uint32_t* ssn, uint32_t* out);
+void orp_gtao_prefilter(const orp_inputs* in, const orp_params* q, float* mip0, float* mip1, float* mip2);
+void orp_gtao_main(const orp_inputs* in, const orp_params* q, const float* mip0, const float* mip1,
+                   const float* mip2, const uint32_t* normals, uint16_t* ao_raw);
+void orp_gtao_denoise(const orp_inputs* in, const orp_params* q, const uint16_t* ao_raw, const float* mip0,
+                      uint16_t* ao);
+void orp_bloom_threshold(const orp_inputs* in, const orp_params* q, uint16_t* out);
+void orp_bloom_blur(int hw, int hh, const uint16_t* src, uint16_t* dst, float dirx, float diry, float tx, float ty);
+void orp_lighting(const orp_inputs* in, const orp_params* q, const uint32_t* normals, const uint16_t* ao,
+                  const orp_env* env, const uint32_t* brdf, const uint16_t* bloom, const uint16_t* curves,
+                  uint16_t* lit);
+void orp_brdf_lut(int y0, int y1, uint32_t* out);
+void orp_env_mip(const uint16_t* src, int sw, int sh, uint16_t* dst, int dw, int dh);
+void orp_curve_lut(float contrast, float brightness, float gamma, uint16_t out[256]);
+float orp_atan2(float y, float x);
+float orp_asin(float x);
+float orp_sin(float x);
+float orp_cos(float x);
+float orp_log2(float x);
+float orp_pow(float x, float y);
 void orc_morton_n(const uint32_t* x, const uint32_t* y, uint32_t* out, uint64_t n);
 void orc_bucket_key20_n(const uint32_t* depth_bits, uint64_t n, uint32_t dmin, uint32_t dmax,
                         uint32_t* buckets, uint32_t* keys);

@@ -1,0 +1,208 @@
+"""Host side of the deferred frame tail (no GPU): the restated host helpers
+(mat4Inverse, computeLightDirection, ibl.ts f32ToF16 and the Radiance HDR
+decoder, the material curve LUTs), the oracle's elementary functions against
+libm, and properties of the oracle's passes on small synthetic G-buffers."""
+import ctypes
+import math
+import struct
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def D(pkg):
+    return pkg.deferred
+
+
+def test_mat4_inverse(D):
+    rng = np.random.default_rng(1)
+    m = rng.normal(0, 1, 16).astype(np.float32)
+    inv = D.mat4_inverse(m)
+    ref = np.linalg.inv(m.astype(np.float64).reshape(4, 4).T).T.reshape(16)
+    np.testing.assert_allclose(inv, ref, rtol=1e-5, atol=1e-6)
+    assert D.mat4_inverse(np.zeros(16, np.float32)) is None
+    assert np.array_equal(D.mat4_inverse(np.eye(4, dtype=np.float32).reshape(16)), np.eye(4, dtype=np.float32).reshape(16))
+
+
+def test_light_direction_modes(D):
+    cam = (0.0, 1.0, 3.0)
+    c = D.light_direction("camera", cam, (0.0, 0.0, 0.0))
+    np.testing.assert_allclose(c, np.array([0, -1, -3]) / math.sqrt(10), rtol=1e-12)
+    assert D.light_direction("overhead", cam) == (0.0, -1.0, 0.0)
+    r = D.light_direction("rim", cam)
+    np.testing.assert_allclose(r, np.array([0, -0.5, 3]) / math.hypot(0.5, 3), rtol=1e-12)
+    f = D.light_direction("fixed", cam)
+    np.testing.assert_allclose(f, (math.cos(0.8) * math.cos(0.6), -math.sin(0.6), math.sin(0.8) * math.cos(0.6)))
+    assert D.light_direction("camera", cam, cam) == (0.0, 0.0, 0.0)  # `|| 1` guards the zero length
+
+
+def _f16_ibl_scalar(v: float) -> int:
+    """ibl.ts f32ToF16, one value at a time."""
+    bits = struct.unpack("<I", struct.pack("<f", v))[0]
+    sign = (bits >> 16) & 0x8000
+    raw = (bits >> 23) & 0xFF
+    frac = bits & 0x7FFFFF
+    if raw == 0xFF:
+        return sign | 0x7C01 if frac else sign | 0x7C00
+    e = raw - 127 + 15
+    if e >= 31:
+        return sign | 0x7C00
+    if e > 0:
+        return (sign | (e << 10) | (frac >> 13)) + ((frac >> 12) & 1)
+    if e > -10:
+        shift = 1 - e
+        return sign | (((0x800000 | frac) >> (13 + shift)) + (((0x800000 | frac) >> (12 + shift)) & 1))
+    return sign
+
+
+def test_f32_to_f16_ibl(D):
+    rng = np.random.default_rng(2)
+    vals = np.concatenate([np.float32([0, -0.0, 1, -1, 65504, 65519, 65520, 1e-5, 6e-8, 3e-8, 1e-9, np.inf, -np.inf,
+                                       np.nan, 0.5 + 2 ** -12, 0.5 + 3 * 2 ** -12]),
+                           rng.normal(0, 100, 2000).astype(np.float32), (rng.uniform(0, 1e-4, 500)).astype(np.float32)])
+    got = D.f32_to_f16_ibl(vals)
+    want = np.array([_f16_ibl_scalar(float(v)) for v in vals], np.uint16)
+    assert np.array_equal(got, want)
+
+
+def _hdr_bytes(rgbe: np.ndarray, rle: bool) -> bytes:
+    h, w = rgbe.shape[:2]
+    out = bytearray(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {h} +X {w}\n".encode())
+    for y in range(h):
+        if not rle:
+            out += rgbe[y].astype(np.uint8).tobytes()
+            continue
+        out += bytes([2, 2, w >> 8, w & 255])
+        for ch in range(4):
+            row = rgbe[y, :, ch]
+            x = 0
+            while x < w:  # alternate a run and a literal chunk
+                run = 1
+                while x + run < w and row[x + run] == row[x] and run < 127:
+                    run += 1
+                if run >= 3:
+                    out += bytes([128 + run, int(row[x])])
+                    x += run
+                else:
+                    n = min(w - x, 3)
+                    out += bytes([n]) + bytes(int(v) for v in row[x:x + n])
+                    x += n
+    return bytes(out)
+
+
+@pytest.mark.parametrize("rle", [False, True])
+def test_radiance_hdr_decode(D, rle):
+    rng = np.random.default_rng(3)
+    h, w = 5, 12
+    rgbe = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    rgbe[:, 4:9] = rgbe[:, 4:5]  # runs
+    rgbe[1, 2, 3] = 0             # e == 0 -> black
+    data = _hdr_bytes(rgbe, rle)
+    assert D.parse_hdr_header(data) == (w, h)
+    img = D.decode_radiance_hdr(data, 99, 99)  # the header's size wins
+    assert img.shape == (h, w, 4)
+    scale = np.power(2.0, rgbe[..., 3].astype(np.float64) - 136)
+    want = (rgbe[..., :3] * scale[..., None]).astype(np.float32)
+    want[rgbe[..., 3] == 0] = 0
+    assert np.array_equal(img[..., :3], want) and np.all(img[..., 3] == 1)
+    with pytest.raises(ValueError, match="Could not parse HDR resolution"):
+        D.parse_hdr_header(b"#?RADIANCE\n\n+X 4 -Y 2\n")
+
+
+def test_params_layout_matches_oracle(pkg, orc):
+    P, O = pkg._lib.PostParams, orc.PostParams
+    assert [f for f, _ in P._fields_] == [f for f, _ in O._fields_]
+    assert ctypes.sizeof(P) == ctypes.sizeof(O)
+    for f, _ in P._fields_:
+        assert getattr(P, f).offset == getattr(O, f).offset, f
+
+
+def test_oracle_elementary_functions(orc):
+    xs = np.linspace(-7.0, 7.0, 2001).astype(np.float32)
+    s = np.array([orc.post_math("sin", float(x)) for x in xs])
+    c = np.array([orc.post_math("cos", float(x)) for x in xs])
+    np.testing.assert_allclose(s, np.sin(xs.astype(np.float64)), atol=2.5e-7)
+    np.testing.assert_allclose(c, np.cos(xs.astype(np.float64)), atol=2.5e-7)
+    rng = np.random.default_rng(4)
+    ys, xs2 = rng.normal(0, 1, 2000).astype(np.float32), rng.normal(0, 1, 2000).astype(np.float32)
+    a = np.array([orc.post_math("atan2", float(y), float(x)) for y, x in zip(ys, xs2)])
+    np.testing.assert_allclose(a, np.arctan2(ys.astype(np.float64), xs2.astype(np.float64)), atol=4e-7)
+    for y, x, want in ((0.0, -1.0, math.pi), (-0.0, -1.0, -math.pi), (1.0, 0.0, math.pi / 2), (0.0, 0.0, 0.0)):
+        assert orc.post_math("atan2", y, x) == pytest.approx(want, abs=3e-7)
+    u = np.linspace(-1, 1, 1001).astype(np.float32)
+    np.testing.assert_allclose([orc.post_math("asin", float(v)) for v in u], np.arcsin(u.astype(np.float64)), atol=4e-4)
+    for x, y in ((0.5, 2.2), (0.2, 1 / 2.2), (0.9, 5.0), (3.0, 0.5)):
+        assert orc.post_math("pow", x, y) == pytest.approx(np.float32(x) ** np.float32(y), rel=3e-6)
+    assert orc.post_math("pow", 0.0, 5.0) == 0.0 and orc.post_math("pow", 1.0, 7.0) == 1.0
+    assert orc.post_math("log2", 8.0) == pytest.approx(3.0, rel=1e-7)
+
+
+def test_curve_lut(orc, pkg):
+    # materialCurves.ts generateLUT in double, f32 store, truncating f16
+    for c, b, g in ((1.0, 0.0, 1.0), (1.3, -0.05, 0.8), (0.0, 0.2, 2.0), (2.0, 0.0, 0.1)):
+        c32, b32, g32 = (float(np.float32(v)) for v in (c, b, g))
+        v = np.arange(256) / 255.0
+        v = np.clip((v - 0.5) * c32 + 0.5 + b32, 0, 1) ** g32
+        want = pkg.splats.f32_to_f16_trunc(np.clip(v, 0, 1).astype(np.float32))
+        assert np.array_equal(orc.post_curve_lut(c, b, g), want)
+
+
+def _flat_gbuffer(pkg, W=48, H=40, depth=0.5):
+    color = np.zeros((H, W, 4), np.float32)
+    color[..., :3] = 0.6
+    color[..., 3] = 1.0
+    d = np.full((H, W), depth, np.float32)
+    d[:, :4] = 1.0  # a background strip
+    normal = np.zeros((H, W), np.uint32)
+    material = np.zeros((H, W, 4), np.uint32)
+    material[..., 0] = int(pkg.splats.f32_to_f16_trunc(np.float32([0.5]))[0]) | (0 << 16)
+    return color, d, normal, material
+
+
+def test_oracle_passes_on_a_flat_wall(pkg, orc):
+    """A camera facing a constant-depth wall: reconstructed normals face the
+    camera, the wall occludes nothing, background pixels pass through."""
+    D = pkg.deferred
+    W, H = 48, 40
+    cam = pkg.camera.OrbitCamera(azimuth=0.0, elevation=0.0, distance=3.0)
+    q = D.frame_params(cam, W, H)
+    color, depth, normal, material = _flat_gbuffer(pkg, W, H, depth=0.9)
+    inp, keep = orc.post_inputs(color, depth, normal, material)
+    ssn = orc.post_ss_normals(inp, q)
+    n = orc.f16_to_f32(ssn.view(np.uint16).reshape(-1)).reshape(H, W, 2)
+    # a plane of constant NDC depth facing the camera encodes to oct (0, 0) up to rounding
+    assert np.abs(n[10:30, 10:40]).max() < 2e-2
+    assert np.all(ssn[:, :4] == 0)  # background, mode 0: the neutral word
+    nrm = orc.post_bilateral(inp, q, ssn)
+    assert np.all(nrm[:, :4] == ssn[:, :4])
+    m0, m1, m2 = orc.post_gtao_prefilter(inp, q)
+    assert m1.shape == ((H + 1) // 2, (W + 1) // 2) and np.all(m1 == np.minimum.reduceat(
+        np.minimum.reduceat(m0, np.arange(0, H, 2), 0), np.arange(0, W, 2), 1))
+    ao = orc.post_gtao_denoise(inp, q, orc.post_gtao_main(inp, q, (m0, m1, m2), nrm), m0)
+    aof = orc.f16_to_f32(ao[..., 0].reshape(-1)).reshape(H, W)
+    assert aof[8:32, 12:36].min() > 0.9  # a flat wall faces the camera: little occlusion
+    bloom = orc.post_bloom_threshold(inp, q)
+    assert np.all(orc.f16_to_f32(bloom[..., :3].reshape(-1)) == 0)  # no emissive, no bloom
+    lit = orc.post_lighting(inp, q, nrm, ao, orc.placeholder_env(), orc.post_brdf_lut(0, 0), bloom,
+                            np.stack([orc.post_curve_lut(1, 0, 1)] * 3))
+    litf = orc.f16_to_f32(lit.reshape(-1)).reshape(H, W, 4)
+    assert np.array_equal(litf[:, :4, :3], np.float32(orc.f16_to_f32(orc.f16_rne(color[:, :4, :3].reshape(-1)))).reshape(H, 4, 3))
+    assert np.all(litf[:, :4, 3] == 0) and np.all(litf[:, 4:, 3] == 1)
+    assert np.all(np.isfinite(litf)) and litf[:, 4:, :3].min() > 0
+
+
+def test_oracle_env_chain_and_bloom_blur(orc, pkg):
+    rng = np.random.default_rng(5)
+    img = rng.uniform(0, 4, (16, 32, 4)).astype(np.float32)
+    l0 = pkg.deferred.f32_to_f16_ibl(img.reshape(-1)).reshape(16, 32, 4)
+    env = orc.post_env_chain(l0)
+    assert env["levels"] == 6 and env["dims"][-1] == (1, 1)
+    # level 1 is the 2x2 box average of level 0, rounded to f16
+    l0f = orc.f16_to_f32(l0.reshape(-1)).reshape(16, 32, 4)
+    box = ((l0f[0::2, 0::2] + l0f[0::2, 1::2]) + l0f[1::2, 0::2] + l0f[1::2, 1::2]) * np.float32(0.25)
+    assert np.array_equal(env["texels"][512:512 + 128].reshape(8, 16, 4), orc.f16_rne(box.reshape(-1)).reshape(8, 16, 4))
+    # a blur of a constant image is that constant times the weights' sum (1 up to rounding)
+    const = np.tile(orc.f16_rne(np.float32([0.5, 0.25, 1.0, 1.0])), (6, 9, 1)).astype(np.uint16)
+    out = orc.f16_to_f32(orc.post_bloom_blur(const, 1 / 9, 0.0, 1 / 9, 1 / 6).reshape(-1)).reshape(6, 9, 4)
+    np.testing.assert_allclose(out[..., :3], np.broadcast_to([0.5, 0.25, 1.0], (6, 9, 3)), rtol=2e-3)
