@@ -475,6 +475,9 @@ def run_ours(args, rank, world, local):
         "roofline": roofline, "clocks": clocks.summary(),
         "gpu_back_to_front_sort_ms": round(sort_ms, 4),
     }
+    if rank == 0 and not args.no_deferred:
+        log("deferred tail leg")
+        out["deferred"] = run_deferred(pkg, F, wl, args, dev, cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_train:
         log("training leg")
         out["train"] = run_train(pkg, args, dev)
@@ -488,6 +491,76 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         print(json.dumps(out))
     res.destroy()
+
+
+def run_deferred(pkg, F, wl, args, dev, cpu: bool) -> dict:
+    """The deferred frame tail (normals, bilateral, GTAO, bloom, lighting) on
+    the timed frame's G-buffer at its viewport, unprofiled (bloom on the side
+    stream) and per pass (profiled), plus the oracle's time for the same tail."""
+    import torch
+
+    D = pkg.deferred
+    W, H = wl.width, wl.height
+    post = D.DeferredPasses(W, H)
+    post.set_environment(D.synthetic_environment(1024, 512, seed=0))
+    q = D.frame_params(wl.cameras[0], W, H)
+    lit = torch.zeros((H, W, 4), dtype=torch.float16, device=dev)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def tail():
+        post.encode(stream, F["color"], F["gb"], q, lit)
+
+    for _ in range(args.warmup):
+        tail()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        tail()
+        e.record(stream)
+        e.synchronize()
+        times.append(s.elapsed_time(e))
+    post.set_profiling(True)
+    passes = {}
+    for _ in range(args.steps):
+        flush.zero_()
+        tail()
+        for name, ms in post.pass_times():
+            passes.setdefault(name, []).append(ms)
+    post.set_profiling(False)
+    ms = statistics.mean(times)
+    out = {"ms": round(ms, 4), "tails_per_s": round(1000.0 / ms, 1),
+           "passes_ms": {k: round(statistics.mean(v), 4) for k, v in passes.items()},
+           "kernels_per_tail": 9, "viewport": [W, H],
+           "environment": "synthetic 1024x512 equirect, seeded (stand-in for the reference's 1k HDRI)"}
+    if cpu:
+        import oracle
+
+        torch.cuda.synchronize()
+        inp, keep = oracle.post_inputs(F["color"].float().cpu().numpy(), F["gb"]["depth"].cpu().numpy(),
+                                       F["gb"]["normal"].cpu().numpy(), F["gb"]["material"].cpu().numpy())
+        ew, eh = post.env_size
+        env = oracle.post_env_chain(post.buffer("env").cpu().numpy().view(np.uint16)[: ew * eh * 4].reshape(eh, ew, 4))
+        brdf = post.buffer("brdf_lut").cpu().numpy().view(np.uint32).reshape(256, 256)
+        curves = post.buffer("curves").cpu().numpy().view(np.uint16)[:768].reshape(3, 256)
+        hw, hh = (W + 1) // 2, (H + 1) // 2
+        tx, ty = float(np.float32(1.0 / hw)), float(np.float32(1.0 / hh))
+        t0 = time.perf_counter()
+        nrm = oracle.post_bilateral(inp, q, oracle.post_ss_normals(inp, q))
+        mips = oracle.post_gtao_prefilter(inp, q)
+        ao = oracle.post_gtao_denoise(inp, q, oracle.post_gtao_main(inp, q, mips, nrm), mips[0])
+        bloom = oracle.post_bloom_blur(oracle.post_bloom_blur(oracle.post_bloom_threshold(inp, q), tx, 0.0, tx, ty),
+                                       0.0, ty, tx, ty)
+        ref = oracle.post_lighting(inp, q, nrm, ao, env, brdf, bloom, curves)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(1.0 / dt, 4), "unit": "tails/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"one {W}x{H} tail through the oracle (C, OpenMP)"}
+        out["matches_oracle"] = bool(np.array_equal(ref, lit.cpu().numpy().view(np.uint16)))
+    post.destroy()
+    return out
 
 
 def load_traffic(kernel: str):
@@ -643,6 +716,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiler runs)")
     ap.add_argument("--no-train", action="store_true", help="skip the fwd+bwd leg (train500k)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg (8 scenes, 2,000 requests)")
+    ap.add_argument("--no-deferred", action="store_true", help="skip the deferred-tail leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -10,6 +10,8 @@
 //   log: x = m*2^e, m in [sqrt(1/2), sqrt(2)], s = (m-1)/(m+1),
 //        log(m) = 2 atanh(s) = 2s + 2s^3/3 + 2s^5/5 + 2s^7/7 + 2s^9/9.
 #pragma once
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #ifndef HDSR_HD
@@ -98,7 +100,13 @@ HDSR_HD float hx_logf(float x) {
 }
 
 // pack2x16float rounding: round-to-nearest-even, overflow -> inf, NaN -> 0x7E00.
+// On the device the conversion instruction rounds the same way (cvt.rn.f16.f32);
+// only its NaN encoding differs, so NaN is mapped first.
 HDSR_HD uint32_t f32_to_f16(float f) {
+#ifdef __CUDA_ARCH__
+  if (f != f) return 0x7E00u;
+  return (uint32_t)__half_as_ushort(__float2half_rn(f));
+#else
   uint32_t x = f2u(f);
   uint32_t sign = (x >> 16) & 0x8000u;
   uint32_t ax = x & 0x7FFFFFFFu;
@@ -114,9 +122,17 @@ HDSR_HD uint32_t f32_to_f16(float f) {
   uint32_t rem = mant & 0x1FFFu;
   if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h += 1u;
   return sign | h;
+#endif
 }
 
+// f16 -> f32 is exact; the device instruction keeps every value, NaNs are
+// rebuilt with their payload as the host path does.
 HDSR_HD float f16_to_f32(uint32_t h) {
+#ifdef __CUDA_ARCH__
+  if ((h & 0x7C00u) == 0x7C00u && (h & 0x3FFu) != 0u)
+    return u2f(((h & 0x8000u) << 16) | 0x7F800000u | ((h & 0x3FFu) << 13));
+  return __half2float(__ushort_as_half((unsigned short)(h & 0xFFFFu)));
+#else
   uint32_t sign = (h & 0x8000u) << 16;
   uint32_t e = (h >> 10) & 0x1Fu;
   uint32_t m = h & 0x3FFu;
@@ -126,6 +142,7 @@ HDSR_HD float f16_to_f32(uint32_t h) {
   }
   if (e == 31) return u2f(sign | 0x7F800000u | (m << 13));
   return u2f(sign | ((e + 112u) << 23) | (m << 13));
+#endif
 }
 
 HDSR_HD uint32_t pack2x16(float a, float b) { return f32_to_f16(a) | (f32_to_f16(b) << 16); }

@@ -136,10 +136,22 @@ __global__ void __launch_bounds__(256) k_ss_normals(PostArgs a) {
 // ---------------------------------------------------------------------------
 // bilateral normal filter
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void bilateral_tap(float4 c, F3 cn, float dden, float sd2, float ne, float spatialW,
+                                              float4 s, F3& acc, float& total) {
+  F3 sn = f3(s.x, s.y, s.z);
+  float depthDiff = fabsf(c.w - s.w) / dden;
+  float depthW = hx_expf(-depthDiff * depthDiff / sd2);
+  float normalW = px_pow(mx(dot(cn, sn), 0.0f), ne);
+  float w = spatialW * depthW * normalW;
+  acc = add(acc, muls(sn, w));
+  total = total + w;
+}
+
+template <int RC>
 __global__ void __launch_bounds__(256) k_bilateral(PostArgs a) {
   extern __shared__ float4 s_nd[];           // (16+2R)^2 decoded normal + depth
   __shared__ float s_spatial[17 * 17];
-  const int R = (int)a.p.bilateral_radius;
+  const int R = RC > 0 ? RC : (int)a.p.bilateral_radius;
   const int T = 16 + 2 * R;
   const int tid = threadIdx.y * 16 + threadIdx.x;
   const int bx = blockIdx.x * 16, by = blockIdx.y * 16;
@@ -166,19 +178,12 @@ __global__ void __launch_bounds__(256) k_bilateral(PostArgs a) {
   const float dden = mx(c.w, 0.001f);
   F3 acc = f3(0.0f, 0.0f, 0.0f);
   float total = 0.0f;
+#pragma unroll 1
   for (int dy = -R; dy <= R; ++dy) {
     const float4* row = s_nd + (threadIdx.y + R + dy) * T + threadIdx.x + R;
-    for (int dx = -R; dx <= R; ++dx) {
-      float4 s = row[dx];
-      F3 sn = f3(s.x, s.y, s.z);
-      float spatialW = s_spatial[(dy + R) * (2 * R + 1) + dx + R];
-      float depthDiff = fabsf(c.w - s.w) / dden;
-      float depthW = hx_expf(-depthDiff * depthDiff / sd2);
-      float normalW = px_pow(mx(dot(cn, sn), 0.0f), ne);
-      float w = spatialW * depthW * normalW;
-      acc = add(acc, muls(sn, w));
-      total = total + w;
-    }
+#pragma unroll
+    for (int dx = -R; dx <= R; ++dx)
+      bilateral_tap(c, cn, dden, sd2, ne, s_spatial[(dy + R) * (2 * R + 1) + dx + R], row[dx], acc, total);
   }
   a.nrm[idx] = oct_word(normalize(divs(acc, mx(total, 0.0001f))));
 }
@@ -255,6 +260,9 @@ __device__ __forceinline__ void horizon_sample(const PostArgs& a, const float pi
   }
 }
 
+// TC > 0: the step count known at compile time (t and the mip level of each
+// step do not depend on the slice, so they are computed once per pixel).
+template <int TC>
 __global__ void __launch_bounds__(256) k_gtao_main(PostArgs a, float4 projInfo) {
   int x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
   if (x >= a.W || y >= a.H) return;
@@ -276,20 +284,40 @@ __global__ void __launch_bounds__(256) k_gtao_main(PostArgs a, float4 projInfo) 
   const float a1 = 0.754877686500549316406f;   // f32(1 / 1.3247179572)
   const float a2 = a1 * a1;
   float sox = fractf((float)idxr * a1 + 0.5f), soy = fractf((float)idxr * a2 + 0.5f);
-  const uint32_t S = a.p.ao_slices, T = a.p.ao_steps;
+  const uint32_t S = a.p.ao_slices, T = TC > 0 ? (uint32_t)TC : a.p.ao_steps;
+  float tt[TC > 0 ? TC : 1];
+  int tm[TC > 0 ? TC : 1];
+  if (TC > 0) {
+#pragma unroll
+    for (int st = 1; st <= (TC > 0 ? TC : 1); ++st) {
+      float t = ((float)st + soy * 0.5f) / (float)T;
+      tt[st - 1] = t;
+      tm[st - 1] = to_i32(clampf(px_log2(pixelRadius * t / 4.0f), 0.0f, 2.0f));
+    }
+  }
   float totalAO = 0.0f;
   F3 bent = f3(0.0f, 0.0f, 0.0f);
   for (uint32_t sl = 0; sl < S; ++sl) {
     float phi = (3.14159274101257324219f / (float)S) * ((float)sl + sox);
     float ds, dc;
     px_sincos(phi, &ds, &dc);
+    const float dcp = dc * pixelRadius, dsp = ds * pixelRadius;
     float bestP = -1.0f, bestN = -1.0f;
-    for (uint32_t st = 1; st <= T; ++st) {
-      float t = ((float)st + soy * 0.5f) / (float)T;
-      float ox = dc * pixelRadius * t / a.vw, oy = ds * pixelRadius * t / a.vh;
-      int mip = to_i32(clampf(px_log2(pixelRadius * t / 4.0f), 0.0f, 2.0f));
-      horizon_sample(a, pi, u + ox, v + oy, mip, viewPos, vn, bestP);
-      horizon_sample(a, pi, u - ox, v - oy, mip, viewPos, vn, bestN);
+    if (TC > 0) {
+#pragma unroll
+      for (int k = 0; k < (TC > 0 ? TC : 1); ++k) {
+        float ox = dcp * tt[k] / a.vw, oy = dsp * tt[k] / a.vh;
+        horizon_sample(a, pi, u + ox, v + oy, tm[k], viewPos, vn, bestP);
+        horizon_sample(a, pi, u - ox, v - oy, tm[k], viewPos, vn, bestN);
+      }
+    } else {
+      for (uint32_t st = 1; st <= T; ++st) {
+        float t = ((float)st + soy * 0.5f) / (float)T;
+        float ox = dcp * t / a.vw, oy = dsp * t / a.vh;
+        int mip = to_i32(clampf(px_log2(pixelRadius * t / 4.0f), 0.0f, 2.0f));
+        horizon_sample(a, pi, u + ox, v + oy, mip, viewPos, vn, bestP);
+        horizon_sample(a, pi, u - ox, v - oy, mip, viewPos, vn, bestN);
+      }
     }
     float nds = vn.x * dc + vn.y * ds + vn.z * 0.0f;
     float cP = mx(bestP, nds * 0.08f), cN = mx(bestN, -nds * 0.08f);
@@ -357,22 +385,34 @@ __global__ void __launch_bounds__(256) k_bloom_threshold(PostArgs a) {
   a.bloom_a[(uint64_t)y * a.hw + x] = pack_h4(em.x * weight, em.y * weight, em.z * weight, 1.0f);
 }
 
-// bilinear sample of an rgba16f image; repeat_u selects repeat on u, else clamp-to-edge
+// bilinear sample of an rgba16f image; repeat_u selects repeat on u, else clamp-to-edge.
+// The corner indices equal floor(coordinate) (+1) wrapped or clamped; the
+// float is bounded first so the integer arithmetic cannot overflow (a bound
+// only moves indices that clamp to the same edge, or, for repeat, lie beyond
+// 2^24 texels, where the weights are NaN or the coordinate is not finite).
+__device__ __forceinline__ int wrap_index(int i, int w) {
+  if ((unsigned)i < (unsigned)w) return i;
+  int r = i % w;
+  return r < 0 ? r + w : r;
+}
 __device__ __forceinline__ float4 bilinear(const uint2* img, int w, int h, float u, float v, bool repeat_u) {
   float fx = u * (float)w - 0.5f, fy = v * (float)h - 0.5f;
   float x0f = floorf(fx), y0f = floorf(fy);
   float ax = fx - x0f, ay = fy - y0f;
-  long long x0 = to_i32(x0f), y0 = to_i32(y0f);
-  long long x1 = x0 + 1, y1 = y0 + 1;
+  int x0, x1;
   if (repeat_u) {
-    x0 = ((x0 % w) + w) % w;
-    x1 = ((x1 % w) + w) % w;
+    x0 = to_i32(clampf(x0f, -16777216.0f, 16777216.0f));
+    if (!(x0f == x0f)) x0 = 0;
+    x1 = wrap_index(x0 + 1, w);
+    x0 = wrap_index(x0, w);
   } else {
-    x0 = x0 < 0 ? 0 : (x0 > w - 1 ? w - 1 : x0);
-    x1 = x1 < 0 ? 0 : (x1 > w - 1 ? w - 1 : x1);
+    x0 = to_i32(clampf(x0f, -1.0f, (float)w));
+    x1 = clampi(x0 + 1, 0, w - 1);
+    x0 = clampi(x0, 0, w - 1);
   }
-  y0 = y0 < 0 ? 0 : (y0 > h - 1 ? h - 1 : y0);
-  y1 = y1 < 0 ? 0 : (y1 > h - 1 ? h - 1 : y1);
+  int y0 = to_i32(clampf(y0f, -1.0f, (float)h));
+  int y1 = clampi(y0 + 1, 0, h - 1);
+  y0 = clampi(y0, 0, h - 1);
   float4 t00 = h4(img[y0 * w + x0]), t10 = h4(img[y0 * w + x1]);
   float4 t01 = h4(img[y1 * w + x0]), t11 = h4(img[y1 * w + x1]);
   float bx = 1.0f - ax, by = 1.0f - ay;
@@ -410,9 +450,7 @@ __global__ void __launch_bounds__(256) k_bloom_blur(PostArgs a, const uint2* src
 constexpr float kPI = 3.14159274101257324219f;      // f32(3.14159265359)
 constexpr float kTwoPI = 6.28318548202514648438f;   // f32(2 * 3.14159265359)
 
-__device__ __forceinline__ float4 sample_env(const PostArgs& a, F3 dir, float lod) {
-  float s, c;
-  px_sincos(a.p.env_rotation, &s, &c);
+__device__ __forceinline__ float4 sample_env(const PostArgs& a, float s, float c, F3 dir, float lod) {
   F3 rd = f3(c * dir.x + s * dir.z, dir.y, -s * dir.x + c * dir.z);
   float u = px_atan2(rd.z, rd.x) / kTwoPI + 0.5f;
   float v = 0.5f - px_asin(clampf(rd.y, -1.0f, 1.0f)) / kPI;
@@ -467,7 +505,9 @@ __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
       mat4_mul(a.p.view_proj_inverse, nx, ny, 1.0f, 1.0f, wf);
       F3 vd = normalize(sub(f3(wf[0] / wf[3], wf[1] / wf[3], wf[2] / wf[3]),
                             f3(wn[0] / wn[3], wn[1] / wn[3], wn[2] / wn[3])));
-      float4 e = sample_env(a, vd, 0.0f);
+      float rs, rc;
+      px_sincos(a.p.env_rotation, &rs, &rc);
+      float4 e = sample_env(a, rs, rc, vd, 0.0f);
       F3 m = linear_to_srgb(tonemap(f3(e.x, e.y, e.z), a.p.exposure));
       *out = pack_h4(m.x, m.y, m.z, 0.0f);
     } else {
@@ -533,12 +573,14 @@ __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
       F3 diffDir = normalize(mix3(N, bentN, 0.5f));
       float maxLod = px_log2((float)a.env_w);
       float diffLod = mx(maxLod - 2.0f, 3.0f);
-      float4 irr = sample_env(a, diffDir, diffLod);
+      float rs, rc;
+      px_sincos(a.p.env_rotation, &rs, &rc);
+      float4 irr = sample_env(a, rs, rc, diffDir, diffLod);
       F3 diffIBL = f3(kD.x * albedo.x * irr.x, kD.y * albedo.y * irr.y, kD.z * albedo.z * irr.z);
       F3 I = neg(V);
       float dNI = 2.0f * dot(N, I);
       F3 Rr = f3(I.x - dNI * N.x, I.y - dNI * N.y, I.z - dNI * N.z);
-      float4 pref = sample_env(a, Rr, roughness * maxLod);
+      float4 pref = sample_env(a, rs, rc, Rr, roughness * maxLod);
       int bxi = to_i32(clampf(NdotV * 255.0f, 0.0f, 255.0f));
       int byi = to_i32(clampf(roughness * 255.0f, 0.0f, 255.0f));
       uint32_t bw = a.brdf[byi * kBrdfSize + bxi];
@@ -635,6 +677,18 @@ __global__ void __launch_bounds__(256) k_env_mip(const uint2* src, int sw, int s
 }
 
 dim3 grid16(int w, int h) { return dim3((unsigned)((w + 15) / 16), (unsigned)((h + 15) / 16)); }
+
+// the reference's radius (3) unrolled; any other radius loops
+void launch_bilateral(dim3 g, dim3 blk, size_t smem, cudaStream_t s, const PostArgs& a) {
+  if (a.p.bilateral_radius == 3u) k_bilateral<3><<<g, blk, smem, s>>>(a);
+  else k_bilateral<0><<<g, blk, smem, s>>>(a);
+}
+
+// the reference's 4 steps per side unrolled; any other count loops
+void launch_gtao_main(dim3 g, dim3 blk, cudaStream_t s, const PostArgs& a, float4 projInfo) {
+  if (a.p.ao_steps == 4u) k_gtao_main<4><<<g, blk, 0, s>>>(a, projInfo);
+  else k_gtao_main<0><<<g, blk, 0, s>>>(a, projInfo);
+}
 
 }  // namespace
 
@@ -902,11 +956,11 @@ hdsr_status hdsr_post_encode(hdsr_post* p, const hdsr_post_inputs* in, const hds
     cudaEventRecord(p->ev[0], s);
     k_ss_normals<<<g, blk, 0, s>>>(a);
     cudaEventRecord(p->ev[1], s);
-    k_bilateral<<<g, blk, bil_smem, s>>>(a);
+    launch_bilateral(g, blk, bil_smem, s, a);
     cudaEventRecord(p->ev[2], s);
     k_gtao_prefilter<<<g, blk, 0, s>>>(a);
     cudaEventRecord(p->ev[3], s);
-    k_gtao_main<<<g, blk, 0, s>>>(a, projInfo);
+    launch_gtao_main(g, blk, s, a, projInfo);
     cudaEventRecord(p->ev[4], s);
     k_gtao_denoise<<<g, blk, 0, s>>>(a);
     cudaEventRecord(p->ev[5], s);
@@ -933,9 +987,9 @@ hdsr_status hdsr_post_encode(hdsr_post* p, const hdsr_post_inputs* in, const hds
     }
     if (e == cudaSuccess) {
       k_ss_normals<<<g, blk, 0, s>>>(a);
-      k_bilateral<<<g, blk, bil_smem, s>>>(a);
+      launch_bilateral(g, blk, bil_smem, s, a);
       k_gtao_prefilter<<<g, blk, 0, s>>>(a);
-      k_gtao_main<<<g, blk, 0, s>>>(a, projInfo);
+      launch_gtao_main(g, blk, s, a, projInfo);
       k_gtao_denoise<<<g, blk, 0, s>>>(a);
       e = cudaStreamWaitEvent(s, p->join, 0);
     }
