@@ -26,6 +26,7 @@ enum Ctl : int {
   kCtlBwdTile = 20,    // dynamic tile counter of the adjoint rasteriser
   kCtlSortCount = 21,  // key count of the back-to-front sort (hdsr_sort_back_to_front)
   kCtlSortFlags = 22,  // its skip flags (always 0: the sort never skips)
+  kCtlScatterItem = 23,// dynamic work counter of the segment scatter
   kCtlWords = 64
 };
 

@@ -865,8 +865,8 @@ hdsr_status hdsr_post_set_environment(hdsr_post* p, const uint16_t* rgba16f, uin
                                       void* stream) {
   if (!p) return HDSR_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(p->side);
+  // earlier encodes may still read the old chain on any stream
+  cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(p, e, "set_environment sync");
   if (width == 0 || height == 0 || !rgba16f) return set_placeholder_env(p);
   if (width > 65536 || height > 65536) return fail(p, HDSR_ERR_INVALID_ARG, "environment larger than 65536");

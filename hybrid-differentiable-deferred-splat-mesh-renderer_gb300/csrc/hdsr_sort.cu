@@ -358,8 +358,13 @@ __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
   const uint32_t lt = lanemask_lt();
   const uint32_t total = a.ctl[kCtlSegments] * 2u;
   const uint32_t P = a.ctl[kCtlPairsLo];
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
+  // items (segment, half) from a counter: segments differ widely in work, a
+  // warp that finishes early takes the next one
+  for (;;) {
+    uint32_t w = 0u;
+    if (lane == 0u) w = atomicAdd(a.ctl + kCtlScatterItem, 1u);
+    w = __shfl_sync(0xFFFFFFFFu, w, 0);
+    if (w >= total) break;
     const uint32_t s = w >> 1, half = w & 1u;
     uint32_t sb, beg, end;
     seg_locate(a, tables, s, sb, beg, end);
