@@ -23,8 +23,13 @@ namespace hdsr {
 namespace {
 
 constexpr int kWarps = 4;
-constexpr int kFields = 19;
-enum Field { F_CX, F_CY, F_KA, F_KB, F_KC, F_OP, F_R, F_G, F_B, F_D, F_MR, F_MM, F_NX, F_NY, F_NZ, F_CF, F_ER, F_EG, F_EB };
+// A staged entry is five float4 rows (entry-major): the splat loop reads them
+// as five broadcast 16-byte loads; the staging stores (80-byte lane stride)
+// touch distinct banks within each 8-lane phase.
+//   row 0: cx, cy, -a/2, -b     row 1: -c/2, opacity, r, g
+//   row 2: b, depth, rough, met row 3: nx, ny, nz, confidence
+//   row 4: er, eg, eb, 0
+constexpr int kRows = 5;
 
 struct Quad {
   float T[4];
@@ -99,9 +104,10 @@ __device__ __forceinline__ float raster_expf(float x) {
   return p * u2f((uint32_t)(ki + 127) << 23);
 }
 
-__device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, const float (*s)[32], int i) {
-  const float cx = s[F_CX][i], cy = s[F_CY][i];
-  const float ka = s[F_KA][i], kb = s[F_KB][i], kc = s[F_KC][i];
+__device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, const float4 (*s)[kRows], int i) {
+  const float4 r0 = s[i][0], r1 = s[i][1];
+  const float cx = r0.x, cy = r0.y;
+  const float ka = r0.z, kb = r0.w, kc = r1.x;
   const float dx0 = p00x - cx, dy0 = p00y - cy;
   const float dx1 = dx0 + 1.0f, dy1 = dy0 + 1.0f;
   const float dxv[4] = {dx0, dx1, dx0, dx1};
@@ -110,11 +116,12 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
 #pragma unroll
   for (int k = 0; k < 4; ++k) pw[k] = fmaf(kc * dyv[k], dyv[k], fmaf(kb * dxv[k], dyv[k], (ka * dxv[k]) * dxv[k]));
   if (pw[0] <= -4.0f && pw[1] <= -4.0f && pw[2] <= -4.0f && pw[3] <= -4.0f) return;
-  const float op = s[F_OP][i];
-  const float sr = s[F_R][i], sg = s[F_G][i], sb = s[F_B][i];
-  const float sd = s[F_D][i], mr = s[F_MR][i], mm = s[F_MM][i];
-  const float nx = s[F_NX][i], ny = s[F_NY][i], nz = s[F_NZ][i];
-  const float sc = s[F_CF][i], er = s[F_ER][i], eg = s[F_EG][i], eb = s[F_EB][i];
+  const float4 r2 = s[i][2], r3 = s[i][3], r4 = s[i][4];
+  const float op = r1.y;
+  const float sr = r1.z, sg = r1.w, sb = r2.x;
+  const float sd = r2.y, mr = r2.z, mm = r2.w;
+  const float nx = r3.x, ny = r3.y, nz = r3.z;
+  const float sc = r3.w, er = r4.x, eg = r4.y, eb = r4.z;
   // a splat without emission adds exactly +0 to the emissive sums: skip it
   // (uniform across the warp, all lanes read the same splat)
   const bool emits = er != 0.0f || eg != 0.0f || eb != 0.0f;
@@ -190,28 +197,14 @@ __device__ __forceinline__ Row load_row(const FrameArgs& a, uint32_t e) {
   return w;
 }
 
-__device__ __forceinline__ void stage_row(float (*s)[32], const Row& w, uint32_t lane) {
-  s[F_CX][lane] = w.g.x;
-  s[F_CY][lane] = w.g.y;
-  s[F_KA][lane] = w.g.z * -0.5f;
-  s[F_KB][lane] = -w.g.w;
-  s[F_KC][lane] = u2f(w.ap.x) * -0.5f;
-  s[F_OP][lane] = hi16(w.ap.y);
-  s[F_R][lane] = lo16(w.ap.z);
-  s[F_G][lane] = hi16(w.ap.z);
-  s[F_B][lane] = lo16(w.ap.w);
-  s[F_D][lane] = u2f(w.depth);
-  s[F_MR][lane] = lo16(w.gb.x);
-  s[F_MM][lane] = hi16(w.gb.x);
+__device__ __forceinline__ void stage_row(float4 (*s)[kRows], const Row& w, uint32_t slot) {
   float nx, ny, nz;
   oct_decode(lo16(w.gb.y), hi16(w.gb.y), nx, ny, nz);
-  s[F_NX][lane] = nx;
-  s[F_NY][lane] = ny;
-  s[F_NZ][lane] = nz;
-  s[F_CF][lane] = lo16(w.conf);
-  s[F_ER][lane] = lo16(w.gb.z);
-  s[F_EG][lane] = hi16(w.gb.z);
-  s[F_EB][lane] = lo16(w.gb.w);
+  s[slot][0] = make_float4(w.g.x, w.g.y, w.g.z * -0.5f, -w.g.w);
+  s[slot][1] = make_float4(u2f(w.ap.x) * -0.5f, hi16(w.ap.y), lo16(w.ap.z), hi16(w.ap.z));
+  s[slot][2] = make_float4(lo16(w.ap.w), u2f(w.depth), lo16(w.gb.x), hi16(w.gb.x));
+  s[slot][3] = make_float4(nx, ny, nz, lo16(w.conf));
+  s[slot][4] = make_float4(lo16(w.gb.z), hi16(w.gb.z), lo16(w.gb.w), 0.0f);
 }
 
 // Can the entry reach any pixel centre of the rectangle [x0, x1] x [y0, y1]
@@ -259,10 +252,10 @@ __device__ __forceinline__ bool touches_rect(float cx, float cy, float ia, float
 
 // Work unit: half a tile (rows 0-7 or 8-15), taken from an atomic counter.
 __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(FrameArgs a) {
-  __shared__ float s_pay[kWarps][kFields][32];
+  __shared__ float4 s_pay[kWarps][32][kRows];
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  float (*s)[32] = s_pay[warp];
+  float4 (*s)[kRows] = s_pay[warp];
   const uint32_t items = 2u * a.tile_count;
   for (;;) {
     uint32_t item = 0;
