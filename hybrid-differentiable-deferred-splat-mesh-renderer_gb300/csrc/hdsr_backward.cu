@@ -23,10 +23,12 @@
 //                      alpha_k)) + dL/dA T_f / (1 - alpha_k),   A = 1 - T_f,
 //      and dL/dc_k = dL/dO w_k. Per entry the warp sums its lanes' values
 //      (butterfly shuffles) and one lane adds them to the entry's accumulators.
-//   3. k_project_bwd: per sortRank, recompute the projection in fp32 and apply
+//   3. k_project_bwd: per sortRank, recompute the projection (double-float) and apply
 //      the chain rule back to the scene arrays (atomic adds: a splat id may
 //      appear in sortedIndices more than once).
-#define HDSR_BWD_REAL double
+#ifndef HDSR_BWD_REAL
+#define HDSR_BWD_REAL df64
+#endif
 #include "hdsr_proj_adjoint.cuh"
 
 namespace hdsr {
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(128) k_project_bwd(BwdArgs b) {
   }
   // colour = clamp(SH(dir), 0, 1), dir = normalize(cam - p)
   {
-    const uint32_t deg = f2u(ld(U + 25));
+    const uint32_t deg = f2u(__ldg(U + 25));
     const uint32_t nb = (deg + 1) * (deg + 1) - 1;
     const uint32_t shStride = nb * 3;
     const uint64_t base = (uint64_t)id * (3 + shStride + 3);

@@ -1,10 +1,11 @@
 // hdsr_proj_adjoint.cuh — the projection of one splat recomputed with every
 // intermediate its adjoint needs (gpu_project_splats.wgsl:112-358, colour and
 // 2D conic), in the scalar type HDSR_BWD_REAL chosen by the including unit
-// (both use fp64: for splats seen nearly edge-on the conic and its adjoint
-// combine large terms that cancel, and at fp32 a few gradients land 1e-3 to
-// 1e-2 from the FP64 ones).
+// (both use double-float, df64, by default; fp64 on request: for splats seen
+// nearly edge-on the conic and its adjoint combine large terms that cancel,
+// and at fp32 a few gradients land 1e-3 to 1e-2 from the FP64 ones).
 #pragma once
+#include "hdsr_df64.cuh"
 #include "hdsr_internal.cuh"
 
 namespace hdsr {
@@ -12,11 +13,12 @@ namespace {
 
 // Scalar type of the recompute (HDSR_BWD_REAL, set by the including unit).
 #ifndef HDSR_BWD_REAL
-#error "define HDSR_BWD_REAL (float or double) before including hdsr_proj_adjoint.cuh"
+#error "define HDSR_BWD_REAL (float, double or df64) before including hdsr_proj_adjoint.cuh"
 #endif
 using real = HDSR_BWD_REAL;
 __device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ df64 rsqrt_(df64 x) { return df_sqrt(x); }
 __device__ __forceinline__ float rexp_(float x) { return hx_expf(x); }
 __device__ __forceinline__ double rexp_(double x) { return exp(x); }
 __device__ __forceinline__ real rmax_(real a, real b) { return a > b ? a : b; }
@@ -126,7 +128,7 @@ __device__ void proj_recompute(const FrameArgs& a, uint32_t id, Proj& P) {
   P.dlen = rsqrt_(dot(dv, dv));
   const real idl = real(1) / P.dlen;
   P.dir = f3(dv.x * idl, dv.y * idl, dv.z * idl);
-  const uint32_t deg = f2u(ld(U + 25));
+  const uint32_t deg = f2u(__ldg(U + 25));
   const uint32_t shStride = ((deg + 1) * (deg + 1) - 1) * 3;
   const float* sh = a.sh + (uint64_t)id * (3 + shStride + 3);
   real basis[15];
