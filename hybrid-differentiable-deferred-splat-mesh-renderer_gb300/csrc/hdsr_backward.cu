@@ -38,7 +38,10 @@ namespace {
 constexpr float kBgR = 0.02f, kBgG = 0.02f, kBgB = 0.04f;  // composite background (T-weighted)
 
 constexpr int kBwdWarps = 4;
-enum BField { B_CX, B_CY, B_KA, B_KB, B_KC, B_OP, B_R, B_G, B_B, B_IA, B_IB, B_IC, B_RANK, kBFields };
+// A staged entry is four float4 rows, read with broadcast 16-byte loads:
+//   row 0: cx, cy, -ia/2, -ib   row 1: -ic/2, opacity, r, g
+//   row 2: b, ia, ib, ic        row 3: sortRank bits, 0, 0, 0
+constexpr int kBRows = 4;
 
 // Same test as the rasteriser's (hdsr_raster.cu): can the entry reach a
 // pixel centre of [x0, x1] x [y0, y1] with power > -4 and alpha > 1/255?
@@ -72,7 +75,7 @@ __device__ __forceinline__ bool bwd_touches(float cx, float cy, float ia, float 
 // Stages entry e into slot `slot` of the batch if it can reach the half tile
 // [x0, x0 + 15] x [y0, y0 + 7]; returns whether it was kept (warp-collective:
 // every lane calls it, lanes without an entry pass valid = false).
-__device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float (*s)[32], uint32_t e, bool valid,
+__device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float4 (*s)[kBRows], uint32_t e, bool valid,
                                                    uint32_t lane, float x0, float y0) {
   const FrameArgs& a = b.f;
   bool keep = false;
@@ -88,19 +91,10 @@ __device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float (*s)[
   const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
   if (keep) {
     const uint32_t k = __popc(kept & ((1u << lane) - 1u));
-    s[B_CX][k] = p0.x;
-    s[B_CY][k] = p0.y;
-    s[B_KA][k] = p0.z * -0.5f;
-    s[B_KB][k] = -p0.w;
-    s[B_KC][k] = p1.x * -0.5f;
-    s[B_OP][k] = p1.y;
-    s[B_R][k] = p1.z;
-    s[B_G][k] = p1.w;
-    s[B_B][k] = p2.x;
-    s[B_IA][k] = p0.z;
-    s[B_IB][k] = p0.w;
-    s[B_IC][k] = p1.x;
-    s[B_RANK][k] = u2f(r);
+    s[k][0] = make_float4(p0.x, p0.y, p0.z * -0.5f, -p0.w);
+    s[k][1] = make_float4(p1.x * -0.5f, p1.y, p1.z, p1.w);
+    s[k][2] = make_float4(p2.x, p0.z, p0.w, p1.x);
+    s[k][3] = make_float4(u2f(r), 0.0f, 0.0f, 0.0f);
   }
   return __popc(kept);
 }
@@ -129,11 +123,11 @@ __device__ __forceinline__ uint32_t warp_sum9(const float (&g)[9], uint32_t lane
 }
 
 __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
-  __shared__ float s_pay[kBwdWarps][kBFields][32];
+  __shared__ float4 s_pay[kBwdWarps][32][kBRows];
   const FrameArgs& a = b.f;
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  float (*s)[32] = s_pay[warp];
+  float4 (*s)[kBRows] = s_pay[warp];
   const uint32_t items = 2u * a.tile_count;
   for (;;) {
     uint32_t item = 0;
@@ -165,8 +159,9 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       const uint32_t n = bwd_stage_kept(b, s, start + b0 + lane, lane < nb, lane, rx0, ry0);
       __syncwarp();
       for (uint32_t i = 0; i < n && !done; ++i) {
-        const float cx = s[B_CX][i], cy = s[B_CY][i], ka = s[B_KA][i], kb = s[B_KB][i], kc = s[B_KC][i];
-        const float op = s[B_OP][i];
+        const float4 r0 = s[i][0], r1 = s[i][1];
+        const float cx = r0.x, cy = r0.y, ka = r0.z, kb = r0.w, kc = r1.x;
+        const float op = r1.y;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const float dx = dxv[k] - cx, dy = dyv[k] - cy;
@@ -175,9 +170,9 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
           const bool valid = (pw > -4.0f) && (al > (1.0f / 255.0f)) && (T[k] >= 0.001f);
           if (valid) {
             const float w = al * T[k];
-            C[k][0] = fmaf(s[B_R][i], w, C[k][0]);
-            C[k][1] = fmaf(s[B_G][i], w, C[k][1]);
-            C[k][2] = fmaf(s[B_B][i], w, C[k][2]);
+            C[k][0] = fmaf(r1.z, w, C[k][0]);
+            C[k][1] = fmaf(r1.w, w, C[k][1]);
+            C[k][2] = fmaf(s[i][2].x, w, C[k][2]);
             T[k] = T[k] * (1.0f - al);
           }
         }
@@ -209,9 +204,10 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       const uint32_t n = bwd_stage_kept(b, s, start + b0 + lane, lane < nb, lane, rx0, ry0);
       __syncwarp();
       for (uint32_t i = 0; i < n; ++i) {
-        const float cx = s[B_CX][i], cy = s[B_CY][i], ka = s[B_KA][i], kb = s[B_KB][i], kc = s[B_KC][i];
-        const float op = s[B_OP][i], cr = s[B_R][i], cg = s[B_G][i], cb = s[B_B][i];
-        const float ia = s[B_IA][i], ib = s[B_IB][i], ic = s[B_IC][i];
+        const float4 r0 = s[i][0], r1 = s[i][1], r2 = s[i][2];
+        const float cx = r0.x, cy = r0.y, ka = r0.z, kb = r0.w, kc = r1.x;
+        const float op = r1.y, cr = r1.z, cg = r1.w, cb = r2.x;
+        const float ia = r2.y, ib = r2.z, ic = r2.w;
         float g[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         bool any = false;
 #pragma unroll
@@ -249,7 +245,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
         if (__any_sync(0xFFFFFFFFu, any)) {
           float v;
           const uint32_t j = warp_sum9(g, lane, v);
-          if (!(lane & 1u) && j < 9u && v != 0.0f) atomicAdd(b.g2d + (size_t)f2u(s[B_RANK][i]) * kG2d + j, v);
+          if (!(lane & 1u) && j < 9u && v != 0.0f) atomicAdd(b.g2d + (size_t)f2u(s[i][3].x) * kG2d + j, v);
         }
       }
       __syncwarp();
