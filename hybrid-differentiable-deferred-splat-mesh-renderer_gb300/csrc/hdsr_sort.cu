@@ -348,6 +348,11 @@ __global__ void __launch_bounds__(1024) k_seg_scan(FrameArgs a) {
     atomicOr(a.ctl + kCtlFlags, 0x8u);
 }
 
+#ifndef HDSR_SCATTER_STEP
+#define HDSR_SCATTER_STEP 8
+#endif
+constexpr int kScatterStep = HDSR_SCATTER_STEP;
+
 // Two warps per segment: half h takes tile rows 4h..4h+3 (tiles 32h + lane).
 __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
   constexpr uint32_t C = kSegEntries / 32u;
@@ -393,22 +398,29 @@ __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
       const uint32_t r = (uint32_t)k[c] & 0xFFFFFFu;
       uint32_t u = __reduce_or_sync(0xFFFFFFFFu, m);
       uint32_t inc = 0u;
+      // kScatterStep covered tiles per step: independent ballot / shuffle chains
       while (u) {
-        const uint32_t t0 = __ffs(u) - 1u;
-        u &= u - 1u;
-        const bool has1 = u != 0u;
-        const uint32_t t1 = has1 ? __ffs(u) - 1u : t0;
-        u &= u - 1u;  // no-op when u == 0
-        const bool take0 = (m >> t0) & 1u;
-        const bool take1 = has1 && ((m >> t1) & 1u);
-        const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, take0);
-        const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, take1);
-        const uint32_t o0 = __shfl_sync(0xFFFFFFFFu, pos, t0) + __popc(b0 & lt);
-        const uint32_t o1 = __shfl_sync(0xFFFFFFFFu, pos, t1) + __popc(b1 & lt);
-        if (take0 && o0 < P) a.entries[o0] = r;
-        if (take1 && o1 < P) a.entries[o1] = r;
-        if (lane == t0) inc += __popc(b0);
-        if (has1 && lane == t1) inc += __popc(b1);
+        uint32_t t[kScatterStep], bq[kScatterStep];
+        bool has[kScatterStep], tk[kScatterStep];
+#pragma unroll
+        for (int q = 0; q < kScatterStep; ++q) {
+          has[q] = u != 0u;
+          t[q] = has[q] ? __ffs(u) - 1u : 0u;
+          u &= u - 1u;  // no-op when u == 0
+        }
+#pragma unroll
+        for (int q = 0; q < kScatterStep; ++q) {
+          tk[q] = has[q] && ((m >> t[q]) & 1u);
+          bq[q] = __ballot_sync(0xFFFFFFFFu, tk[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < kScatterStep; ++q) {
+          const uint32_t o = __shfl_sync(0xFFFFFFFFu, pos, t[q]) + __popc(bq[q] & lt);
+          if (tk[q] && o < P) a.entries[o] = r;
+        }
+#pragma unroll
+        for (int q = 0; q < kScatterStep; ++q)
+          if (has[q] && lane == t[q]) inc += __popc(bq[q]);
       }
       pos += inc;
     }
