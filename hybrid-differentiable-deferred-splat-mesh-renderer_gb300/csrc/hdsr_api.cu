@@ -445,7 +445,6 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   if (fork && (e = cudaStreamWaitEvent(s, h->join_ev, 0)) != cudaSuccess) return cuda_fail(h, e, "join");
   // superblock lists in depth order, sorted by superblock (stable)
   if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
-  if ((e = launch_emit_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "emit_superblocks");
   RadixJob sj = dj;
   sj.count = a.ctl + kCtlSbPairs;
   sj.out_low = nullptr;
@@ -466,7 +465,7 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
     if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
     h->launches += 2;
   }
-  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 3 * kDepthPasses + 1 + n_splat_launch +
+  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 3 * kDepthPasses + 1 +
                  3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
   return HDSR_OK;
 }

@@ -91,7 +91,7 @@ struct FrameArgs {
   uint2* aux;                     // tile box u8x4, f16 normal confidence|0
   uint32_t* depth;                // f32 NDC depth bits
   uint32_t* ntiles;               // tiles touched per sortRank (0 if invisible)
-  unsigned long long* dkeys_a;    // depth << 32 | sortRank, per sortRank
+  unsigned long long* dkeys_a;    // depth << 32 | superblock count << 24 | sortRank, per sortRank
   unsigned long long* dkeys_b;
   uint32_t* order;                // sortRanks in ascending (depth, sortRank)
   uint32_t* nsb;                  // superblocks touched per sortRank
@@ -175,7 +175,6 @@ cudaError_t launch_tile_counts(const FrameArgs& a, cudaStream_t s);   // 2 launc
 cudaError_t launch_depth_range(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
-cudaError_t launch_emit_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
 cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 3 launches
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);

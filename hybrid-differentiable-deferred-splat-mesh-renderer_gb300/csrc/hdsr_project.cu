@@ -259,8 +259,11 @@ __global__ void __launch_bounds__(256) k_project(FrameArgs a) {
   a.aux[r] = make_uint2(box, pack2x16(conf, 0.0f));
   a.depth[r] = f2u(depthNdc);
   a.ntiles[r] = (t1x - t0x + 1u) * (t1y - t0y + 1u);
-  a.nsb[r] = ((t1x >> a.sb_shift) - (t0x >> a.sb_shift) + 1u) * ((t1y >> a.sb_shift) - (t0y >> a.sb_shift) + 1u);
-  a.dkeys_a[r] = ((unsigned long long)f2u(depthNdc) << 32) | r;
+  const uint32_t nsb = ((t1x >> a.sb_shift) - (t0x >> a.sb_shift) + 1u) * ((t1y >> a.sb_shift) - (t0y >> a.sb_shift) + 1u);
+  a.nsb[r] = nsb;
+  // the superblock count (<= 9) rides in bits 24-31 of the key's sortRank word,
+  // so the depth order carries it to the superblock scan without a gather
+  a.dkeys_a[r] = ((unsigned long long)f2u(depthNdc) << 32) | ((unsigned long long)nsb << 24) | r;
 }
 
 // Tile counts: each visible splat adds +1 over its tile box to a 2D
@@ -464,33 +467,6 @@ __global__ void __launch_bounds__(256) k_depth_range(FrameArgs a) {
   }
 }
 
-// Superblock lists: splat i of the depth order writes one entry per
-// superblock its tile box touches, superblock << 36 | local rect << 24 |
-// sortRank, at the prefix offsets of the superblock counts in depth order.
-__global__ void __launch_bounds__(256) k_emit_sb(FrameArgs a) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.N) return;
-  if (a.ctl[kCtlFlags] & 0x1u) return;
-  const uint32_t r = checked_rank(a.order[i], a.N, a.ctl);
-  const uint32_t box = a.aux[r].x;
-  if (box == kSentinel) return;
-  const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
-  uint32_t o = a.sb_off[i];
-  for (uint32_t sy = y0 >> kSbShift; sy <= y1 >> kSbShift; ++sy) {
-    const uint32_t by = sy << kSbShift;
-    const uint32_t ly0 = y0 > by ? y0 - by : 0u, ly1 = y1 - by < 7u ? y1 - by : 7u;
-    for (uint32_t sx = x0 >> kSbShift; sx <= x1 >> kSbShift; ++sx) {
-      const uint32_t bx = sx << kSbShift;
-      const uint32_t lx0 = x0 > bx ? x0 - bx : 0u, lx1 = x1 - bx < 7u ? x1 - bx : 7u;
-      const uint32_t rect = lx0 | (lx1 << 3) | (ly0 << 6) | (ly1 << 9);
-      if (o < a.sb_cap)
-        a.sbk_a[o] = ((unsigned long long)(sy * a.sb_cols + sx) << kSbKeyShift) |
-                     ((unsigned long long)rect << 24) | r;
-      ++o;
-    }
-  }
-}
-
 }  // namespace
 
 cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s) {
@@ -537,11 +513,6 @@ cudaError_t launch_tile_counts(const FrameArgs& a, cudaStream_t s) {
 
 cudaError_t launch_depth_range(const FrameArgs& a, cudaStream_t s) {
   if (a.N) k_depth_range<<<(a.N + 255) / 256, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_emit_sb(const FrameArgs& a, cudaStream_t s) {
-  if (a.N) k_emit_sb<<<(a.N + 255) / 256, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

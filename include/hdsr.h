@@ -184,7 +184,8 @@ typedef enum hdsr_buffer_id {
   HDSR_BUF_TILE_ENTRIES = 7,  /* u32[P] sortRank per entry, final per-tile order */
   HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] per final entry: tile<<(20+R) | k20<<R | sortRank */
   HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat superblock counts, depth order */
-  HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] sortRanks in ascending (depth bits, sortRank) */
+  HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] ascending (depth bits, sortRank): sortRank in bits 0-23,
+                                 the splat's superblock count in bits 24-31 */
 } hdsr_buffer_id;
 
 /* Device address and byte size of an internal buffer (valid until destroy). */
