@@ -1,4 +1,4 @@
-// hdsr_project.cu — frame init, projection, tile counting and key emission.
+// hdsr_project.cu — frame init, projection and tile counting.
 //
 // k_project follows gpu_project_splats.wgsl:112-358 step by step (one thread
 // per sortRank) and writes the reference's 14-word projection cache as four
@@ -8,11 +8,11 @@
 // from a 2D difference grid: each splat adds its tile box with four
 // additions, a 2D prefix sum gives every tile's count; a second grid at
 // superblock (8x8 tiles) granularity gives the length of every superblock's
-// list and so the lists' starts and their 256-entry segments. k_emit_sb
-// lists each splat, in ascending (depth, sortRank) order, once per
-// superblock it touches, with its tile box clipped to the superblock; the
-// lists replace scatter_tile_refs and the cooperative large-splat scatter
-// (gpu_large_splat_scatter.wgsl). When the 20-bit log-depth keys are
+// list and so the lists' starts and their 256-entry segments. The
+// superblock scan (hdsr_scan.cu) lists each splat, in ascending (depth,
+// sortRank) order, once per superblock it touches, with its tile box clipped
+// to the superblock; the lists replace scatter_tile_refs and the cooperative
+// large-splat scatter (gpu_large_splat_scatter.wgsl). When the 20-bit log-depth keys are
 // requested, k_depth_range keeps the per-tile depth min/max of the hot-tile
 // bucket mapping (gpu_tile_bucket_sort.wgsl:232-237).
 #include "hdsr_internal.cuh"
