@@ -16,7 +16,8 @@ e2e     the same frames/s through the C ABI with host buffers: every step
         frame and copies the four output images back.
 --impl reference  times the reference's CPU path restated in C (the oracle;
         the reference itself is TypeScript/WGSL and cannot run here) on the
-        same workload with all host threads, one full frame per step.
+        same workload with all host threads, one full frame per step, stopping
+        after 120 s of frames (steps_run says how many ran).
 N > 1   runs N independent replicas (one per GPU); value = frames of all ranks
         / the slowest rank's time.
 """
@@ -40,6 +41,7 @@ sys.path.insert(0, str(ROOT))
 import __graft_entry__  # noqa: E402
 
 METRIC = "760k-splat 1080p frames/s"
+REFERENCE_TIME_CAP_S = 120.0
 UNIT = "frames/s"
 
 
@@ -70,7 +72,10 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons, sampled every 50 ms from before the
+    warm-up until after the timed loop; summary(t0, t1) keeps the samples that
+    arrived during the timed region [t0, t1] (host clock), or, when the region
+    is shorter than the sampling interval, the first sample after t0."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -84,7 +89,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -96,7 +101,7 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
 
     def __exit__(self, *exc):
         if self.proc:
@@ -106,8 +111,13 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self) -> dict:
-        if not self.rows:
+    def summary(self, t0: float | None = None, t1: float | None = None) -> dict:
+        rows = [r for t, r in self.rows if t0 is None or t0 <= t <= t1]
+        window = "timed region"
+        if not rows and t0 is not None:
+            after = [r for t, r in self.rows if t >= t0]
+            rows, window = after[:1], "first sample after the timed region began"
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
 
         def num(x):
@@ -116,12 +126,12 @@ class ClockSampler:
             except ValueError:
                 return None
 
-        sm = [num(r[1]) for r in self.rows if num(r[1]) is not None]
-        mx = [num(r[2]) for r in self.rows if num(r[2]) is not None]
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "window": window}
 
 
 def setup_frame(pkg, wl, device_index=0):
@@ -395,6 +405,7 @@ def run_ours(args, rank, world, local):
     def frame():
         pkg.encode_full_compute_compositor_pipeline(stream, res)
 
+    clocks = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
         frame()
     torch.cuda.synchronize()
@@ -403,16 +414,19 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     launches0 = res.launch_count()
     times = []
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
-            flush.zero_()
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s.record(stream)
-            frame()
-            e.record(stream)
-            e.synchronize()
-            times.append(s.elapsed_time(e))
-        torch.cuda.synchronize()
+    t_begin = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        frame()
+        e.record(stream)
+        e.synchronize()
+        times.append(s.elapsed_time(e))
+    torch.cuda.synchronize()
+    t_end = time.perf_counter()
+    time.sleep(0.15)  # let the sample taken during the region arrive
+    clocks.__exit__(None, None, None)
     launches = res.launch_count() - launches0
     st = res.check_frame()
     # per-pass times: the same frames again with profiling events (one stream)
@@ -472,7 +486,7 @@ def run_ours(args, rank, world, local):
         "e2e": e2e, "gpu_launches": int(launches),
         "passes_ms": {k: round(v, 4) for k, v in mean_pass.items()},
         "pass_share": {k: round(v / frame_ms, 4) for k, v in mean_pass.items()},
-        "roofline": roofline, "clocks": clocks.summary(),
+        "roofline": roofline, "clocks": clocks.summary(t_begin, t_end),
         "gpu_back_to_front_sort_ms": round(sort_ms, 4),
     }
     if rank == 0 and not args.no_deferred:
@@ -711,21 +725,28 @@ def run_reference(args, rank, world):
     order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
     f = oracle.render_frame(u, packed, order, threads=threads, composite=False)
     cap = f["total_pairs"] + 16
-    for _ in range(args.warmup):
-        oracle.render_frame(u, packed, order, threads=threads, cap=cap)
+    oracle.render_frame(u, packed, order, threads=threads, cap=cap)  # warm (page-in); more would not change it
+    # a step is one full frame; the run stops after REFERENCE_TIME_CAP_S so
+    # that any --steps finishes within a few minutes
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    done = 0
+    while done < args.steps:
         oracle.render_frame(u, packed, order, threads=threads, cap=cap)
+        done += 1
+        if time.perf_counter() - t0 > REFERENCE_TIME_CAP_S:
+            break
     dt = time.perf_counter() - t0
-    value = args.steps / dt
+    value = done / dt
     out = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": round(dt * 1000.0 / args.steps, 2), "higher_is_better": True,
+           "steps_run": done, "warmup": args.warmup, "ms_per_step": round(dt * 1000.0 / done, 2),
+           "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
            "impl": "reference", "config": {**wl.describe(), "pairs": int(f["total_pairs"])},
            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"one full frame of {wl.name} per step through the oracle (C restatement "
-                                      f"of the reference's WGSL passes; the TypeScript/WebGPU original cannot "
-                                      f"run on this machine)"},
+                            "sample": f"{done} full frames of {wl.name} (one per step, at most "
+                                      f"{REFERENCE_TIME_CAP_S:.0f} s) through the oracle (C restatement of the "
+                                      f"reference's WGSL passes; the TypeScript/WebGPU original cannot run on "
+                                      f"this machine)"},
            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -733,7 +754,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hot760k")
