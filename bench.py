@@ -184,6 +184,9 @@ def pass_bytes(name: str, N: int, P: int, Q: int, S: int, sh_floats: int) -> flo
     if name == "tile_entries":
         # count and scatter read the Q keys; segment tables 3x; P entries out
         return Q * 16 + S * 256 * 3 + P * 4
+    if name == "chunk_masks":
+        # the Q sorted list keys in, one 8-byte tile mask per 32 keys out
+        return Q * 8 + (Q + 31) // 32 * 8
     return None
 
 

@@ -35,6 +35,7 @@ COLOR_RGBA32F = 1
 CFG_KEEP_SORTED_KEYS = 0x1
 CFG_NO_GRAPH = 0x2
 CFG_BACKWARD = 0x4
+CFG_TILE_ENTRIES = 0x8
 
 DEV_OVERFLOW = 0x1
 DEV_TIMEOUT = 0x2

@@ -70,10 +70,11 @@ class TileSplatCompositorResources:
     """Owner of one compositor handle (and of every internal device buffer)."""
 
     def __init__(self, plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,
-                 keep_sorted_keys: bool = False, backward: bool = False):
+                 keep_sorted_keys: bool = False, backward: bool = False, tile_entries: bool = False):
         self.plan = plan
         self._lib = _lib.load()
-        flags = (_lib.CFG_KEEP_SORTED_KEYS if keep_sorted_keys else 0) | (_lib.CFG_BACKWARD if backward else 0)
+        flags = ((_lib.CFG_KEEP_SORTED_KEYS if keep_sorted_keys else 0) | (_lib.CFG_BACKWARD if backward else 0)
+                 | (_lib.CFG_TILE_ENTRIES if tile_entries else 0))
         cfg = _lib.Config(int(pair_capacity), _lib.COLOR_RGBA32F if f32_color else _lib.COLOR_RGBA16F, flags)
         handle = ctypes.c_void_p()
         status = self._lib.hdsr_create_tile_splat_compositor(ctypes.byref(plan._c()), ctypes.byref(cfg),
@@ -82,11 +83,12 @@ class TileSplatCompositorResources:
         self.handle = handle
         self.f32_color = f32_color
         self.bind_groups = None
+        # no frame yet: the lookup builds nothing
+        self._pair_capacity = self.buffer_address("tile_entries")[1] // 4
 
     @property
     def pair_capacity(self) -> int:
-        _, size = self.buffer_address("tile_entries")
-        return size // 4
+        return self._pair_capacity
 
     def destroy(self) -> None:
         if self.handle:
@@ -168,8 +170,9 @@ class _DeviceView:
 
 
 def create_tile_splat_compositor(plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,
-                                 keep_sorted_keys: bool = False, backward: bool = False) -> TileSplatCompositorResources:
-    return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys, backward)
+                                 keep_sorted_keys: bool = False, backward: bool = False,
+                                 tile_entries: bool = False) -> TileSplatCompositorResources:
+    return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys, backward, tile_entries)
 
 
 def sort_back_to_front(stream, resources: TileSplatCompositorResources, view, out) -> None:

@@ -20,7 +20,7 @@ namespace {
 constexpr uint32_t kMaxProfiledPasses = 24;
 // names of the profiled passes, indexed by the ids recorded in encode()
 const char* const kPassNames[] = {"upload_uniforms", "frame_init", "project", "tile_counts", "unused_4",
-                                  "scan_tiles", "depth_sort", "superblock_lists", "tile_entries", "unused_9",
+                                  "scan_tiles", "depth_sort", "superblock_lists", "tile_entries", "chunk_masks",
                                   "unused_10", "unused_11", "unused_12", "unused_13", "unused_14",
                                   "unused_15", "unused_16", "raster"};
 constexpr uint32_t kNumPassNames = sizeof(kPassNames) / sizeof(kPassNames[0]);
@@ -40,6 +40,7 @@ struct hdsr_compositor {
   bool scene_bound = false;
   bool outputs_bound = false;
   bool sorted_valid = false;
+  bool entries_valid = false;      // a.entries holds the last full frame's per-tile lists
   cudaStream_t last_stream = nullptr;
   bool has_last_stream = false;
   uint64_t launches = 0;           // kernels queued by this handle
@@ -208,6 +209,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.sb_start, (uint64_t)a.num_sb + 1u, "superblock_starts");
   ALLOC(a.seg_first, (uint64_t)a.num_sb + 1u, "segment_firsts");
   ALLOC(a.seg_cnt, (uint64_t)a.seg_cap * kSbTiles, "segment_counts");
+  ALLOC(a.chunk_mask, sb_cap / kChunkEntries + 1u, "chunk_masks");
   ALLOC(a.tile_cnt, M, "tile_counts");
   ALLOC(a.tile_dmin, M, "tile_dmin");
   ALLOC(a.tile_dmax, M, "tile_dmax");
@@ -389,6 +391,12 @@ static void mark(hdsr_compositor* h, cudaStream_t s, uint32_t id) {
   cudaEventRecord(h->ev[++h->ev_used], s);
 }
 
+// Does every full frame write the per-tile lists? (The 20-bit log-depth keys
+// are computed from them.)
+static bool entries_each_frame(const hdsr_compositor* h) {
+  return (h->cfg.flags & (HDSR_CFG_TILE_ENTRIES | HDSR_CFG_KEEP_SORTED_KEYS)) != 0u;
+}
+
 static hdsr_status encode_checks(hdsr_compositor* h, bool full) {
   if (!h) return HDSR_ERR_INVALID_ARG;
   if (!h->scene_bound || !h->outputs_bound) return fail(h, HDSR_ERR_NOT_BOUND, "bind scene and outputs first");
@@ -459,14 +467,19 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
       return cuda_fail(h, e, "superblock_sort");
   }
   mark(h, s, 7);
-  if ((e = launch_tile_entries(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_entries");
-  mark(h, s, 8);
+  if ((e = launch_chunk_masks(a, s)) != cudaSuccess) return cuda_fail(h, e, "chunk_masks");
+  mark(h, s, 9);
+  if (entries_each_frame(h)) {
+    if ((e = launch_tile_entries(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_entries");
+    mark(h, s, 8);
+    if (a.tile_count) h->launches += 3;
+  }
   if (a.log_keys) {
     if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
     h->launches += 2;
   }
   h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 3 * kDepthPasses + 1 +
-                 3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 3 : 0);
+                 3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 1 : 0);
   return HDSR_OK;
 }
 
@@ -484,7 +497,21 @@ static hdsr_status encode_raster(hdsr_compositor* h, cudaStream_t s, bool full) 
   if (a.tile_count) h->launches += 1;
   h->last_stream = s;
   h->has_last_stream = true;
-  if (full) h->sorted_valid = true;
+  if (full) {
+    h->sorted_valid = true;
+    h->entries_valid = entries_each_frame(h);
+  }
+  return HDSR_OK;
+}
+
+// The per-tile lists of the last full frame, queued on `s` unless the frame
+// wrote them (the superblock lists they come from stay until the next frame).
+static hdsr_status ensure_entries(hdsr_compositor* h, cudaStream_t s) {
+  if (h->entries_valid || !h->sorted_valid) return HDSR_OK;
+  cudaError_t e = launch_tile_entries(h->args, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "tile_entries");
+  if (h->args.tile_count) h->launches += 3;
+  h->entries_valid = true;
   return HDSR_OK;
 }
 
@@ -563,6 +590,8 @@ hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* g, v
   b.d_rot = g->d_rotations;
   b.d_opa = g->d_opacities;
   b.d_sh = g->d_sh;
+  hdsr_status es = ensure_entries(h, s);
+  if (es != HDSR_OK) return es;
   if ((e = launch_backward(b, s)) != cudaSuccess) return cuda_fail(h, e, "backward");
   h->launches += (a.N ? 2 : 0) + (a.tile_count ? 1 : 0);
   return HDSR_OK;
@@ -614,7 +643,14 @@ hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, u
     case HDSR_BUF_DEPTH: *ptr = a.depth; *bytes = N * 4; break;
     case HDSR_BUF_TILE_COUNTS: *ptr = a.tile_cnt; *bytes = M * 4; break;
     case HDSR_BUF_TILE_OFFSETS: *ptr = a.tile_off; *bytes = M * 4; break;
-    case HDSR_BUF_TILE_ENTRIES: *ptr = a.entries; *bytes = cap * 4; break;
+    case HDSR_BUF_TILE_ENTRIES:
+      if (!h->entries_valid && h->sorted_valid && h->has_last_stream) {
+        hdsr_status es = ensure_entries(h, h->last_stream);
+        if (es != HDSR_OK) return es;
+        cudaError_t e = cudaStreamSynchronize(h->last_stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+      }
+      *ptr = a.entries; *bytes = cap * 4; break;
     case HDSR_BUF_SORTED_KEYS:
       if (!a.sorted_keys) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_KEEP_SORTED_KEYS");
       *ptr = a.sorted_keys; *bytes = cap * 8; break;

@@ -41,6 +41,19 @@ constexpr uint32_t kSbShift = 3;
 constexpr uint32_t kSbTiles = 64;
 constexpr uint32_t kSbKeyShift = 36;
 constexpr uint32_t kSegEntries = 256;            // list entries per segment
+constexpr uint32_t kChunkEntries = 32;           // list entries per chunk mask
+
+// Local rect of a superblock list entry: x0 | x1 << 3 | y0 << 6 | y1 << 9.
+HDSR_HD uint32_t local_rect(unsigned long long k) { return (uint32_t)(k >> 24) & 0xFFFu; }
+
+// The superblock tiles a local rect covers: bit y * 8 + x.
+HDSR_HD unsigned long long rect_tiles(uint32_t rc) {
+  const uint32_t x0 = rc & 7u, x1 = (rc >> 3) & 7u, y0 = (rc >> 6) & 7u, y1 = rc >> 9;
+  const unsigned long long row = (unsigned long long)(((2u << x1) - (1u << x0)) & 0xFFu);
+  const unsigned long long rows_hi = y1 == 7u ? ~0ull : (1ull << (8u * y1 + 8u)) - 1ull;
+  const unsigned long long rows_lo = ~((1ull << (8u * y0)) - 1ull);
+  return row * 0x0101010101010101ull & rows_hi & rows_lo;
+}
 constexpr uint32_t kMaxSuperblocks = 1024;       // 255 tiles a side -> <= 32 x 32
 
 // One LSD radix pass over u64 keys: digit = (key >> shift) & (2^bits - 1).
@@ -104,6 +117,7 @@ struct FrameArgs {
   uint32_t* sb_start;             // num_sb + 1: first entry of each superblock's list
   uint32_t* seg_first;            // num_sb + 1: first segment of each superblock's list
   uint32_t* seg_cnt;              // kSbTiles per segment: tile counts, then entry bases
+  unsigned long long* chunk_mask; // per 32-entry chunk of sbk_sorted: the local tiles its entries cover
   // tiles
   uint32_t* tile_cnt;
   uint32_t* tile_dmin;
@@ -176,6 +190,7 @@ cudaError_t launch_depth_range(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
+cudaError_t launch_chunk_masks(const FrameArgs& a, cudaStream_t s);   // 1 launch
 cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 3 launches
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 // back-to-front order of the bound positions for a view matrix (row 2 of the

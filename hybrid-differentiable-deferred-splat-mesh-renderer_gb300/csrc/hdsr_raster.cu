@@ -7,13 +7,13 @@
 // only when power > -4, alpha > 1/255 and T >= 0.001; G-buffer votes are
 // gated at weight > 0.01; a quad stops once all four T < 0.001.
 //
-// GB300 layout: one warp owns a 16x16 tile, each lane two 2x2 quads
-// (rows 0-7 and 8-15 of the tile), composited in two passes over the tile's
-// entries so that only one quad's accumulators are live (about half the
-// registers, twice the resident warps) and each half stops on its own. Splat
-// batches of 32 entries are gathered from the SoA projection cache (one entry
-// per lane, 16-byte loads) into the warp's shared-memory slab and read as
-// broadcasts. Warps take tiles from an atomic counter. FP32 transmittance.
+// GB300 layout: a warp owns half a tile (16x8 pixels, one 2x2 quad per
+// lane), taken from an atomic counter, so that each half stops on its own. It
+// reads the tile's entries straight from its superblock's depth-ordered list
+// (no per-tile list is written on the frame path; see k_raster), culls them
+// against the half tile, gathers the kept ones from the SoA projection cache
+// (one entry per lane, 16-byte loads) into the warp's shared-memory slab and
+// reads them as broadcasts. FP32 transmittance.
 // Arithmetic is the canonical form: power = fma(c' dy, dy, fma(b' dx, dy,
 // (a' dx) dx)) and every "acc += v * w" is fma(v, w, acc).
 #include "hdsr_internal.cuh"
@@ -179,15 +179,14 @@ __device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, ui
   }
 }
 
-// One entry's cache row, as loaded (prefetched a batch ahead).
+// One entry's cache row, as loaded (prefetched a chunk ahead).
 struct Row {
   float4 g;
   uint4 ap, gb;
   uint32_t conf, depth;
 };
 
-__device__ __forceinline__ Row load_row(const FrameArgs& a, uint32_t e) {
-  const uint32_t r = checked_rank(__ldg(a.entries + e), a.N, a.ctl);
+__device__ __forceinline__ Row load_row(const FrameArgs& a, uint32_t r) {
   Row w;
   w.g = __ldg(a.geo + r);
   w.ap = __ldg(a.app + r);
@@ -250,12 +249,36 @@ __device__ __forceinline__ bool touches_rect(float cx, float cy, float ia, float
 #define HDSR_RASTER_MIN_BLOCKS 4
 #endif
 
+// A list entry whose rect covers no tile (x0 = 7 > x1 = 0).
+constexpr unsigned long long kNoKey = 7ull << 24;
+constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
+
+__device__ __forceinline__ bool rect_covers(unsigned long long k, uint32_t lx, uint32_t ly) {
+  const uint32_t rc = local_rect(k);
+  return lx >= (rc & 7u) && lx <= ((rc >> 3) & 7u) && ly >= ((rc >> 6) & 7u) && ly <= (rc >> 9);
+}
+
+// Covering entries waiting to be composited, per warp (a ring of sortRanks).
+constexpr uint32_t kQueue = 256;
+constexpr uint32_t kChunksPerFill = 4;
+
 // Work unit: half a tile (rows 0-7 or 8-15), taken from an atomic counter.
+// The tile's entries, in order, are the entries of its superblock's list
+// (ascending (depth bits, sortRank)) whose local rect covers the tile: the
+// same sequence the per-tile lists hold. The warp visits only the list's
+// 32-entry chunks whose mask holds the tile (mask windows of 32 chunks, one
+// ballot each), four chunks per fill with their keys loaded together, and
+// appends the covering entries' sortRanks to its queue in order. Batches of
+// up to 32 queued entries are then composited as from a per-tile list: each
+// lane gathers one cache row, the rows of the next batch in flight while the
+// current one is composited.
 __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(FrameArgs a) {
   __shared__ float4 s_pay[kWarps][32][kRows];
+  __shared__ uint32_t s_queue[kWarps][kQueue];
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   float4 (*s)[kRows] = s_pay[warp];
+  uint32_t* queue = s_queue[warp];
   const uint32_t items = 2u * a.tile_count;
   for (;;) {
     uint32_t item = 0;
@@ -264,8 +287,9 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
     if (item >= items) break;
     const uint32_t tile_idx = item >> 1, half = item & 1u;
     const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
-    const uint32_t t = morton(tx, ty);
-    const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
+    const uint32_t sb = (ty >> kSbShift) * a.sb_cols + (tx >> kSbShift);
+    const uint32_t lx = tx & 7u, ly = ty & 7u, tbit = ly * 8u + lx;
+    const uint32_t beg = a.sb_start[sb], end = a.sb_start[sb + 1u];
     const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
     const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
     const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
@@ -274,22 +298,66 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
     const uint32_t lt = (1u << lane) - 1u;
     Quad q;
     quad_init(q);
-    Row next;
-    if (lane < count) next = load_row(a, start + lane);
-    for (uint32_t b = 0; b < count; b += 32u) {
-      const uint32_t n = count - b < 32u ? count - b : 32u;
-      // keep, in order, the batch's entries that can reach this half tile
-      const bool keep = lane < n && touches_rect(next.g.x, next.g.y, next.g.z, next.g.w, u2f(next.ap.x),
-                                                 hi16(next.ap.y), rx0, rx0 + 15.0f, ry0, ry0 + 7.0f);
-      const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
-      if (keep) stage_row(s, next, __popc(kept & lt));
+    // chunk iterator over [beg, end) and the queue (head: next to composite)
+    uint32_t wnext = beg / kChunkEntries, wbase = 0u, want = 0u, head = 0u, tail = 0u;
+    const uint32_t clast = beg < end ? (end - 1u) / kChunkEntries : 0u;
+    bool more = beg < end;
+    // the next chunk (ascending) whose mask holds the tile, or kNoChunk
+    auto next_chunk = [&]() -> uint32_t {
+      while (want == 0u) {
+        if (wnext > clast) return kNoChunk;
+        const uint32_t c = wnext + lane;
+        const bool has = c <= clast && ((__ldg(a.chunk_mask + c) >> tbit) & 1ull) != 0ull;
+        want = __ballot_sync(0xFFFFFFFFu, has);
+        wbase = wnext;
+        wnext += 32u;
+      }
+      const uint32_t c = wbase + (uint32_t)(__ffs(want) - 1);
+      want &= want - 1u;
+      return c;
+    };
+    // append the covering entries of up to kChunksPerFill chunks, in order
+    auto fill = [&]() {
+      unsigned long long k[kChunksPerFill];
+#pragma unroll
+      for (uint32_t j = 0; j < kChunksPerFill; ++j) {
+        const uint32_t c = more ? next_chunk() : kNoChunk;
+        more = c != kNoChunk;
+        const uint32_t i = c * kChunkEntries + lane;
+        k[j] = more && i >= beg && i < end ? __ldg(a.sbk_sorted + i) : kNoKey;
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < kChunksPerFill; ++j) {
+        const bool in = rect_covers(k[j], lx, ly);
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+        if (in) queue[(tail + __popc(m & lt)) & (kQueue - 1u)] = (uint32_t)k[j] & 0xFFFFFFu;
+        tail += __popc(m);
+      }
       __syncwarp();
-      if (b + 32u + lane < count) next = load_row(a, start + b + 32u + lane);  // in flight during the batch
+    };
+    while (more && tail - head < 32u) fill();
+    uint32_t n = tail - head < 32u ? tail - head : 32u;
+    Row cur;
+    if (lane < n) cur = load_row(a, checked_rank(queue[(head + lane) & (kQueue - 1u)], a.N, a.ctl));
+    head += n;
+    while (n > 0u) {
+      // keep, in order, the batch's entries that can reach this half tile
+      const bool keep = lane < n && touches_rect(cur.g.x, cur.g.y, cur.g.z, cur.g.w, u2f(cur.ap.x), hi16(cur.ap.y),
+                                                 rx0, rx0 + 15.0f, ry0, ry0 + 7.0f);
+      const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
+      if (keep) stage_row(s, cur, __popc(kept & lt));
+      // the next batch: its rows in flight while this one is composited
+      while (more && tail - head < 32u) fill();
+      const uint32_t n2 = tail - head < 32u ? tail - head : 32u;
+      if (lane < n2) cur = load_row(a, checked_rank(queue[(head + lane) & (kQueue - 1u)], a.N, a.ctl));
+      head += n2;
+      __syncwarp();
       const uint32_t nk = __popc(kept);
       for (uint32_t i = 0; i < nk; ++i)
         if (!q.done) quad_splat(q, p00x, p00y, s, (int)i);
       __syncwarp();
       if (__all_sync(0xFFFFFFFFu, q.done)) break;
+      n = n2;
     }
     quad_store(a, q, bx, by);
   }

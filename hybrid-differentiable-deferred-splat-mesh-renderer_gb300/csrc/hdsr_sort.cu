@@ -270,8 +270,6 @@ __device__ __forceinline__ void seg_locate(const FrameArgs& a, const SegTables& 
   end = lim - beg < kSegEntries ? lim : beg + kSegEntries;
 }
 
-__device__ __forceinline__ uint32_t local_rect(unsigned long long k) { return (uint32_t)(k >> 24) & 0xFFFu; }
-
 __global__ void __launch_bounds__(256) k_seg_count(FrameArgs a) {
   constexpr uint32_t kGrid = 9u * 9u;
   __shared__ int s_diff[8][kGrid + 3u];
@@ -477,6 +475,33 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
   k_radix_colscan<<<1u << j.bits, 256, 0, s>>>(j);
   if (last) k_radix_downsweep<true><<<grid_last, kRadixThreads, smem, s>>>(j);
   else k_radix_downsweep<false><<<grid_mid, kRadixThreads, smem, s>>>(j);
+  return cudaGetLastError();
+}
+
+// Chunk masks: for every 32-entry chunk of the sorted superblock lists, the
+// union of its entries' local rects (bit y * 8 + x of the superblock). The
+// rasteriser walks a tile's superblock list and reads only the chunks whose
+// mask holds the tile. A chunk that straddles two superblocks' lists carries
+// the union over both: a reader then visits a chunk that may hold none of its
+// tile's entries, which costs time only.
+__global__ void __launch_bounds__(256) k_chunk_masks(FrameArgs a) {
+  if (a.ctl[kCtlFlags] & 0x1u) return;
+  const uint32_t Q = a.ctl[kCtlSbPairs];
+  const uint32_t chunks = (Q + kChunkEntries - 1u) / kChunkEntries;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < chunks; c += nw) {
+    const uint32_t i = c * kChunkEntries + lane;
+    const unsigned long long m = i < Q ? rect_tiles(local_rect(__ldg(a.sbk_sorted + i))) : 0ull;
+    const uint32_t lo = __reduce_or_sync(0xFFFFFFFFu, (uint32_t)m);
+    const uint32_t hi = __reduce_or_sync(0xFFFFFFFFu, (uint32_t)(m >> 32));
+    if (lane == 0u) a.chunk_mask[c] = (unsigned long long)hi << 32 | lo;
+  }
+}
+
+cudaError_t launch_chunk_masks(const FrameArgs& a, cudaStream_t s) {
+  if (!a.tile_count) return cudaSuccess;
+  k_chunk_masks<<<a.num_sms * 8, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -72,6 +72,8 @@ typedef struct hdsr_plan {
 #define HDSR_CFG_KEEP_SORTED_KEYS 0x1u  /* compute the 20-bit log-depth keys per entry */
 #define HDSR_CFG_NO_GRAPH         0x2u  /* reserved: kernels are always launched directly */
 #define HDSR_CFG_BACKWARD         0x4u  /* allocate the adjoint's buffers (hdsr_encode_backward) */
+#define HDSR_CFG_TILE_ENTRIES     0x8u  /* write the per-tile entry lists in every full frame
+                                           (otherwise built on demand: see HDSR_BUF_TILE_ENTRIES) */
 
 /* Options of createTileSplatCompositor — gpuTileSplatCompositor.ts:141-145
  * ({f16?}); the f16 composite variant is not rebuilt (FP32 transmittance). */
@@ -181,14 +183,20 @@ typedef enum hdsr_buffer_id {
   HDSR_BUF_DEPTH = 4,         /* u32[N]: f32 NDC depth bits */
   HDSR_BUF_TILE_COUNTS = 5,   /* u32[M] */
   HDSR_BUF_TILE_OFFSETS = 6,  /* u32[M] exclusive prefix of tile counts */
-  HDSR_BUF_TILE_ENTRIES = 7,  /* u32[P] sortRank per entry, final per-tile order */
+  HDSR_BUF_TILE_ENTRIES = 7,  /* u32[P] sortRank per entry, final per-tile order. The rasteriser
+                                 reads the superblock lists, so a frame writes these lists only
+                                 with HDSR_CFG_TILE_ENTRIES or HDSR_CFG_KEEP_SORTED_KEYS; else
+                                 hdsr_get_buffer builds them for the last full frame on the
+                                 handle's last stream and synchronizes that stream, and
+                                 hdsr_encode_backward builds them on its own stream. */
   HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] per final entry: tile<<(20+R) | k20<<R | sortRank */
   HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat superblock counts, depth order */
   HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] ascending (depth bits, sortRank): sortRank in bits 0-23,
                                  the splat's superblock count in bits 24-31 */
 } hdsr_buffer_id;
 
-/* Device address and byte size of an internal buffer (valid until destroy). */
+/* Device address and byte size of an internal buffer (valid until destroy).
+ * HDSR_BUF_TILE_ENTRIES may first build the per-tile lists (see above). */
 hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** device_ptr,
                             uint64_t* bytes);
 

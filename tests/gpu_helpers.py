@@ -12,7 +12,7 @@ def u32(t):
 
 
 def render_gpu(pkg, scene, cam, W, H, *, f32_color=False, keep_keys=True, pair_capacity=0, order=None,
-               sh_degree=None):
+               sh_degree=None, tile_entries=False):
     import torch
 
     packed = pkg.splats.pack_splat_attributes(scene)
@@ -22,7 +22,7 @@ def render_gpu(pkg, scene, cam, W, H, *, f32_color=False, keep_keys=True, pair_c
     if order is None:
         order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
     res = pkg.create_tile_splat_compositor(plan, pair_capacity=pair_capacity, f32_color=f32_color,
-                                           keep_sorted_keys=keep_keys)
+                                           keep_sorted_keys=keep_keys, tile_entries=tile_entries)
     bufs = pkg.splats.upload_splat_attribute_buffers(packed, order)
     color, gb = pkg.create_output_textures(plan, f32_color=f32_color)
     pkg.create_tile_splat_bind_groups(res, bufs, color, gb)

@@ -210,6 +210,31 @@ def test_composite_only_and_determinism(cuda, pkg, orc):
         assert np.array_equal(third[k], first[k]), k
 
 
+def test_tile_entries_on_demand(cuda, pkg, orc):
+    # The rasteriser reads the superblock lists, so without
+    # HDSR_CFG_TILE_ENTRIES / KEEP_SORTED_KEYS a frame writes no per-tile
+    # lists: the readback builds them once (3 launches), bit-exact, and the
+    # image equals that of a handle that writes them every frame.
+    wl = pkg.workloads.plain50k()
+    lazy = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height, keep_keys=False)
+    eager = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height, keep_keys=False, tile_entries=True)
+    n0 = lazy["res"].launch_count()
+    gpu = read_gpu(lazy)
+    assert lazy["res"].launch_count() == n0 + 3
+    assert_frame_parity(orc, lazy, gpu=gpu)
+    again = read_gpu(lazy)
+    assert lazy["res"].launch_count() == n0 + 3
+    assert np.array_equal(again["tile_entries"], gpu["tile_entries"])
+    n1 = eager["res"].launch_count()
+    ref = read_gpu(eager)
+    assert eager["res"].launch_count() == n1
+    for k in ("tile_entries", "normal", "material"):
+        assert np.array_equal(ref[k], gpu[k]), k
+    assert np.array_equal(ref["color"].view(np.uint16), gpu["color"].view(np.uint16))
+    lazy["res"].destroy()
+    eager["res"].destroy()
+
+
 def test_overflow_is_reported_not_faulted(cuda, pkg, orc):
     import torch
 

@@ -217,6 +217,80 @@ def test_keys20_order_matches_frame_tiles(small_frame, orc):
         assert np.array_equal(a, b)
 
 
+def _rect_tiles(rc: int) -> int:
+    """The device's tile mask of a superblock-local rect (rect_tiles in
+    hdsr_internal.cuh), formula for formula."""
+    x0, x1, y0, y1 = rc & 7, (rc >> 3) & 7, (rc >> 6) & 7, rc >> 9
+    row = ((2 << x1) - (1 << x0)) & 0xFF
+    hi = (1 << 64) - 1 if y1 == 7 else (1 << (8 * y1 + 8)) - 1
+    lo = ~((1 << (8 * y0)) - 1) & ((1 << 64) - 1)
+    return (row * 0x0101010101010101) & hi & lo & ((1 << 64) - 1)
+
+
+def test_rect_tile_mask_formula():
+    for rc in range(4096):
+        x0, x1, y0, y1 = rc & 7, (rc >> 3) & 7, (rc >> 6) & 7, rc >> 9
+        if x0 > x1 or y0 > y1:
+            continue
+        want = sum(1 << (y * 8 + x) for y in range(y0, y1 + 1) for x in range(x0, x1 + 1))
+        assert _rect_tiles(rc) == want, rc
+
+
+def _morton(x: int, y: int) -> int:
+    m = 0
+    for b in range(16):
+        m |= ((x >> b) & 1) << (2 * b) | ((y >> b) & 1) << (2 * b + 1)
+    return m
+
+
+def test_superblock_walk_yields_the_tile_lists(small_frame):
+    # The rasteriser reads a tile's entries from its superblock's list (8x8
+    # tiles: every visible splat in ascending (depth bits, sortRank) order,
+    # its tile box clipped to the superblock), keeping the entries whose rect
+    # covers the tile and visiting only the 32-entry chunks whose mask holds
+    # the tile. That walk must give the canonical per-tile list exactly.
+    f = small_frame["frame"]
+    box, depth = f["proj_cache"][:, 7], f["depth"]
+    cols, rows = (f["W"] + 15) // 16, (f["H"] + 15) // 16
+    sb_cols, sb_rows = (cols + 7) // 8, (rows + 7) // 8
+    vis = np.nonzero(box != 0xFFFFFFFF)[0]
+    order = vis[np.lexsort((vis, depth[vis]))]
+    lists = [[] for _ in range(sb_cols * sb_rows)]
+    for r in order:
+        b = int(box[r])
+        x0, y0, x1, y1 = b & 255, (b >> 8) & 255, (b >> 16) & 255, b >> 24
+        for sy in range(y0 >> 3, (y1 >> 3) + 1):
+            for sx in range(x0 >> 3, (x1 >> 3) + 1):
+                rc = (max(x0 - 8 * sx, 0) | min(x1 - 8 * sx, 7) << 3 | max(y0 - 8 * sy, 0) << 6
+                      | min(y1 - 8 * sy, 7) << 9)
+                lists[sy * sb_cols + sx].append((rc, int(r)))
+    flat = [e for lst in lists for e in lst]
+    starts = np.concatenate([[0], np.cumsum([len(lst) for lst in lists])]).astype(np.int64)
+    masks = [0] * ((len(flat) + 31) // 32)
+    for i, (rc, _) in enumerate(flat):
+        masks[i // 32] |= _rect_tiles(rc)
+    walked_chunks = skipped = 0
+    for ty in range(rows):
+        for tx in range(cols):
+            sb = (ty >> 3) * sb_cols + (tx >> 3)
+            bit = 1 << ((ty & 7) * 8 + (tx & 7))
+            beg, end = int(starts[sb]), int(starts[sb + 1])
+            got = []
+            for c in range(beg // 32, (end - 1) // 32 + 1 if end > beg else beg // 32):
+                if not masks[c] & bit:
+                    skipped += 1
+                    continue
+                walked_chunks += 1
+                for i in range(max(beg, 32 * c), min(end, 32 * c + 32)):
+                    rc, r = flat[i]
+                    if _rect_tiles(rc) & bit:
+                        got.append(r)
+            t = _morton(tx, ty)
+            o, n = int(f["tile_offsets"][t]), int(f["tile_counts"][t])
+            assert got == f["tile_entries"][o:o + n].tolist(), (tx, ty)
+    assert walked_chunks > 0 and skipped > 0
+
+
 def test_composite_close_to_fp64(small_frame, orc):
     f = small_frame["frame"]
     img = orc.f16_to_f32(f["color"].reshape(-1)).reshape(f["H"], f["W"], 4).astype(np.float64)
