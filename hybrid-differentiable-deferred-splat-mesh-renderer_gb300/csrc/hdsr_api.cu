@@ -590,8 +590,6 @@ hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* g, v
   b.d_rot = g->d_rotations;
   b.d_opa = g->d_opacities;
   b.d_sh = g->d_sh;
-  hdsr_status es = ensure_entries(h, s);
-  if (es != HDSR_OK) return es;
   if ((e = launch_backward(b, s)) != cudaSuccess) return cuda_fail(h, e, "backward");
   h->launches += (a.N ? 2 : 0) + (a.tile_count ? 1 : 0);
   return HDSR_OK;

@@ -10,7 +10,7 @@
 // Every threshold of the composite (power > -4, alpha > 1/255, T >= 0.001,
 // the 0.99 alpha cap) and every clamp of the projection (opacity, colour,
 // view depth, w) is held fixed: a clamped quantity passes no gradient. The
-// per-tile entry lists of the forward frame are reused.
+// forward frame's superblock lists are walked again (no per-tile lists).
 //   1. k_bwd_prep: per sortRank, the screen-space parameters of the adjoint
 //      (centre, conic, clamped opacity with the anti-aliasing factor, clamped
 //      SH colour); zeroes the screen-space accumulators.
@@ -43,50 +43,19 @@ constexpr int kBwdWarps = 4;
 //   row 2: b, ia, ib, ic        row 3: sortRank bits, 0, 0, 0
 constexpr int kBRows = 4;
 
-// Same test as the rasteriser's (hdsr_raster.cu): can the entry reach a
-// pixel centre of [x0, x1] x [y0, y1] with power > -4 and alpha > 1/255?
-__device__ __forceinline__ bool bwd_touches(float cx, float cy, float ia, float ib, float ic, float op, float x0,
-                                            float x1, float y0, float y1) {
-  const float xa = x0 - cx, xb = x1 - cx, ya = y0 - cy, yb = y1 - cy;
-  const float xm = fmaxf(fabsf(xa), fabsf(xb)), ym = fmaxf(fabsf(ya), fabsf(yb));
-  const float mag = 0.5f * ia * xm * xm + fabsf(ib) * xm * ym + 0.5f * ic * ym * ym;
-  const float margin = 1e-3f + 1e-5f * mag;
-  float best;
-  if (xa <= 0.0f && xb >= 0.0f && ya <= 0.0f && yb >= 0.0f) {
-    best = 0.0f;
-  } else {
-    float e = -3.4e38f;
-    const float xs[2] = {xa, xb}, ys[2] = {ya, yb};
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const float x = xs[k];
-      const float dy = fminf(fmaxf(-ib * x / ic, ya), yb);
-      e = fmaxf(e, -0.5f * ia * x * x - ib * x * dy - 0.5f * ic * dy * dy);
-      const float y = ys[k];
-      const float dx = fminf(fmaxf(-ib * y / ia, xa), xb);
-      e = fmaxf(e, -0.5f * ia * dx * dx - ib * dx * y - 0.5f * ic * y * y);
-    }
-    best = e;
-  }
-  const float lim = fmaxf(-4.0f, -__logf(255.0f * op));
-  return best > lim - margin - 1e-3f;
-}
-
-// Stages entry e into slot `slot` of the batch if it can reach the half tile
-// [x0, x0 + 15] x [y0, y0 + 7]; returns whether it was kept (warp-collective:
-// every lane calls it, lanes without an entry pass valid = false).
-__device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float4 (*s)[kBRows], uint32_t e, bool valid,
+// Stages the entry of sortRank r, in order, if it can reach the half tile
+// [x0, x0 + 15] x [y0, y0 + 7]; returns how many of the batch were kept
+// (warp-collective: every lane calls it, lanes without an entry pass
+// valid = false).
+__device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float4 (*s)[kBRows], uint32_t r, bool valid,
                                                    uint32_t lane, float x0, float y0) {
-  const FrameArgs& a = b.f;
   bool keep = false;
-  uint32_t r = 0;
   float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
   if (valid) {
-    r = checked_rank(__ldg(a.entries + e), a.N, a.ctl);
     p0 = b.par[(size_t)r * 3];
     p1 = b.par[(size_t)r * 3 + 1];
     p2 = b.par[(size_t)r * 3 + 2];
-    keep = bwd_touches(p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, x0, x0 + 15.0f, y0, y0 + 7.0f);
+    keep = reaches_rect(p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, x0, x0 + 15.0f, y0, y0 + 7.0f);
   }
   const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
   if (keep) {
@@ -124,6 +93,7 @@ __device__ __forceinline__ uint32_t warp_sum9(const float (&g)[9], uint32_t lane
 
 __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
   __shared__ float4 s_pay[kBwdWarps][32][kBRows];
+  __shared__ uint32_t s_queue[kBwdWarps][kWalkQueue];
   const FrameArgs& a = b.f;
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -136,8 +106,6 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     if (item >= items) break;
     const uint32_t tile_idx = item >> 1, half = item & 1u;
     const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
-    const uint32_t t = morton(tx, ty);
-    const uint32_t start = a.tile_off[t], count = a.tile_cnt[t];
     const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
     const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
     const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
@@ -154,9 +122,13 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     bool done = false;
     uint32_t n_end = 0;
     const float rx0 = (float)(tx * 16u) + 0.5f, ry0 = (float)(ty * 16u + 8u * half) + 0.5f;
-    for (uint32_t b0 = 0; b0 < count; b0 += 32u) {
-      const uint32_t nb = count - b0 < 32u ? count - b0 : 32u;
-      const uint32_t n = bwd_stage_kept(b, s, start + b0 + lane, lane < nb, lane, rx0, ry0);
+    TileWalk walk;
+    walk.start(a, tx, ty, s_queue[warp]);
+    for (;;) {
+      uint32_t rank = 0;
+      const uint32_t nb = walk.take(a, lane, 32u, rank);
+      if (nb == 0u) break;
+      const uint32_t n = bwd_stage_kept(b, s, rank, lane < nb, lane, rx0, ry0);
       __syncwarp();
       for (uint32_t i = 0; i < n && !done; ++i) {
         const float4 r0 = s[i][0], r1 = s[i][1];
@@ -179,7 +151,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
         done = T[0] < 0.001f && T[1] < 0.001f && T[2] < 0.001f && T[3] < 0.001f;
       }
       __syncwarp();
-      n_end = b0 + nb;
+      n_end += nb;
       if (__all_sync(0xFFFFFFFFu, done)) break;
     }
     // outputs and their incoming gradients (pixels outside the image: none)
@@ -198,10 +170,14 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       T[k] = 1.0f;
       C[k][0] = C[k][1] = C[k][2] = 0.0f;
     }
-    // pass B: gradients, same entries in the same order
-    for (uint32_t b0 = 0; b0 < n_end; b0 += 32u) {
-      const uint32_t nb = n_end - b0 < 32u ? n_end - b0 : 32u;
-      const uint32_t n = bwd_stage_kept(b, s, start + b0 + lane, lane < nb, lane, rx0, ry0);
+    // pass B: gradients, the same n_end entries in the same order
+    walk.start(a, tx, ty, s_queue[warp]);
+    for (uint32_t b0 = 0; b0 < n_end;) {
+      uint32_t rank = 0;
+      const uint32_t nb = walk.take(a, lane, n_end - b0 < 32u ? n_end - b0 : 32u, rank);
+      b0 += nb;
+      if (nb == 0u) break;
+      const uint32_t n = bwd_stage_kept(b, s, rank, lane < nb, lane, rx0, ry0);
       __syncwarp();
       for (uint32_t i = 0; i < n; ++i) {
         const float4 r0 = s[i][0], r1 = s[i][1], r2 = s[i][2];

@@ -172,6 +172,131 @@ __device__ __forceinline__ uint32_t checked_rank(uint32_t r, uint32_t N, uint32_
   return 0u;
 }
 
+// The half-tile cull of the rasteriser and of its adjoint.
+// Can the entry reach any pixel centre of the rectangle [x0, x1] x [y0, y1]
+// with power > -4 and alpha > 1/255? The power, -0.5 ia dx^2 - ib dx dy -
+// 0.5 ic dy^2 (d = p - c), is concave: its maximum over the rectangle is 0
+// when the centre lies inside, else the best point of one of the four edges
+// (each a 1D parabola, vertex clamped to the edge). Conservative: the
+// continuous rectangle contains every pixel centre, the alpha limit uses a
+// fast log with margin, and the margin grows with the size of the terms, far
+// above the rounding of this test or of the rasteriser's own power. The edge
+// vertices use approximate reciprocals: a vertex off by a relative d lowers
+// that edge's value by at most 0.5 ic (y d)^2 (resp. ia), about 1e-13 of the
+// terms, far inside the margin. An entry that fails the test changes no pixel
+// of the rectangle (every pixel is invalid for it), so skipping it is exact.
+__device__ __forceinline__ bool reaches_rect(float cx, float cy, float ia, float ib, float ic, float op, float x0,
+                                             float x1, float y0, float y1) {
+  const float xa = x0 - cx, xb = x1 - cx, ya = y0 - cy, yb = y1 - cy;
+  const float xm = mx(fabsf(xa), fabsf(xb)), ym = mx(fabsf(ya), fabsf(yb));
+  const float mag = 0.5f * ia * xm * xm + fabsf(ib) * xm * ym + 0.5f * ic * ym * ym;
+  const float margin = 1e-3f + 1e-5f * mag;
+  float best;
+  if (xa <= 0.0f && xb >= 0.0f && ya <= 0.0f && yb >= 0.0f) {
+    best = 0.0f;
+  } else {
+    float e = -3.4e38f;
+    const float xs[2] = {xa, xb}, ys[2] = {ya, yb};
+    const float ric = __fdividef(1.0f, ic), ria = __fdividef(1.0f, ia);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const float x = xs[k];
+      const float dy = clampf(-ib * x * ric, ya, yb);
+      e = mx(e, -0.5f * ia * x * x - ib * x * dy - 0.5f * ic * dy * dy);
+      const float y = ys[k];
+      const float dx = clampf(-ib * y * ria, xa, xb);
+      e = mx(e, -0.5f * ia * dx * dx - ib * dx * y - 0.5f * ic * y * y);
+    }
+    best = e;
+  }
+  // alpha = min(0.99, op exp(power)) > 1/255 needs power > -log(255 op)
+  const float lim = mx(-4.0f, -__logf(255.0f * op));
+  return best > lim - margin - 1e-3f;
+}
+
+// One tile's entries, in order, read from its superblock's list (ascending
+// (depth bits, sortRank)): the entries whose local rect covers the tile, the
+// same sequence a per-tile list holds. Warp-collective: every lane calls
+// every method. Only the list's 32-entry chunks whose mask holds the tile are
+// read (mask windows of 32 chunks, one ballot each), kWalkFill chunks per
+// fill with their keys loaded together, and the covering entries' sortRanks
+// are appended in order to a per-warp ring of kWalkQueue words.
+constexpr uint32_t kWalkQueue = 256;
+#ifndef HDSR_RASTER_FILL
+#define HDSR_RASTER_FILL 4
+#endif
+constexpr uint32_t kWalkFill = HDSR_RASTER_FILL;
+constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
+constexpr unsigned long long kNoKey = 7ull << 24;  // a rect that covers no tile (x0 = 7 > x1 = 0)
+
+__device__ __forceinline__ bool rect_covers(unsigned long long k, uint32_t lx, uint32_t ly) {
+  const uint32_t rc = local_rect(k);
+  return lx >= (rc & 7u) && lx <= ((rc >> 3) & 7u) && ly >= ((rc >> 6) & 7u) && ly <= (rc >> 9);
+}
+
+struct TileWalk {
+  uint32_t* queue;
+  uint32_t beg, end, clast, wnext, wbase, want, head, tail, lx, ly, tbit;
+  bool more;
+
+  __device__ __forceinline__ void start(const FrameArgs& a, uint32_t tx, uint32_t ty, uint32_t* q) {
+    const uint32_t sb = (ty >> kSbShift) * a.sb_cols + (tx >> kSbShift);
+    queue = q;
+    beg = a.sb_start[sb];
+    end = a.sb_start[sb + 1u];
+    lx = tx & 7u;
+    ly = ty & 7u;
+    tbit = ly * 8u + lx;
+    clast = beg < end ? (end - 1u) / kChunkEntries : 0u;
+    wnext = beg / kChunkEntries;
+    wbase = want = head = tail = 0u;
+    more = beg < end;
+  }
+  // the next chunk (ascending) whose mask holds the tile, or kNoChunk
+  __device__ __forceinline__ uint32_t next_chunk(const FrameArgs& a, uint32_t lane) {
+    while (want == 0u) {
+      if (wnext > clast) return kNoChunk;
+      const uint32_t c = wnext + lane;
+      const bool has = c <= clast && ((__ldg(a.chunk_mask + c) >> tbit) & 1ull) != 0ull;
+      want = __ballot_sync(0xFFFFFFFFu, has);
+      wbase = wnext;
+      wnext += 32u;
+    }
+    const uint32_t c = wbase + (uint32_t)(__ffs(want) - 1);
+    want &= want - 1u;
+    return c;
+  }
+  // append the covering entries of up to kWalkFill chunks, in order
+  __device__ __forceinline__ void fill(const FrameArgs& a, uint32_t lane) {
+    unsigned long long k[kWalkFill];
+#pragma unroll
+    for (uint32_t j = 0; j < kWalkFill; ++j) {
+      const uint32_t c = more ? next_chunk(a, lane) : kNoChunk;
+      more = c != kNoChunk;
+      const uint32_t i = c * kChunkEntries + lane;
+      k[j] = more && i >= beg && i < end ? __ldg(a.sbk_sorted + i) : kNoKey;
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (uint32_t j = 0; j < kWalkFill; ++j) {
+      const bool in = rect_covers(k[j], lx, ly);
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+      if (in) queue[(tail + __popc(m & lt)) & (kWalkQueue - 1u)] = (uint32_t)k[j] & 0xFFFFFFu;
+      tail += __popc(m);
+    }
+    __syncwarp();
+  }
+  // the next batch: up to `limit` (<= 32) entries; lane i gets entry i's
+  // sortRank (checked against N) when i < the returned count
+  __device__ __forceinline__ uint32_t take(const FrameArgs& a, uint32_t lane, uint32_t limit, uint32_t& rank) {
+    while (more && tail - head < limit) fill(a, lane);
+    const uint32_t n = tail - head < limit ? tail - head : limit;
+    if (lane < n) rank = checked_rank(queue[(head + lane) & (kWalkQueue - 1u)], a.N, a.ctl);
+    head += n;
+    return n;
+  }
+};
+
 // Bounded spin for decoupled-lookback waits (iterations of ~100 ns).
 constexpr uint32_t kSpinLimit = 1u << 22;
 

@@ -206,79 +206,22 @@ __device__ __forceinline__ void stage_row(float4 (*s)[kRows], const Row& w, uint
   s[slot][4] = make_float4(lo16(w.gb.z), hi16(w.gb.z), lo16(w.gb.w), 0.0f);
 }
 
-// Can the entry reach any pixel centre of the rectangle [x0, x1] x [y0, y1]
-// with power > -4 and alpha > 1/255? The power, -0.5 ia dx^2 - ib dx dy -
-// 0.5 ic dy^2 (d = p - c), is concave: its maximum over the rectangle is 0
-// when the centre lies inside, else the best point of one of the four edges
-// (each a 1D parabola, vertex clamped to the edge). Conservative: the
-// continuous rectangle contains every pixel centre, the alpha limit uses a
-// fast log with margin, and the margin grows with the size of the terms, far
-// above the rounding of this test or of the rasteriser's own power. An entry
-// that fails the test changes no pixel of the rectangle (every pixel is
-// invalid for it), so skipping it is exact.
-__device__ __forceinline__ bool touches_rect(float cx, float cy, float ia, float ib, float ic, float op, float x0,
-                                             float x1, float y0, float y1) {
-  const float xa = x0 - cx, xb = x1 - cx, ya = y0 - cy, yb = y1 - cy;
-  const float xm = mx(fabsf(xa), fabsf(xb)), ym = mx(fabsf(ya), fabsf(yb));
-  const float mag = 0.5f * ia * xm * xm + fabsf(ib) * xm * ym + 0.5f * ic * ym * ym;
-  const float margin = 1e-3f + 1e-5f * mag;
-  float best;
-  if (xa <= 0.0f && xb >= 0.0f && ya <= 0.0f && yb >= 0.0f) {
-    best = 0.0f;
-  } else {
-    float e = -3.4e38f;
-    const float xs[2] = {xa, xb}, ys[2] = {ya, yb};
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const float x = xs[k];
-      const float dy = clampf(-ib * x / ic, ya, yb);
-      e = mx(e, -0.5f * ia * x * x - ib * x * dy - 0.5f * ic * dy * dy);
-      const float y = ys[k];
-      const float dx = clampf(-ib * y / ia, xa, xb);
-      e = mx(e, -0.5f * ia * dx * dx - ib * dx * y - 0.5f * ic * y * y);
-    }
-    best = e;
-  }
-  // alpha = min(0.99, op exp(power)) > 1/255 needs power > -log(255 op)
-  const float lim = mx(-4.0f, -__logf(255.0f * op));
-  return best > lim - margin - 1e-3f;
-}
-
 // Resident blocks per SM the register budget is fitted to.
 #ifndef HDSR_RASTER_MIN_BLOCKS
 #define HDSR_RASTER_MIN_BLOCKS 4
 #endif
 
-// A list entry whose rect covers no tile (x0 = 7 > x1 = 0).
-constexpr unsigned long long kNoKey = 7ull << 24;
-constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
-
-__device__ __forceinline__ bool rect_covers(unsigned long long k, uint32_t lx, uint32_t ly) {
-  const uint32_t rc = local_rect(k);
-  return lx >= (rc & 7u) && lx <= ((rc >> 3) & 7u) && ly >= ((rc >> 6) & 7u) && ly <= (rc >> 9);
-}
-
-// Covering entries waiting to be composited, per warp (a ring of sortRanks).
-constexpr uint32_t kQueue = 256;
-constexpr uint32_t kChunksPerFill = 4;
-
 // Work unit: half a tile (rows 0-7 or 8-15), taken from an atomic counter.
-// The tile's entries, in order, are the entries of its superblock's list
-// (ascending (depth bits, sortRank)) whose local rect covers the tile: the
-// same sequence the per-tile lists hold. The warp visits only the list's
-// 32-entry chunks whose mask holds the tile (mask windows of 32 chunks, one
-// ballot each), four chunks per fill with their keys loaded together, and
-// appends the covering entries' sortRanks to its queue in order. Batches of
-// up to 32 queued entries are then composited as from a per-tile list: each
-// lane gathers one cache row, the rows of the next batch in flight while the
-// current one is composited.
+// The tile's entries come from its superblock's list through a TileWalk
+// (hdsr_internal.cuh), in batches of up to 32: each lane gathers one cache
+// row, the rows of the next batch in flight while the current one is
+// composited.
 __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(FrameArgs a) {
   __shared__ float4 s_pay[kWarps][32][kRows];
-  __shared__ uint32_t s_queue[kWarps][kQueue];
+  __shared__ uint32_t s_queue[kWarps][kWalkQueue];
   if (a.ctl[kCtlFlags] & 0x1u) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   float4 (*s)[kRows] = s_pay[warp];
-  uint32_t* queue = s_queue[warp];
   const uint32_t items = 2u * a.tile_count;
   for (;;) {
     uint32_t item = 0;
@@ -287,9 +230,6 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
     if (item >= items) break;
     const uint32_t tile_idx = item >> 1, half = item & 1u;
     const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
-    const uint32_t sb = (ty >> kSbShift) * a.sb_cols + (tx >> kSbShift);
-    const uint32_t lx = tx & 7u, ly = ty & 7u, tbit = ly * 8u + lx;
-    const uint32_t beg = a.sb_start[sb], end = a.sb_start[sb + 1u];
     const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
     const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
     const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
@@ -298,59 +238,21 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
     const uint32_t lt = (1u << lane) - 1u;
     Quad q;
     quad_init(q);
-    // chunk iterator over [beg, end) and the queue (head: next to composite)
-    uint32_t wnext = beg / kChunkEntries, wbase = 0u, want = 0u, head = 0u, tail = 0u;
-    const uint32_t clast = beg < end ? (end - 1u) / kChunkEntries : 0u;
-    bool more = beg < end;
-    // the next chunk (ascending) whose mask holds the tile, or kNoChunk
-    auto next_chunk = [&]() -> uint32_t {
-      while (want == 0u) {
-        if (wnext > clast) return kNoChunk;
-        const uint32_t c = wnext + lane;
-        const bool has = c <= clast && ((__ldg(a.chunk_mask + c) >> tbit) & 1ull) != 0ull;
-        want = __ballot_sync(0xFFFFFFFFu, has);
-        wbase = wnext;
-        wnext += 32u;
-      }
-      const uint32_t c = wbase + (uint32_t)(__ffs(want) - 1);
-      want &= want - 1u;
-      return c;
-    };
-    // append the covering entries of up to kChunksPerFill chunks, in order
-    auto fill = [&]() {
-      unsigned long long k[kChunksPerFill];
-#pragma unroll
-      for (uint32_t j = 0; j < kChunksPerFill; ++j) {
-        const uint32_t c = more ? next_chunk() : kNoChunk;
-        more = c != kNoChunk;
-        const uint32_t i = c * kChunkEntries + lane;
-        k[j] = more && i >= beg && i < end ? __ldg(a.sbk_sorted + i) : kNoKey;
-      }
-#pragma unroll
-      for (uint32_t j = 0; j < kChunksPerFill; ++j) {
-        const bool in = rect_covers(k[j], lx, ly);
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
-        if (in) queue[(tail + __popc(m & lt)) & (kQueue - 1u)] = (uint32_t)k[j] & 0xFFFFFFu;
-        tail += __popc(m);
-      }
-      __syncwarp();
-    };
-    while (more && tail - head < 32u) fill();
-    uint32_t n = tail - head < 32u ? tail - head : 32u;
+    TileWalk walk;
+    walk.start(a, tx, ty, s_queue[warp]);
+    uint32_t rank = 0;
+    uint32_t n = walk.take(a, lane, 32u, rank);
     Row cur;
-    if (lane < n) cur = load_row(a, checked_rank(queue[(head + lane) & (kQueue - 1u)], a.N, a.ctl));
-    head += n;
+    if (lane < n) cur = load_row(a, rank);
     while (n > 0u) {
       // keep, in order, the batch's entries that can reach this half tile
-      const bool keep = lane < n && touches_rect(cur.g.x, cur.g.y, cur.g.z, cur.g.w, u2f(cur.ap.x), hi16(cur.ap.y),
+      const bool keep = lane < n && reaches_rect(cur.g.x, cur.g.y, cur.g.z, cur.g.w, u2f(cur.ap.x), hi16(cur.ap.y),
                                                  rx0, rx0 + 15.0f, ry0, ry0 + 7.0f);
       const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
       if (keep) stage_row(s, cur, __popc(kept & lt));
       // the next batch: its rows in flight while this one is composited
-      while (more && tail - head < 32u) fill();
-      const uint32_t n2 = tail - head < 32u ? tail - head : 32u;
-      if (lane < n2) cur = load_row(a, checked_rank(queue[(head + lane) & (kQueue - 1u)], a.N, a.ctl));
-      head += n2;
+      const uint32_t n2 = walk.take(a, lane, 32u, rank);
+      if (lane < n2) cur = load_row(a, rank);
       __syncwarp();
       const uint32_t nk = __popc(kept);
       for (uint32_t i = 0; i < nk; ++i)

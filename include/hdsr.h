@@ -187,8 +187,7 @@ typedef enum hdsr_buffer_id {
                                  reads the superblock lists, so a frame writes these lists only
                                  with HDSR_CFG_TILE_ENTRIES or HDSR_CFG_KEEP_SORTED_KEYS; else
                                  hdsr_get_buffer builds them for the last full frame on the
-                                 handle's last stream and synchronizes that stream, and
-                                 hdsr_encode_backward builds them on its own stream. */
+                                 handle's last stream and synchronizes that stream. */
   HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] per final entry: tile<<(20+R) | k20<<R | sortRank */
   HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat superblock counts, depth order */
   HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] ascending (depth bits, sortRank): sortRank in bits 0-23,
