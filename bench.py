@@ -72,7 +72,7 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons, sampled every 50 ms from before the
+    """nvidia-smi clocks / throttle reasons, sampled every 20 ms from before the
     warm-up until after the timed loop; summary(t0, t1) keeps the samples that
     arrived during the timed region [t0, t1] (host clock), or, when the region
     is shorter than the sampling interval, the first sample after t0."""
@@ -89,7 +89,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()

@@ -214,6 +214,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.tile_dmin, M, "tile_dmin");
   ALLOC(a.tile_dmax, M, "tile_dmax");
   ALLOC(a.tile_off, M, "tile_offsets");
+  ALLOC(a.tile_order, (uint64_t)plan->tile_columns * plan->tile_rows, "tile_order");
   ALLOC(a.tile_log, M, "tile_log");
   ALLOC(a.entries, cap, "tile_entries");
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }

@@ -104,8 +104,8 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     if (lane == 0) item = atomicAdd(a.ctl + kCtlBwdTile, 1u);
     item = __shfl_sync(0xFFFFFFFFu, item, 0);
     if (item >= items) break;
-    const uint32_t tile_idx = item >> 1, half = item & 1u;
-    const uint32_t tx = tile_idx % a.cols, ty = tile_idx / a.cols;
+    const uint32_t tile = a.tile_order[item >> 1], half = item & 1u;
+    const uint32_t tx = tile & 0xFFFFu, ty = tile >> 16;
     const uint32_t bx = tx * 16u + (lane & 7u) * 2u;
     const uint32_t by = ty * 16u + ((lane >> 3) + 4u * half) * 2u;
     const float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;

@@ -27,6 +27,8 @@ enum Ctl : int {
   kCtlSortCount = 21,  // key count of the back-to-front sort (hdsr_sort_back_to_front)
   kCtlSortFlags = 22,  // its skip flags (always 0: the sort never skips)
   kCtlScatterItem = 23,// dynamic work counter of the segment scatter
+  kCtlOrderFront = 24, // tiles placed at the front of the rasterisers' work order
+  kCtlOrderBack = 25,  // tiles placed at its back
   kCtlWords = 64
 };
 
@@ -42,6 +44,7 @@ constexpr uint32_t kSbTiles = 64;
 constexpr uint32_t kSbKeyShift = 36;
 constexpr uint32_t kSegEntries = 256;            // list entries per segment
 constexpr uint32_t kChunkEntries = 32;           // list entries per chunk mask
+constexpr uint32_t kHeavyTile = 1024;            // entries from which a tile goes first in the work order
 
 // Local rect of a superblock list entry: x0 | x1 << 3 | y0 << 6 | y1 << 9.
 HDSR_HD uint32_t local_rect(unsigned long long k) { return (uint32_t)(k >> 24) & 0xFFFu; }
@@ -123,6 +126,7 @@ struct FrameArgs {
   uint32_t* tile_dmin;
   uint32_t* tile_dmax;
   uint32_t* tile_off;
+  uint32_t* tile_order;           // tile_count: ty << 16 | tx, the rasterisers' work order
   float2* tile_log;               // (logMin, keyScale)
   // entries
   unsigned long long* sorted_keys;  // optional: tile, 20-bit log-depth key, sortRank per entry

@@ -164,6 +164,16 @@ HDSR_HD uint32_t morton(uint32_t x, uint32_t y) {
   return a | (b << 1);
 }
 
+// The even bits of m, compacted (inverse of the interleave above).
+HDSR_HD uint32_t morton_even(uint32_t m) {
+  m &= 0x55555555u;
+  m = (m | (m >> 1)) & 0x33333333u;
+  m = (m | (m >> 2)) & 0x0F0F0F0Fu;
+  m = (m | (m >> 4)) & 0x00FF00FFu;
+  m = (m | (m >> 8)) & 0x0000FFFFu;
+  return m;
+}
+
 // Per-tile log-depth mapping of the hot-tile bucket cascade
 // (gpu_tile_bucket_sort.wgsl:240-244), scaled to 2^20 keys instead of 128
 // buckets: keyScale = 1048576/R = 8192 * (128/R) exactly, so a key's top

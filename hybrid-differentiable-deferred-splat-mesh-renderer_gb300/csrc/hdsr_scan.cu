@@ -97,6 +97,15 @@ struct TileScan {
   static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) {
     a.tile_off[i] = excl;
     const uint32_t c = a.tile_cnt[i];
+    // work order of the rasterisers: tiles of >= kHeavyTile entries first
+    // (the slow ones start early), the rest from the back; the order decides
+    // only which warp takes a tile when, never a pixel
+    const uint32_t tx = morton_even(i), ty = morton_even(i >> 1);
+    if (tx < a.cols && ty < a.rows) {
+      const uint32_t packed = ty << 16 | tx;
+      if (c >= kHeavyTile) a.tile_order[atomicAdd(a.ctl + kCtlOrderFront, 1u)] = packed;
+      else a.tile_order[a.tile_count - 1u - atomicAdd(a.ctl + kCtlOrderBack, 1u)] = packed;
+    }
     if (c == 0u) return;
     if (a.log_keys) a.tile_log[i] = tile_log_params(a.tile_dmin[i], a.tile_dmax[i]);
     if (c > kMaxTileEntries) {
