@@ -27,26 +27,36 @@ __device__ __forceinline__ void st_volatile(unsigned long long* p, unsigned long
 }
 
 // Exclusive prefix of all tiles before `tile`, walking back through their
-// status words (single thread).
-__device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t epoch, uint32_t* ctl) {
+// status words 32 at a time (warp-collective): lane l reads tile
+// base - l, waiting (bounded) until it is posted; the nearest inclusive
+// prefix in the window ends the walk, else the 32 aggregates are added and
+// the window moves back. Positions before tile 0 count as an inclusive 0.
+__device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t epoch, uint32_t* ctl,
+                             uint32_t lane) {
   uint32_t prefix = 0;
-  int t = (int)tile - 1;
-  while (t >= 0) {
-    unsigned long long st;
-    uint32_t spins = 0;
-    for (;;) {
-      st = ld_volatile(status + t);
-      if ((uint32_t)(st >> 34) == (epoch & 0x3FFFFFFFu) && ((st >> 32) & 3ull) != 0ull) break;
-      if (++spins > kSpinLimit) {
-        atomicOr(ctl + kCtlFlags, 0x2u);
-        st = make_status(epoch, kFlagInc, 0u);
-        break;
+  for (int base = (int)tile - 1;; base -= 32) {
+    const int t = base - (int)lane;
+    unsigned long long st = make_status(epoch, kFlagInc, 0u);
+    if (t >= 0) {
+      uint32_t spins = 0;
+      for (;;) {
+        st = ld_volatile(status + t);
+        if ((uint32_t)(st >> 34) == (epoch & 0x3FFFFFFFu) && ((st >> 32) & 3ull) != 0ull) break;
+        if (++spins > kSpinLimit) {
+          atomicOr(ctl + kCtlFlags, 0x2u);
+          st = make_status(epoch, kFlagInc, 0u);
+          break;
+        }
+        __nanosleep(64);
       }
-      __nanosleep(64);
     }
-    prefix += (uint32_t)st;
-    if (((st >> 32) & 3ull) == kFlagInc) break;
-    --t;
+    const uint32_t inc = __ballot_sync(0xFFFFFFFFu, ((st >> 32) & 3ull) == kFlagInc);
+    const uint32_t first = inc ? (uint32_t)(__ffs(inc) - 1) : 32u;
+    uint32_t v = lane <= first ? (uint32_t)st : 0u;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    prefix += v;
+    if (inc) break;
   }
   return prefix;
 }
@@ -54,8 +64,7 @@ __device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t
 // Superblock lists: splat i of the depth order writes one entry per
 // superblock its tile box touches, superblock << 36 | local rect << 24 |
 // sortRank, starting at its exclusive prefix o of the counts in depth order.
-__device__ __forceinline__ void emit_superblock_entries(const FrameArgs& a, uint32_t r, uint32_t o) {
-  const uint32_t box = a.aux[r].x;
+__device__ __forceinline__ void emit_superblock_entries(const FrameArgs& a, uint32_t r, uint32_t box, uint32_t o) {
   if (box == kSentinel) return;
   const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
   for (uint32_t sy = y0 >> kSbShift; sy <= y1 >> kSbShift; ++sy) {
@@ -81,9 +90,17 @@ struct SbScan {
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
   static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.order[i] >> 24; }
-  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) {
+  // what store needs, loaded for all of a thread's items before any store
+  struct Pre {
+    uint32_t r, box;
+  };
+  static __device__ Pre pre(const FrameArgs& a, uint32_t i) {
+    const uint32_t r = checked_rank(a.order[i] & 0xFFFFFFu, a.N, a.ctl);
+    return Pre{r, a.aux[r].x};
+  }
+  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl, const Pre& p) {
     a.sb_off[i] = excl;
-    emit_superblock_entries(a, checked_rank(a.order[i] & 0xFFFFFFu, a.N, a.ctl), excl);
+    emit_superblock_entries(a, p.r, p.box, excl);
   }
   static __device__ void finish(const FrameArgs& a, uint32_t total) { a.ctl[kCtlSbPairs] = total; }
 };
@@ -94,18 +111,28 @@ struct TileScan {
   static __device__ uint32_t counter() { return kCtlScanMTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_m; }
   static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.tile_cnt[i]; }
-  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl) {
+  using Pre = uint32_t;
+  static __device__ Pre pre(const FrameArgs& a, uint32_t i) { return a.tile_cnt[i]; }
+  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl, const Pre& c) {
     a.tile_off[i] = excl;
-    const uint32_t c = a.tile_cnt[i];
     // work order of the rasterisers: tiles of >= kHeavyTile entries first
     // (the slow ones start early), the rest from the back; the order decides
-    // only which warp takes a tile when, never a pixel
+    // only which warp takes a tile when, never a pixel. One atomic per warp
+    // and end (the calling lanes may be a partial warp).
     const uint32_t tx = morton_even(i), ty = morton_even(i >> 1);
-    if (tx < a.cols && ty < a.rows) {
-      const uint32_t packed = ty << 16 | tx;
-      if (c >= kHeavyTile) a.tile_order[atomicAdd(a.ctl + kCtlOrderFront, 1u)] = packed;
-      else a.tile_order[a.tile_count - 1u - atomicAdd(a.ctl + kCtlOrderBack, 1u)] = packed;
+    const bool in_grid = tx < a.cols && ty < a.rows, heavy = in_grid && c >= kHeavyTile;
+    const uint32_t act = __activemask(), lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+    const uint32_t mh = __ballot_sync(act, heavy), ml = __ballot_sync(act, in_grid && !heavy);
+    const uint32_t leader = (uint32_t)(__ffs(act) - 1);
+    uint32_t bh = 0u, bl = 0u;
+    if (lane == leader) {
+      if (mh) bh = atomicAdd(a.ctl + kCtlOrderFront, (uint32_t)__popc(mh));
+      if (ml) bl = atomicAdd(a.ctl + kCtlOrderBack, (uint32_t)__popc(ml));
     }
+    bh = __shfl_sync(act, bh, leader);
+    bl = __shfl_sync(act, bl, leader);
+    if (heavy) a.tile_order[bh + __popc(mh & lt)] = ty << 16 | tx;
+    else if (in_grid) a.tile_order[a.tile_count - 1u - (bl + __popc(ml & lt))] = ty << 16 | tx;
     if (c == 0u) return;
     if (a.log_keys) a.tile_log[i] = tile_log_params(a.tile_dmin[i], a.tile_dmax[i]);
     if (c > kMaxTileEntries) {
@@ -173,18 +200,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(FrameArgs a) {
         if (lane >= (uint32_t)o) wi += v;
       }
       if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-      if (lane == kScanThreads / 32 - 1) {
-        const uint32_t total = wi;
-        if (tile == 0) {
-          st_volatile(status + tile, make_status(epoch, kFlagInc, total));
-          s_prefix = 0u;
-        } else {
-          st_volatile(status + tile, make_status(epoch, kFlagAgg, total));
-          uint32_t prefix = lookback(status, tile, epoch, a.ctl);
-          st_volatile(status + tile, make_status(epoch, kFlagInc, prefix + total));
-          s_prefix = prefix;
-        }
-        if (tile == num_tiles - 1) Policy::finish(a, s_prefix + total);
+      const uint32_t total = __shfl_sync(0xFFFFFFFFu, wi, kScanThreads / 32 - 1);
+      uint32_t prefix = 0u;
+      if (tile == 0) {
+        if (lane == 0) st_volatile(status + tile, make_status(epoch, kFlagInc, total));
+      } else {
+        if (lane == 0) st_volatile(status + tile, make_status(epoch, kFlagAgg, total));
+        prefix = lookback(status, tile, epoch, a.ctl, lane);
+        if (lane == 0) st_volatile(status + tile, make_status(epoch, kFlagInc, prefix + total));
+      }
+      if (lane == 0) {
+        s_prefix = prefix;
+        if (tile == num_tiles - 1) Policy::finish(a, prefix + total);
       }
     }
     __syncthreads();
@@ -196,11 +223,19 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(FrameArgs a) {
       running += vals[k];
     }
     __syncthreads();
+    // the stores' inputs for all items first (independent loads in flight
+    // together), then the stores
+    typename Policy::Pre pre[kScanItems];
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+      const uint32_t g = base + k * kScanThreads + tid;
+      if (g < n) pre[k] = Policy::pre(a, g);
+    }
 #pragma unroll
     for (uint32_t k = 0; k < kScanItems; ++k) {
       uint32_t i = k * kScanThreads + tid;
       uint32_t g = base + i;
-      if (g < n) Policy::store(a, g, s_data[i + i / 32]);
+      if (g < n) Policy::store(a, g, s_data[i + i / 32], pre[k]);
     }
     __syncthreads();
   }
