@@ -402,6 +402,9 @@ def run_ours(args, rank, world, local):
     F = setup_frame(pkg, wl, local)
     res, plan = F["res"], F["plan"]
     N, P = plan.splat_count, int(F["stats"]["total_pairs"])
+    # every leg runs on a stream of its own: hdsr_encode_full replays a full
+    # frame as a CUDA graph on any stream but the legacy default one
+    torch.cuda.set_stream(torch.cuda.Stream(device=dev))
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 

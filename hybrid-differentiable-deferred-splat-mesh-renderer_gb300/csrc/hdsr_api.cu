@@ -63,6 +63,14 @@ struct hdsr_compositor {
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   uint32_t ev_used = 0;
   uint32_t pass_id[kMaxProfiledPasses] = {};
+  // a full frame's kernels as one CUDA graph: captured on the second full
+  // frame after a bind (the first runs directly) and replayed until the next
+  // bind or profiling change; replays launch the same kernels with the same
+  // arguments, which read the uniforms from device memory
+  cudaGraphExec_t frame_graph = nullptr;
+  uint64_t graph_launches = 0;    // kernels of one replay
+  uint32_t direct_frames = 0;     // full frames launched directly since the last bind
+  bool graph_failed = false;      // capture failed: launch directly until the next bind
   char err[256] = {0};
 };
 
@@ -102,6 +110,14 @@ hdsr_status dev_alloc(hdsr_compositor* h, T** p, uint64_t count, const char* wha
   h->device_bytes += bytes;
   *p = static_cast<T*>(ptr);
   return HDSR_OK;
+}
+
+// The frame graph no longer matches the handle's arguments (or is not wanted).
+void drop_graph(hdsr_compositor* h) {
+  if (h->frame_graph) cudaGraphExecDestroy(h->frame_graph);
+  h->frame_graph = nullptr;
+  h->direct_frames = 0;
+  h->graph_failed = false;
 }
 
 void free_all(hdsr_compositor* h) {
@@ -275,6 +291,7 @@ void hdsr_destroy_tile_splat_compositor(hdsr_compositor* h) {
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->side) cudaStreamDestroy(h->side);
+  drop_graph(h);
   free_all(h);
   cudaSetDevice(prev);
   delete h;
@@ -307,6 +324,7 @@ hdsr_status hdsr_bind_scene(hdsr_compositor* h, const hdsr_scene_views* sc) {
   a.sh_degree = sc->sh_degree;
   h->scene_bound = true;
   h->sorted_valid = false;
+  drop_graph(h);
   return HDSR_OK;
 }
 
@@ -333,6 +351,7 @@ hdsr_status hdsr_bind_outputs(hdsr_compositor* h, const hdsr_output_views* o) {
   a.out_material = o->material;
   a.material_pitch = o->material_pitch;
   h->outputs_bound = true;
+  drop_graph(h);
   return HDSR_OK;
 }
 
@@ -516,6 +535,36 @@ static hdsr_status ensure_entries(hdsr_compositor* h, cudaStream_t s) {
   return HDSR_OK;
 }
 
+// Frames go through the frame graph unless HDSR_CFG_NO_GRAPH, profiling (the
+// per-pass events need direct launches) or a legacy / per-thread default
+// stream (which cannot be captured) says otherwise.
+static bool use_graph(const hdsr_compositor* h, cudaStream_t s) {
+  return !(h->cfg.flags & HDSR_CFG_NO_GRAPH) && !h->profiling && s != nullptr && s != cudaStreamLegacy &&
+         s != cudaStreamPerThread;
+}
+
+// Captures every kernel of a full frame on `s` (nothing runs) into
+// h->frame_graph; on any failure the handle launches directly until the next
+// bind.
+static void capture_frame(hdsr_compositor* h, cudaStream_t s) {
+  const uint64_t before = h->launches;
+  cudaGraph_t g = nullptr;
+  hdsr_status st = HDSR_ERR_CUDA;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    st = encode_pre_raster(h, s);
+    if (st == HDSR_OK) st = encode_raster(h, s, true);
+    if (cudaStreamEndCapture(s, &g) != cudaSuccess) st = HDSR_ERR_CUDA;
+  }
+  h->graph_launches = h->launches - before;
+  h->launches = before;  // captured, not run
+  if (st != HDSR_OK || !g || cudaGraphInstantiate(&h->frame_graph, g, 0) != cudaSuccess) {
+    h->frame_graph = nullptr;
+    h->graph_failed = true;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();  // a failed capture leaves no sticky error: clear its record
+}
+
 static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
   hdsr_status st = encode_checks(h, full);
   if (st != HDSR_OK) return st;
@@ -539,8 +588,23 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
     h->device_u_valid = true;
   }
   mark(h, s, 0);
+  if (full && use_graph(h, s)) {
+    if (!h->frame_graph && !h->graph_failed && h->direct_frames > 0) capture_frame(h, s);
+    if (h->frame_graph) {
+      cudaError_t e = cudaGraphLaunch(h->frame_graph, s);
+      if (e != cudaSuccess) return cuda_fail(h, e, "frame graph launch");
+      h->launches += h->graph_launches;
+      h->last_stream = s;
+      h->has_last_stream = true;
+      h->sorted_valid = true;
+      h->entries_valid = entries_each_frame(h);
+      return HDSR_OK;
+    }
+  }
   if (full && (st = encode_pre_raster(h, s)) != HDSR_OK) return st;
-  return encode_raster(h, s, full);
+  st = encode_raster(h, s, full);
+  if (st == HDSR_OK && full) ++h->direct_frames;
+  return st;
 }
 
 hdsr_status hdsr_encode_full(hdsr_compositor* h, void* stream) { return encode(h, stream, true); }
@@ -671,6 +735,7 @@ hdsr_status hdsr_set_profiling(hdsr_compositor* h, int enable) {
       if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventCreate");
     }
   }
+  if ((enable != 0) != h->profiling) drop_graph(h);
   h->profiling = enable != 0;
   return HDSR_OK;
 }

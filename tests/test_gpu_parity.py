@@ -210,6 +210,41 @@ def test_composite_only_and_determinism(cuda, pkg, orc):
         assert np.array_equal(third[k], first[k]), k
 
 
+def test_frame_graph_replays_match_direct_frames(cuda, pkg, orc):
+    # On a stream other than the legacy default one, the second full frame
+    # after a bind is captured into a CUDA graph that later frames replay;
+    # a rebind drops the graph (the next frames write the new outputs).
+    import torch
+
+    wl = pkg.workloads.plain50k()
+    g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height)  # legacy stream: direct
+    res = g["res"]
+    first = read_gpu(g)
+    per_frame = res.launch_count()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            g["color"].zero_()
+            pkg.encode_full_compute_compositor_pipeline(s, res)
+    s.synchronize()
+    assert res.launch_count() == 4 * per_frame
+    again = read_gpu(g)
+    assert np.array_equal(again["color"].view(np.uint16), first["color"].view(np.uint16))
+    for k in ("out_depth", "normal", "material", "tile_entries"):
+        assert np.array_equal(again[k], first[k]), k
+    color2, gb2 = pkg.create_output_textures(g["plan"])
+    pkg.create_tile_splat_bind_groups(res, g["bufs"], color2, gb2)
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            pkg.encode_full_compute_compositor_pipeline(s, res)
+    s.synchronize()
+    assert torch.equal(color2.view(torch.int16), g["color"].view(torch.int16))
+    assert torch.equal(gb2["material"], g["gb"]["material"])
+    res.destroy()
+
+
 def test_tile_entries_on_demand(cuda, pkg, orc):
     # The rasteriser reads the superblock lists, so without
     # HDSR_CFG_TILE_ENTRIES / KEEP_SORTED_KEYS a frame writes no per-tile
