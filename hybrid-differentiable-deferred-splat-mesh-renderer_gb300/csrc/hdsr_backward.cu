@@ -43,27 +43,34 @@ constexpr int kBwdWarps = 4;
 //   row 2: b, ia, ib, ic        row 3: sortRank bits, 0, 0, 0
 constexpr int kBRows = 4;
 
-// Stages the entry of sortRank r, in order, if it can reach the half tile
+// One entry's adjoint parameters as loaded (a batch ahead of its use).
+struct BwdRow {
+  float4 p0, p1, p2;
+  uint32_t r;
+};
+
+__device__ __forceinline__ void bwd_load(const BwdArgs& b, BwdRow& w, uint32_t r) {
+  w.p0 = b.par[(size_t)r * 3];
+  w.p1 = b.par[(size_t)r * 3 + 1];
+  w.p2 = b.par[(size_t)r * 3 + 2];
+  w.r = r;
+}
+
+// Stages the loaded entry, in order, if it can reach the half tile
 // [x0, x0 + 15] x [y0, y0 + 7]; returns how many of the batch were kept
 // (warp-collective: every lane calls it, lanes without an entry pass
 // valid = false).
-__device__ __forceinline__ uint32_t bwd_stage_kept(const BwdArgs& b, float4 (*s)[kBRows], uint32_t r, bool valid,
-                                                   uint32_t lane, float x0, float y0) {
-  bool keep = false;
-  float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0;
-  if (valid) {
-    p0 = b.par[(size_t)r * 3];
-    p1 = b.par[(size_t)r * 3 + 1];
-    p2 = b.par[(size_t)r * 3 + 2];
-    keep = reaches_rect(p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, x0, x0 + 15.0f, y0, y0 + 7.0f);
-  }
+__device__ __forceinline__ uint32_t bwd_stage_kept(float4 (*s)[kBRows], const BwdRow& w, bool valid, uint32_t lane,
+                                                   float x0, float y0) {
+  const bool keep =
+      valid && reaches_rect(w.p0.x, w.p0.y, w.p0.z, w.p0.w, w.p1.x, w.p1.y, x0, x0 + 15.0f, y0, y0 + 7.0f);
   const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
   if (keep) {
     const uint32_t k = __popc(kept & ((1u << lane) - 1u));
-    s[k][0] = make_float4(p0.x, p0.y, p0.z * -0.5f, -p0.w);
-    s[k][1] = make_float4(p1.x * -0.5f, p1.y, p1.z, p1.w);
-    s[k][2] = make_float4(p2.x, p0.z, p0.w, p1.x);
-    s[k][3] = make_float4(u2f(r), 0.0f, 0.0f, 0.0f);
+    s[k][0] = make_float4(w.p0.x, w.p0.y, w.p0.z * -0.5f, -w.p0.w);
+    s[k][1] = make_float4(w.p1.x * -0.5f, w.p1.y, w.p1.z, w.p1.w);
+    s[k][2] = make_float4(w.p2.x, w.p0.z, w.p0.w, w.p1.x);
+    s[k][3] = make_float4(u2f(w.r), 0.0f, 0.0f, 0.0f);
   }
   return __popc(kept);
 }
@@ -124,11 +131,15 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     const float rx0 = (float)(tx * 16u) + 0.5f, ry0 = (float)(ty * 16u + 8u * half) + 0.5f;
     TileWalk walk;
     walk.start(a, tx, ty, s_queue[warp]);
-    for (;;) {
-      uint32_t rank = 0;
-      const uint32_t nb = walk.take(a, lane, 32u, rank);
-      if (nb == 0u) break;
-      const uint32_t n = bwd_stage_kept(b, s, rank, lane < nb, lane, rx0, ry0);
+    BwdRow cur;
+    uint32_t rank = 0;
+    uint32_t nb = walk.take(a, lane, 32u, rank);
+    if (lane < nb) bwd_load(b, cur, rank);
+    while (nb > 0u) {
+      const uint32_t n = bwd_stage_kept(s, cur, lane < nb, lane, rx0, ry0);
+      // the next batch's parameters in flight while this one is composited
+      const uint32_t nb2 = walk.take(a, lane, 32u, rank);
+      if (lane < nb2) bwd_load(b, cur, rank);
       __syncwarp();
       for (uint32_t i = 0; i < n && !done; ++i) {
         const float4 r0 = s[i][0], r1 = s[i][1];
@@ -153,6 +164,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       __syncwarp();
       n_end += nb;
       if (__all_sync(0xFFFFFFFFu, done)) break;
+      nb = nb2;
     }
     // outputs and their incoming gradients (pixels outside the image: none)
     float O[4][3], Tf[4], gO[4][3], gA[4];
@@ -172,12 +184,14 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
     }
     // pass B: gradients, the same n_end entries in the same order
     walk.start(a, tx, ty, s_queue[warp]);
-    for (uint32_t b0 = 0; b0 < n_end;) {
-      uint32_t rank = 0;
-      const uint32_t nb = walk.take(a, lane, n_end - b0 < 32u ? n_end - b0 : 32u, rank);
-      b0 += nb;
-      if (nb == 0u) break;
-      const uint32_t n = bwd_stage_kept(b, s, rank, lane < nb, lane, rx0, ry0);
+    nb = walk.take(a, lane, n_end < 32u ? n_end : 32u, rank);
+    uint32_t b0 = nb;
+    if (lane < nb) bwd_load(b, cur, rank);
+    while (nb > 0u) {
+      const uint32_t n = bwd_stage_kept(s, cur, lane < nb, lane, rx0, ry0);
+      const uint32_t nb2 = walk.take(a, lane, n_end - b0 < 32u ? n_end - b0 : 32u, rank);
+      b0 += nb2;
+      if (lane < nb2) bwd_load(b, cur, rank);
       __syncwarp();
       for (uint32_t i = 0; i < n; ++i) {
         const float4 r0 = s[i][0], r1 = s[i][1], r2 = s[i][2];
@@ -225,6 +239,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
         }
       }
       __syncwarp();
+      nb = nb2;
     }
   }
 }

@@ -346,7 +346,10 @@ constexpr uint32_t kScanItems = 16;
 constexpr uint32_t kScanThreads = 256;
 constexpr uint32_t kScanTile = kScanItems * kScanThreads;
 constexpr uint32_t kRadixThreads = 256;
-constexpr uint32_t kRadixItems = 15;
+#ifndef HDSR_RADIX_ITEMS
+#define HDSR_RADIX_ITEMS 10
+#endif
+constexpr uint32_t kRadixItems = HDSR_RADIX_ITEMS;
 constexpr uint32_t kRadixTile = kRadixThreads * kRadixItems;
 
 }  // namespace hdsr
