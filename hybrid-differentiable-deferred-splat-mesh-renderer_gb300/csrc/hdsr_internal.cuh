@@ -135,7 +135,7 @@ struct FrameArgs {
   uint32_t* tile_digits;
   uint32_t* bin_base;
   uint32_t radix_tiles_cap;
-  unsigned long long* scan_status_n; // per 4096-element tile of the N scan
+  unsigned long long* scan_status_n; // per kScanTile-element tile of the N scan
   unsigned long long* scan_status_m;
   uint32_t* ctl;
   // outputs (borrowed)
@@ -342,7 +342,10 @@ int handle_encode_pre_raster(hdsr_compositor* h, cudaStream_t s);  // capturable
 int handle_encode_raster(hdsr_compositor* h, cudaStream_t s);
 
 // sizing helpers shared with the API
-constexpr uint32_t kScanItems = 16;
+#ifndef HDSR_SCAN_ITEMS
+#define HDSR_SCAN_ITEMS 8
+#endif
+constexpr uint32_t kScanItems = HDSR_SCAN_ITEMS;
 constexpr uint32_t kScanThreads = 256;
 constexpr uint32_t kScanTile = kScanItems * kScanThreads;
 constexpr uint32_t kRadixThreads = 256;

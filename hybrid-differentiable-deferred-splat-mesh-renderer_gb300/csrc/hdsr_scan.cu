@@ -10,7 +10,7 @@
 //     tileOffsets), the hot-tile statistics of classify_tiles
 //     (gpu_tile_classify.wgsl:44-86) and, when requested, the per-tile
 //     log-depth parameters of the 20-bit keys.
-// Tiles of 4096 elements are claimed through an atomic counter, so a tile
+// Tiles of kScanTile (2048) elements are claimed through an atomic counter, so a tile
 // only waits on tiles already claimed by running blocks; every wait is
 // bounded and sets HDSR_DEV_TIMEOUT when it gives up.
 #include "hdsr_internal.cuh"
