@@ -36,6 +36,7 @@ CFG_KEEP_SORTED_KEYS = 0x1
 CFG_NO_GRAPH = 0x2
 CFG_BACKWARD = 0x4
 CFG_TILE_ENTRIES = 0x8
+CFG_F16_COMPOSITE = 0x10
 
 DEV_OVERFLOW = 0x1
 DEV_TIMEOUT = 0x2

@@ -70,11 +70,12 @@ class TileSplatCompositorResources:
     """Owner of one compositor handle (and of every internal device buffer)."""
 
     def __init__(self, plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,
-                 keep_sorted_keys: bool = False, backward: bool = False, tile_entries: bool = False):
+                 keep_sorted_keys: bool = False, backward: bool = False, tile_entries: bool = False,
+                 f16: bool = False):
         self.plan = plan
         self._lib = _lib.load()
         flags = ((_lib.CFG_KEEP_SORTED_KEYS if keep_sorted_keys else 0) | (_lib.CFG_BACKWARD if backward else 0)
-                 | (_lib.CFG_TILE_ENTRIES if tile_entries else 0))
+                 | (_lib.CFG_TILE_ENTRIES if tile_entries else 0) | (_lib.CFG_F16_COMPOSITE if f16 else 0))
         cfg = _lib.Config(int(pair_capacity), _lib.COLOR_RGBA32F if f32_color else _lib.COLOR_RGBA16F, flags)
         handle = ctypes.c_void_p()
         status = self._lib.hdsr_create_tile_splat_compositor(ctypes.byref(plan._c()), ctypes.byref(cfg),
@@ -171,8 +172,11 @@ class _DeviceView:
 
 def create_tile_splat_compositor(plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,
                                  keep_sorted_keys: bool = False, backward: bool = False,
-                                 tile_entries: bool = False) -> TileSplatCompositorResources:
-    return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys, backward, tile_entries)
+                                 tile_entries: bool = False, f16: bool = False) -> TileSplatCompositorResources:
+    """createTileSplatCompositor (gpuTileSplatCompositor.ts:141-728); `f16` is its
+    {f16} option, the f16 composite variant."""
+    return TileSplatCompositorResources(plan, pair_capacity, f32_color, keep_sorted_keys, backward, tile_entries,
+                                        f16)
 
 
 def sort_back_to_front(stream, resources: TileSplatCompositorResources, view, out) -> None:

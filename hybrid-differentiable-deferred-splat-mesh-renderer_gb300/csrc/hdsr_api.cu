@@ -196,6 +196,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   a.num_sms = sms > 0 ? sms : 1;
   a.color_f32 = h->cfg.color_format == HDSR_COLOR_RGBA32F;
   a.log_keys = (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) ? 1u : 0u;
+  a.composite_f16 = (h->cfg.flags & HDSR_CFG_F16_COMPOSITE) ? 1u : 0u;
   const uint64_t sb_cap = (uint64_t)N * 9u;  // a tile box (<= 17 tiles a side) meets <= 3x3 superblocks
   a.sb_cap = sb_cap;
   a.seg_cap = (uint32_t)((sb_cap + kSegEntries - 1u) / kSegEntries + a.num_sb);
@@ -624,6 +625,8 @@ hdsr_status hdsr_sort_back_to_front(hdsr_compositor* h, const float view[16], ui
 hdsr_status hdsr_encode_backward(hdsr_compositor* h, const hdsr_grad_views* g, void* stream) {
   if (!h) return HDSR_ERR_INVALID_ARG;
   if (!(h->cfg.flags & HDSR_CFG_BACKWARD)) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_BACKWARD");
+  if (h->cfg.flags & HDSR_CFG_F16_COMPOSITE)
+    return fail(h, HDSR_ERR_UNSUPPORTED, "the adjoint differentiates the f32 composite, not HDSR_CFG_F16_COMPOSITE");
   if (!g || !g->d_color) return fail(h, HDSR_ERR_INVALID_ARG, "gradient views are NULL");
   if (!h->sorted_valid) return fail(h, HDSR_ERR_NOT_BOUND, "no frame: encode_full first");
   const FrameArgs& a = h->args;

@@ -100,6 +100,7 @@ struct FrameArgs {
   uint32_t seg_cap;               // capacity of the segment tables
   uint64_t cap;                   // pair capacity
   uint32_t log_keys;              // compute per-tile depth range + 20-bit keys
+  uint32_t composite_f16;         // the f16 composite variant (HDSR_CFG_F16_COMPOSITE)
   // projection cache (SoA) and per-splat data
   float4* geo;                    // centerPx.xy, invCov.xy
   uint4* app;                     // invCov.z bits, f16(radius,opacity), f16 rg, f16 b|0

@@ -104,6 +104,22 @@ __device__ __forceinline__ float raster_expf(float x) {
   return p * u2f((uint32_t)(ki + 127) << 23);
 }
 
+// The f16 composite variant (gpu_tile_splat_composite_f16.wgsl:53-54, 254):
+// its thresholds and background are f16 constants.
+__device__ __forceinline__ __half h16_bits(unsigned short b) { return __ushort_as_half(b); }
+constexpr unsigned short kAlphaTh16 = 0x1C04u;  // 1.0h / 255.0h
+constexpr unsigned short kCutoff16 = 0x1419u;   // 0.001h
+constexpr unsigned short kBgRG16 = 0x251Fu;     // 0.02h
+constexpr unsigned short kBgB16 = 0x291Fu;      // 0.04h
+
+// One entry on the lane's quad. F16 selects the f16 variant
+// (gpu_tile_splat_composite_f16.wgsl:186-233): alpha rounded to f16, T' =
+// T * (1 - alpha) and the weight alpha * T as f16 products, colour by one f16
+// fused multiply-add per channel; the Gaussian, alpha and the G-buffer votes
+// stay f32. Every f16 operation is IEEE round-to-nearest-even (__hmul,
+// __hsub, __hfma); T and the colour sums are kept as the floats of their f16
+// values.
+template <bool F16>
 __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, const float4 (*s)[kRows], int i) {
   const float4 r0 = s[i][0], r1 = s[i][1];
   const float cx = r0.x, cy = r0.y;
@@ -129,13 +145,26 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
   for (int k = 0; k < 4; ++k) {
     const float g = raster_expf(pw[k]);
     const float al = mn(0.99f, op * g);
-    const float nT = q.T[k] * (1.0f - al);
-    const bool valid = (pw[k] > -4.0f) && (al > (1.0f / 255.0f)) && (q.T[k] >= 0.001f);
-    const float w = valid ? al * q.T[k] : 0.0f;
-    q.c[k][0] = fmaf(sr, w, q.c[k][0]);
-    q.c[k][1] = fmaf(sg, w, q.c[k][1]);
-    q.c[k][2] = fmaf(sb, w, q.c[k][2]);
-    if (valid) q.T[k] = nT;
+    float w;
+    if (F16) {
+      const __half a16 = __float2half_rn(al), T16 = __float2half_rn(q.T[k]);
+      const bool valid = (pw[k] > -4.0f) && (al > __half2float(h16_bits(kAlphaTh16))) &&
+                         (q.T[k] >= __half2float(h16_bits(kCutoff16)));
+      const __half w16 = valid ? __hmul(a16, T16) : __float2half_rn(0.0f);
+      w = __half2float(w16);
+      q.c[k][0] = __half2float(__hfma(__float2half_rn(sr), w16, __float2half_rn(q.c[k][0])));
+      q.c[k][1] = __half2float(__hfma(__float2half_rn(sg), w16, __float2half_rn(q.c[k][1])));
+      q.c[k][2] = __half2float(__hfma(__float2half_rn(sb), w16, __float2half_rn(q.c[k][2])));
+      if (valid) q.T[k] = __half2float(__hmul(T16, __hsub(__float2half_rn(1.0f), a16)));
+    } else {
+      const float nT = q.T[k] * (1.0f - al);
+      const bool valid = (pw[k] > -4.0f) && (al > (1.0f / 255.0f)) && (q.T[k] >= 0.001f);
+      w = valid ? al * q.T[k] : 0.0f;
+      q.c[k][0] = fmaf(sr, w, q.c[k][0]);
+      q.c[k][1] = fmaf(sg, w, q.c[k][1]);
+      q.c[k][2] = fmaf(sb, w, q.c[k][2]);
+      if (valid) q.T[k] = nT;
+    }
     const float gw = w > 0.01f ? w : 0.0f;
     q.gd[k] = fmaf(gw, sd, q.gd[k]);
     q.gw[k] = q.gw[k] + gw;
@@ -151,18 +180,28 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
       q.e[k][2] = fmaf(eb, w, q.e[k][2]);
     }
   }
-  q.done = q.T[0] < 0.001f && q.T[1] < 0.001f && q.T[2] < 0.001f && q.T[3] < 0.001f;
+  const float cut = F16 ? __half2float(h16_bits(kCutoff16)) : 0.001f;
+  q.done = q.T[0] < cut && q.T[1] < cut && q.T[2] < cut && q.T[3] < cut;
 }
 
+template <bool F16>
 __device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, uint32_t bx, uint32_t by) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const uint32_t px = bx + (uint32_t)(k & 1), py = by + (uint32_t)(k >> 1);
     if (px >= a.W || py >= a.H) continue;
     const float sw = mx(q.gw[k], 0.0001f);
-    const float cr = fmaf(q.T[k], 0.02f, q.c[k][0]);
-    const float cg = fmaf(q.T[k], 0.02f, q.c[k][1]);
-    const float cb = fmaf(q.T[k], 0.04f, q.c[k][2]);
+    float cr, cg, cb;
+    if (F16) {
+      const __half T16 = __float2half_rn(q.T[k]);
+      cr = __half2float(__hfma(T16, h16_bits(kBgRG16), __float2half_rn(q.c[k][0])));
+      cg = __half2float(__hfma(T16, h16_bits(kBgRG16), __float2half_rn(q.c[k][1])));
+      cb = __half2float(__hfma(T16, h16_bits(kBgB16), __float2half_rn(q.c[k][2])));
+    } else {
+      cr = fmaf(q.T[k], 0.02f, q.c[k][0]);
+      cg = fmaf(q.T[k], 0.02f, q.c[k][1]);
+      cb = fmaf(q.T[k], 0.04f, q.c[k][2]);
+    }
     const float ca = 1.0f - q.T[k];
     char* crow = static_cast<char*>(a.out_color) + (size_t)py * a.color_pitch;
     if (a.color_f32) {
@@ -216,6 +255,7 @@ __device__ __forceinline__ void stage_row(float4 (*s)[kRows], const Row& w, uint
 // (hdsr_internal.cuh), in batches of up to 32: each lane gathers one cache
 // row, the rows of the next batch in flight while the current one is
 // composited.
+template <bool F16>
 __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(FrameArgs a) {
   __shared__ float4 s_pay[kWarps][32][kRows];
   __shared__ uint32_t s_queue[kWarps][kWalkQueue];
@@ -256,12 +296,12 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
       __syncwarp();
       const uint32_t nk = __popc(kept);
       for (uint32_t i = 0; i < nk; ++i)
-        if (!q.done) quad_splat(q, p00x, p00y, s, (int)i);
+        if (!q.done) quad_splat<F16>(q, p00x, p00y, s, (int)i);
       __syncwarp();
       if (__all_sync(0xFFFFFFFFu, q.done)) break;
       n = n2;
     }
-    quad_store(a, q, bx, by);
+    quad_store<F16>(a, q, bx, by);
   }
 }
 
@@ -272,7 +312,10 @@ cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s) {
   const uint32_t want = (2u * a.tile_count + kWarps - 1) / kWarps;
   const uint32_t cap = (uint32_t)a.num_sms * 8u;
   const uint32_t blocks = want < cap ? want : cap;
-  if (blocks) k_raster<<<blocks, kWarps * 32, 0, s>>>(a);
+  if (blocks) {
+    if (a.composite_f16) k_raster<true><<<blocks, kWarps * 32, 0, s>>>(a);
+    else k_raster<false><<<blocks, kWarps * 32, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

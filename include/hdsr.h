@@ -77,9 +77,12 @@ typedef struct hdsr_plan {
 #define HDSR_CFG_BACKWARD         0x4u  /* allocate the adjoint's buffers (hdsr_encode_backward) */
 #define HDSR_CFG_TILE_ENTRIES     0x8u  /* write the per-tile entry lists in every full frame
                                            (otherwise built on demand: see HDSR_BUF_TILE_ENTRIES) */
+#define HDSR_CFG_F16_COMPOSITE    0x10u /* createTileSplatCompositor {f16: true}: the f16 composite
+                                           variant (gpu_tile_splat_composite_f16.wgsl), transmittance
+                                           and colour accumulated in f16; no hdsr_encode_backward */
 
 /* Options of createTileSplatCompositor — gpuTileSplatCompositor.ts:141-145
- * ({f16?}); the f16 composite variant is not rebuilt (FP32 transmittance). */
+ * ({f16?} is HDSR_CFG_F16_COMPOSITE; FP32 transmittance is the default). */
 typedef struct hdsr_config {
   uint64_t pair_capacity;         /* (tile, splat) pairs held; 0 = max(budget, ceil(N*16)) */
   uint32_t color_format;          /* HDSR_COLOR_* */

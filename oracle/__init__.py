@@ -49,7 +49,7 @@ class Frame(ctypes.Structure):
                 ("tile_offsets", c_void_p), ("tile_entries", c_void_p), ("entries_cap", c_uint64),
                 ("chunk_ranges", c_void_p), ("chunk_cap", c_uint32), ("total_pairs", c_uint64),
                 ("small_tiles", c_uint32), ("hot_tiles", c_uint32), ("total_chunks", c_uint32),
-                ("large_splats", c_uint32), ("flags", c_uint32), ("_pad", c_uint32), ("out_color", c_void_p),
+                ("large_splats", c_uint32), ("flags", c_uint32), ("composite_f16", c_uint32), ("out_color", c_void_p),
                 ("out_depth", c_void_p), ("out_normal", c_void_p), ("out_material", c_void_p)]
 
 
@@ -85,7 +85,7 @@ def lib() -> ctypes.CDLL:
         L.orc_sort_back_to_front.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p, c_int]
         L.orc_gpu_sort_prototype_order.restype = c_int
         L.orc_gpu_sort_prototype_order.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p]
-        for nm in ("orc_expf_n", "orc_logf_n", "orc_f16_rne_n", "orc_f16_trunc_n", "orc_f16_to_f32_n"):
+        for nm in ("orc_expf_n", "orc_logf_n", "orc_f16_rne_n", "orc_f16_trunc_n", "orc_f16_to_f32_n", "orc_f64_to_f16_n"):
             getattr(L, nm).argtypes = [c_void_p, c_void_p, c_uint64]
         L.orc_morton_n.argtypes = [c_void_p, c_void_p, c_void_p, c_uint64]
         L.orc_bucket_key20_n.argtypes = [c_void_p, c_uint64, c_uint32, c_uint32, c_void_p, c_void_p]
@@ -125,9 +125,10 @@ def _u32(u):
 
 
 def render_frame(U: np.ndarray, packed, sorted_indices, threads: int | None = None, composite: bool = True,
-                 cap: int | None = None) -> dict:
+                 cap: int | None = None, f16: bool = False) -> dict:
     """Full canonical frame: cache, counts, offsets, per-tile order, outputs.
-    `cap` is the initial entry capacity (grown and retried when too small)."""
+    `cap` is the initial entry capacity (grown and retried when too small);
+    `f16` selects the f16 composite variant (gpu_tile_splat_composite_f16.wgsl)."""
     L = lib()
     U = np.ascontiguousarray(U, np.float32)
     uu = _u32(U)
@@ -147,7 +148,8 @@ def render_frame(U: np.ndarray, packed, sorted_indices, threads: int | None = No
             out.update(color=np.zeros(W * H * 4, np.uint16), out_depth=np.zeros(W * H, np.float32),
                        normal=np.zeros(W * H, np.uint32), material=np.zeros(W * H * 4, np.uint32))
         f = Frame(_p(out["proj_cache"]), _p(out["depth"]), _p(out["tile_counts"]), _p(out["tile_offsets"]),
-                  _p(out["tile_entries"]), cap, _p(out["chunk_ranges"]), chunk_cap, 0, 0, 0, 0, 0, 0, 0,
+                  _p(out["tile_entries"]), cap, _p(out["chunk_ranges"]), chunk_cap, 0, 0, 0, 0, 0, 0,
+                  1 if f16 else 0,
                   _p(out.get("color")), _p(out.get("out_depth")), _p(out.get("normal")), _p(out.get("material")))
         rc = L.orc_render_frame(U.ctypes.data_as(c_void_p), ctypes.byref(scene), ctypes.byref(f), nt)
         if rc == -2:
@@ -265,6 +267,10 @@ def logf(x):
 
 def f16_rne(x):
     return _map("orc_f16_rne_n", x, np.uint16)
+
+
+def f64_to_f16(x):
+    return _map("orc_f64_to_f16_n", x, np.uint16, np.float64)
 
 
 def f16_trunc(x):

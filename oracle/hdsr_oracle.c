@@ -130,6 +130,29 @@ float orc_f16_to_f32(uint16_t h) {
   return bitsf(sign | ((e + 112u) << 23) | (m << 13));
 }
 
+/* IEEE binary16 round-to-nearest-even of a double (overflow -> inf, NaN ->
+ * 0x7E00, subnormals kept). The f16 composite's arithmetic is exact in
+ * double and then rounded here once, which is what a correctly rounded f16
+ * multiply, subtract or fused multiply-add returns. */
+uint16_t orc_f64_to_f16_rne(double x) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  const uint16_t sign = (uint16_t)((b >> 48) & 0x8000u);
+  const uint64_t ab = b & 0x7FFFFFFFFFFFFFFFull;
+  if (ab > 0x7FF0000000000000ull) return (uint16_t)0x7E00u;
+  if (ab >= 0x40EFFE0000000000ull) return (uint16_t)(sign | 0x7C00u); /* >= 65520 */
+  if ((ab >> 52) == 0) return sign;                                    /* double subnormal: rounds to 0 */
+  const int e = (int)(ab >> 52) - 1023;
+  const uint64_t m = (ab & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int shift = e >= -14 ? 42 : 28 - e;  /* keep 11 bits (normal) or value / 2^-24 (subnormal) */
+  if (shift > 63) return sign;
+  uint64_t q = m >> shift;
+  const uint64_t rem = m & ((1ull << shift) - 1ull), half = 1ull << (shift - 1);
+  if (rem > half || (rem == half && (q & 1ull))) q += 1ull;
+  if (e < -14) return (uint16_t)(sign | (uint16_t)q);  /* q == 0x400 is the smallest normal */
+  return (uint16_t)(sign | (uint16_t)((((uint32_t)(e + 15)) << 10) + (uint32_t)(q - 0x400ull)));
+}
+
 /* splats.ts:431-442 — truncating f32ToF16 used by the host packers. */
 uint16_t orc_f32_to_f16_trunc(float value) {
   uint32_t bits = fbits(value);
@@ -839,6 +862,100 @@ static void composite_tile(const float* U, const uint32_t* pc, const uint32_t* d
     }
 }
 
+/* ---------------------------------------------------------------------------
+ * composite, f16 variant — gpu_tile_splat_composite_f16.wgsl:86-285 (the
+ * reference selects it when the adapter has shader-f16, splatRenderer.ts:907).
+ * The Gaussian, alpha and the G-buffer votes stay f32 as in composite_tile;
+ * transmittance and colour are f16: alpha is rounded to f16 (:193),
+ * T' = T * (1 - alpha) rounds twice (:194), the weight is f16(alpha * T)
+ * (:197), colour accumulates with one f16 fused multiply-add per channel
+ * (:199, the canonical form, like the f32 path's fmaf), the thresholds are
+ * the f16 constants 1/255 and 0.001 (:53-54), and the output colour is
+ * fma16(T, bg16, c) (:254-259). Every f16 operation here is computed exactly
+ * in double (the operands are multiples of 2^-48 below 2^5) and rounded once.
+ * ------------------------------------------------------------------------- */
+static inline float h16(double x) { return orc_f16_to_f32(orc_f64_to_f16_rne(x)); }
+
+static void composite_tile_f16(const float* U, const uint32_t* pc, const uint32_t* depth,
+                               const uint32_t* counts, const uint32_t* offsets,
+                               const uint32_t* entries, uint32_t tileX, uint32_t tileY, orc_frame* f) {
+  const uint32_t W = (uint32_t)Uf(U, 16), H = (uint32_t)Uf(U, 17);
+  const uint32_t tileId = orc_morton(tileX, tileY);
+  const uint32_t refStart = offsets[tileId], refCount = counts[tileId];
+  const float bg[3] = {h16(0.02), h16(0.02), h16(0.04)};
+  const float alphaTh = h16(1.0 / 255.0), cutoff = h16(0.001);
+  for (uint32_t ly = 0; ly < 8; ++ly)
+    for (uint32_t lx = 0; lx < 8; ++lx) {
+      uint32_t bx = tileX * 16 + lx * 2, by = tileY * 16 + ly * 2;
+      float p00x = (float)bx + 0.5f, p00y = (float)by + 0.5f;
+      float T[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+      float col[4][3] = {{0}}, em[4][3] = {{0}}, nrm[4][3] = {{0}}, mat[4][2] = {{0}};
+      float gbD[4] = {0}, gbW[4] = {0}, gbC[4] = {0};
+      for (uint32_t k = 0; k < refCount; ++k) {
+        uint32_t r = entries[(uint64_t)refStart + k];
+        const uint32_t* c = pc + (uint64_t)r * PROJ_STRIDE;
+        float cx = bitsf(c[0]), cy = bitsf(c[1]);
+        float ka = bitsf(c[2]) * -0.5f, kc = bitsf(c[4]) * -0.5f, kb = -bitsf(c[3]);
+        float op = unpack_hi(c[6]);
+        float sr = unpack_lo(c[9]), sg = unpack_hi(c[9]), sb = unpack_lo(c[10]);
+        float dx0 = p00x - cx, dy0 = p00y - cy;
+        float dxv[4] = {dx0, dx0 + 1.0f, dx0, dx0 + 1.0f};
+        float dyv[4] = {dy0, dy0, dy0 + 1.0f, dy0 + 1.0f};
+        float pw[4];
+        for (int i = 0; i < 4; ++i)
+          pw[i] = fmaf(kc * dyv[i], dyv[i], fmaf(kb * dxv[i], dyv[i], (ka * dxv[i]) * dxv[i]));
+        if (pw[0] <= -4.0f && pw[1] <= -4.0f && pw[2] <= -4.0f && pw[3] <= -4.0f) continue;
+        float sd = bitsf(depth[r]);
+        float mr = unpack_lo(c[5]), mm = unpack_hi(c[5]);
+        v3 sn = oct_decode(unpack_lo(c[8]), unpack_hi(c[8]));
+        float sc = unpack_lo(c[13]);
+        float er = unpack_lo(c[11]), eg = unpack_hi(c[11]), eb = unpack_lo(c[12]);
+        for (int i = 0; i < 4; ++i) {
+          float g = orc_expf(pw[i]);
+          float a32 = fmin_(0.99f, op * g);
+          float a16 = orc_f16_to_f32(orc_f32_to_f16_rne(a32));
+          float nT = h16((double)T[i] * (double)h16(1.0 - (double)a16));
+          int valid = (pw[i] > -4.0f) && (a32 > alphaTh) && (T[i] >= cutoff);
+          float w = valid ? h16((double)a16 * (double)T[i]) : 0.0f;
+          col[i][0] = h16((double)sr * w + col[i][0]);
+          col[i][1] = h16((double)sg * w + col[i][1]);
+          col[i][2] = h16((double)sb * w + col[i][2]);
+          if (valid) T[i] = nT;
+          float gw = w > 0.01f ? w : 0.0f;
+          gbD[i] = fmaf(gw, sd, gbD[i]);
+          gbW[i] = gbW[i] + gw;
+          mat[i][0] = fmaf(mr, gw, mat[i][0]);
+          mat[i][1] = fmaf(mm, gw, mat[i][1]);
+          nrm[i][0] = fmaf(sn.x, gw, nrm[i][0]);
+          nrm[i][1] = fmaf(sn.y, gw, nrm[i][1]);
+          nrm[i][2] = fmaf(sn.z, gw, nrm[i][2]);
+          gbC[i] = fmaf(sc, gw, gbC[i]);
+          em[i][0] = fmaf(er, w, em[i][0]);
+          em[i][1] = fmaf(eg, w, em[i][1]);
+          em[i][2] = fmaf(eb, w, em[i][2]);
+        }
+        if (T[0] < cutoff && T[1] < cutoff && T[2] < cutoff && T[3] < cutoff) break;
+      }
+      for (int i = 0; i < 4; ++i) {
+        uint32_t px = bx + (uint32_t)(i & 1), py = by + (uint32_t)(i >> 1);
+        if (px >= W || py >= H) continue;
+        uint64_t o = (uint64_t)py * W + px;
+        float sw = fmax_(gbW[i], 0.0001f);
+        float ox, oy;
+        oct_encode(norm3(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2])), &ox, &oy);
+        for (int ch = 0; ch < 3; ++ch)
+          f->out_color[o * 4 + ch] = orc_f64_to_f16_rne((double)T[i] * bg[ch] + col[i][ch]);
+        f->out_color[o * 4 + 3] = orc_f32_to_f16_rne(1.0f - T[i]);
+        f->out_depth[o] = gbD[i] / sw;
+        f->out_normal[o] = pack2x16(ox, oy);
+        f->out_material[o * 4 + 0] = pack2x16(mat[i][0] / sw, mat[i][1] / sw);
+        f->out_material[o * 4 + 1] = pack2x16(em[i][0], em[i][1]);
+        f->out_material[o * 4 + 2] = pack2x16(em[i][2], 0.0f);
+        f->out_material[o * 4 + 3] = pack2x16(gbC[i] / sw, 0.0f);
+      }
+    }
+}
+
 void orc_composite(const float* U, const uint32_t* pc, const uint32_t* depth,
                    const uint32_t* counts, const uint32_t* offsets, const uint32_t* entries,
                    orc_frame* f, int threads) {
@@ -847,8 +964,8 @@ void orc_composite(const float* U, const uint32_t* pc, const uint32_t* depth,
   (void)nt;
 #pragma omp parallel for schedule(dynamic, 8) num_threads(nt)
   for (int64_t i = 0; i < (int64_t)cols * rows; ++i)
-    composite_tile(U, pc, depth, counts, offsets, entries, (uint32_t)(i % cols),
-                   (uint32_t)(i / cols), f);
+    (f->composite_f16 ? composite_tile_f16 : composite_tile)(U, pc, depth, counts, offsets, entries,
+                                                            (uint32_t)(i % cols), (uint32_t)(i / cols), f);
 }
 
 /* ---------------------------------------------------------------------------
@@ -1087,6 +1204,7 @@ void orc_logf_n(const float* in, float* out, uint64_t n) { for (uint64_t i = 0; 
 void orc_f16_rne_n(const float* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f32_to_f16_rne(in[i]); }
 void orc_f16_trunc_n(const float* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f32_to_f16_trunc(in[i]); }
 void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f16_to_f32(in[i]); }
+void orc_f64_to_f16_n(const double* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f64_to_f16_rne(in[i]); }
 void orc_morton_n(const uint32_t* x, const uint32_t* y, uint32_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_morton(x[i], y[i]); }
 /* bucket (gpu_tile_bucket_sort.wgsl:250) and k20 of depths against one
  * tile's (min, max) depth bits; used to check bucket == k20 >> 13. */

@@ -98,7 +98,7 @@ typedef struct {
   uint32_t total_chunks;
   uint32_t large_splats;
   uint32_t flags;
-  uint32_t _pad;
+  uint32_t composite_f16;       /* 1: the f16 composite variant (gpu_tile_splat_composite_f16.wgsl) */
   /* outputs, W*H pixels each (may be NULL to skip the composite) */
   uint16_t* out_color;          /* rgba16f, 4 halves per pixel           */
   float* out_depth;             /* r32f                                  */
@@ -110,6 +110,7 @@ typedef struct {
 float orc_expf(float x);
 float orc_logf(float x);
 uint16_t orc_f32_to_f16_rne(float f);     /* pack2x16float rounding */
+uint16_t orc_f64_to_f16_rne(double x);    /* binary16 round-to-nearest-even of a double */
 float orc_f16_to_f32(uint16_t h);
 uint16_t orc_f32_to_f16_trunc(float f);   /* splats.ts:431-442 f32ToF16 */
 uint32_t orc_morton(uint32_t x, uint32_t y);
@@ -162,6 +163,7 @@ void orc_logf_n(const float* in, float* out, uint64_t n);
 void orc_f16_rne_n(const float* in, uint16_t* out, uint64_t n);
 void orc_f16_trunc_n(const float* in, uint16_t* out, uint64_t n);
 void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n);
+void orc_f64_to_f16_n(const double* in, uint16_t* out, uint64_t n);
 
 /* ---- deferred frame tail (hdsr_post_oracle.c) ---- */
 typedef struct orp_inputs {

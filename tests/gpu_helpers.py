@@ -12,7 +12,7 @@ def u32(t):
 
 
 def render_gpu(pkg, scene, cam, W, H, *, f32_color=False, keep_keys=True, pair_capacity=0, order=None,
-               sh_degree=None, tile_entries=False):
+               sh_degree=None, tile_entries=False, f16=False):
     import torch
 
     packed = pkg.splats.pack_splat_attributes(scene)
@@ -22,14 +22,14 @@ def render_gpu(pkg, scene, cam, W, H, *, f32_color=False, keep_keys=True, pair_c
     if order is None:
         order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
     res = pkg.create_tile_splat_compositor(plan, pair_capacity=pair_capacity, f32_color=f32_color,
-                                           keep_sorted_keys=keep_keys, tile_entries=tile_entries)
+                                           keep_sorted_keys=keep_keys, tile_entries=tile_entries, f16=f16)
     bufs = pkg.splats.upload_splat_attribute_buffers(packed, order)
     color, gb = pkg.create_output_textures(plan, f32_color=f32_color)
     pkg.create_tile_splat_bind_groups(res, bufs, color, gb)
     pkg.write_frame_uniform_buffer(res, u)
     pkg.encode_full_compute_compositor_pipeline(None, res)
     torch.cuda.synchronize()
-    return dict(res=res, plan=plan, u=u, packed=packed, order=order, color=color, gb=gb, bufs=bufs)
+    return dict(res=res, plan=plan, u=u, packed=packed, order=order, color=color, gb=gb, bufs=bufs, f16=f16)
 
 
 def read_gpu(g) -> dict:
@@ -76,7 +76,7 @@ def cache_words(gpu: dict) -> np.ndarray:
 def assert_frame_parity(orc, g, gpu=None, check_keys=True):
     """Bit-exact comparison of every stage with the oracle's canonical frame."""
     gpu = gpu or read_gpu(g)
-    ref = orc.render_frame(g["u"], g["packed"], g["order"])
+    ref = orc.render_frame(g["u"], g["packed"], g["order"], f16=g.get("f16", False))
     assert gpu["status"]["status"] == 0, gpu["status"]
     assert gpu["P"] == ref["total_pairs"]
     # projection cache (visible splats: every word; invisible: the sentinel)

@@ -270,6 +270,44 @@ def test_tile_entries_on_demand(cuda, pkg, orc):
     eager["res"].destroy()
 
 
+@pytest.mark.parametrize("f32_color", [False, True])
+def test_f16_composite_variant_parity(cuda, pkg, orc, f32_color):
+    # createTileSplatCompositor {f16: true} (gpu_tile_splat_composite_f16.wgsl):
+    # f16 transmittance and colour, bit-exact against the oracle's f16 variant
+    wl = pkg.workloads.plain50k()
+    g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height, f16=True, f32_color=f32_color)
+    gpu, ref = assert_frame_parity(orc, g)
+    f32 = orc.render_frame(g["u"], g["packed"], g["order"])
+    a = orc.f16_to_f32(f32["color"].reshape(-1))
+    b = orc.f16_to_f32(ref["color"].reshape(-1))
+    # the variant's own error against the f32 composite (f16 transmittance
+    # has 11 significant bits): measured 0.0054 at most on this frame
+    d = np.abs(a - b)
+    assert d.max() > 0 and float(d.max()) <= 2.0 / 255.0 and float(d.mean()) < 1e-3
+    g["res"].destroy()
+
+
+def test_f16_composite_hot_tiles_and_no_adjoint(cuda, pkg, orc):
+    import torch
+
+    scene = _hot_scene(pkg)
+    g = render_gpu(pkg, scene, pkg.camera.look_from((0, 0, 5)), 128, 96, f16=True)
+    assert_frame_parity(orc, g)
+    res = pkg.create_tile_splat_compositor(g["plan"], backward=True, f16=True)
+    pkg.create_tile_splat_bind_groups(res, g["bufs"], g["color"], g["gb"])
+    pkg.write_frame_uniform_buffer(res, g["u"])
+    pkg.encode_full_compute_compositor_pipeline(None, res)
+    torch.cuda.synchronize()
+    n = g["plan"].splat_count
+    grads = {k: torch.zeros(n * w, device="cuda") for k, w in (("positions", 3), ("log_scales", 3), ("rotations", 4),
+                                                              ("opacities", 1), ("sh", 6))}
+    d_color = torch.zeros((g["plan"].viewport_height, g["plan"].viewport_width, 4), device="cuda")
+    with pytest.raises(pkg._lib.HdsrError):
+        pkg.encode_backward(None, res, d_color, grads)
+    res.destroy()
+    g["res"].destroy()
+
+
 def test_overflow_is_reported_not_faulted(cuda, pkg, orc):
     import torch
 

@@ -143,6 +143,26 @@ def test_f16_round_to_nearest_even_matches_ieee(orc):
     assert np.array_equal(orc.f16_to_f32(h)[finite], h.view(np.float16).astype(np.float32)[finite])
 
 
+def test_f64_to_f16_round_to_nearest_even_matches_ieee(orc):
+    # the f16 composite rounds exact double results once: check the rounding
+    # on random doubles and on every f16 midpoint, exactly and a hair off it
+    # (the cases a rounding through f32 first would get wrong)
+    rng = np.random.default_rng(2)
+    h = np.arange(0x7BFF, dtype=np.uint16)
+    a = h.view(np.float16).astype(np.float64)
+    b = (h + 1).view(np.float16).astype(np.float64)
+    m = (a + b) / 2.0
+    x = np.concatenate([m, m * (1 + 2.0 ** -40), m * (1 - 2.0 ** -40), -m, rng.normal(0, 1, 100000),
+                        rng.normal(0, 1e-6, 20000), rng.uniform(-70000, 70000, 20000),
+                        [0.0, -0.0, 65504.0, 65519.99, 65520.0, 1e300, 1e-300, 2.0 ** -24, 2.0 ** -25,
+                         2.0 ** -25 * (1 + 2.0 ** -30), np.inf, -np.inf]])
+    got = orc.f64_to_f16(x)
+    with np.errstate(over="ignore"):
+        ref = x.astype(np.float16).view(np.uint16)
+    assert np.array_equal(got, ref)
+    assert orc.f64_to_f16([np.nan])[0] == 0x7E00
+
+
 def test_f16_truncation_of_host_packer(orc, pkg):
     """f32ToF16 (splats.ts:431-442): restated in C and in numpy, same bits."""
     rng = np.random.default_rng(2)
@@ -289,6 +309,21 @@ def test_superblock_walk_yields_the_tile_lists(small_frame):
             o, n = int(f["tile_offsets"][t]), int(f["tile_counts"][t])
             assert got == f["tile_entries"][o:o + n].tolist(), (tx, ty)
     assert walked_chunks > 0 and skipped > 0
+
+
+def test_f16_composite_variant(small_frame, orc):
+    # gpu_tile_splat_composite_f16.wgsl: same projection and lists; f16
+    # transmittance and colour change the image, within 2/255 of the f32 one
+    f = small_frame["frame"]
+    h = orc.render_frame(small_frame["u"], small_frame["packed"], small_frame["order"], threads=4, f16=True)
+    for k in ("proj_cache", "tile_counts", "tile_offsets", "tile_entries"):
+        assert np.array_equal(h[k], f[k]), k
+    a = orc.f16_to_f32(f["color"].reshape(-1))
+    b = orc.f16_to_f32(h["color"].reshape(-1))
+    d = np.abs(a - b)
+    assert d.max() > 0 and d.max() <= 2.0 / 255.0 and d.mean() < 5e-4
+    # the variant's constants are the f16 roundings of 1/255, 0.001, 0.02, 0.04
+    assert orc.f64_to_f16([1 / 255, 0.001, 0.02, 0.04]).tolist() == [0x1C04, 0x1419, 0x251F, 0x291F]
 
 
 def test_composite_close_to_fp64(small_frame, orc):
