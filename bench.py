@@ -459,6 +459,16 @@ def run_ours(args, rank, world, local):
     e.record(stream)
     e.synchronize()
     sort_ms = s.elapsed_time(e) / args.steps
+    # a static camera: composite only (encodeCompositeOnly) over the last full
+    # frame's lists, the reference's cheap-frame path (gpuTileSplatCompositor.ts:1001-1014)
+    for _ in range(3):
+        pkg.encode_composite_only(stream, res)
+    s.record(stream)
+    for _ in range(args.steps):
+        pkg.encode_composite_only(stream, res)
+    e.record(stream)
+    e.synchronize()
+    composite_only_ms = s.elapsed_time(e) / args.steps
 
     # end to end through the C ABI with host buffers
     log(f"frames timed: {value:.1f} frames/s")
@@ -494,6 +504,7 @@ def run_ours(args, rank, world, local):
         "pass_share": {k: round(v / frame_ms, 4) for k, v in mean_pass.items()},
         "roofline": roofline, "clocks": clocks.summary(t_begin, t_end),
         "gpu_back_to_front_sort_ms": round(sort_ms, 4),
+        "composite_only_ms": round(composite_only_ms, 4),
     }
     if rank == 0 and not args.no_deferred:
         log("deferred tail leg")
