@@ -25,6 +25,26 @@ def test_library_exports_every_declared_symbol(hdsr_lib):
     assert not missing, missing
 
 
+def test_python_mirror_constants_match_the_header(pkg):
+    # status codes, config flags, device flags and buffer ids of the Python
+    # mirror carry the values include/hdsr.h gives them
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "hdsr.h").read_text(), flags=re.S)
+    lib = pkg._lib
+    defines = dict((m[0], int(m[1], 16)) for m in re.findall(r"#define HDSR_((?:CFG|DEV)_\w+)\s+(0x[0-9a-fA-F]+)u", text))
+    assert {"CFG_F16_COMPOSITE", "CFG_TILE_ENTRIES", "CFG_NO_GRAPH", "DEV_OVERFLOW"} <= set(defines)
+    for name, value in defines.items():
+        if hasattr(lib, name):
+            assert getattr(lib, name) == value, name
+    for name in ("CFG_KEEP_SORTED_KEYS", "CFG_NO_GRAPH", "CFG_BACKWARD", "CFG_TILE_ENTRIES", "CFG_F16_COMPOSITE"):
+        assert getattr(lib, name) == defines[name], name
+    enums = dict((m[0], int(m[1])) for m in re.findall(r"\bHDSR_((?:ERR|BUF)_\w+)\s*=\s*(\d+)", text))
+    for name, value in enums.items():
+        if name.startswith("ERR_"):
+            assert getattr(lib, "HDSR_" + name) == value, name
+    buf = {k: v for k, v in enums.items() if k.startswith("BUF_")}
+    assert {("BUF_" + k.upper()): v for k, v in lib.BUFFER_IDS.items()} == buf
+
+
 def test_abi_version(hdsr_lib):
     assert hdsr_lib.hdsr_abi_version() == 1
 
