@@ -131,7 +131,7 @@ struct FrameArgs {
   float2* tile_log;               // (logMin, keyScale)
   // entries
   unsigned long long* sorted_keys;  // optional: tile, 20-bit log-depth key, sortRank per entry
-  uint32_t* entries;              // final per-tile order (sortRank)
+  uint32_t* entries;              // per-tile lists (sortRank), written on demand or with HDSR_CFG_TILE_ENTRIES
   // radix scratch (shared by every pass, passes run in stream order)
   uint32_t* tile_digits;
   uint32_t* bin_base;

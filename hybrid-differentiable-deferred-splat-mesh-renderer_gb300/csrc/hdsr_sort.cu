@@ -11,12 +11,15 @@
 // (Morton tile, depth bits, sortRank), done in two stages:
 //   1. the depth digits on the N splats (depth is per splat): 4 passes of 8
 //      bits over u64 keys depth << 32 | sortRank; the pairs are then emitted
-//      in that depth order (hdsr_project.cu);
+//      in that depth order (hdsr_scan.cu);
 //   2. the tile: the pairs are listed per superblock of 8x8 tiles by one
 //      (two above 256 superblocks) stable 8-bit pass over the superblock
-//      index, and each list is split by tile with a stable count/scan/scatter
-//      over 256-entry segments (k_seg_*), which writes the 1-u32 tile
-//      entries (sortRank).
+//      index. A tile's entries are then its superblock list filtered by the
+//      entries' local rects: the rasterisers walk the lists (k_chunk_masks
+//      marks which 32-entry chunks hold which tiles), and only on demand is
+//      each list split by tile with a stable count/scan/scatter over
+//      256-entry segments (k_seg_*), which writes the 1-u32 per-tile entries
+//      (sortRank).
 // Each pass is reduce-then-scan: an upsweep counts the digits of every block
 // tile of keys, a column scan turns the counts into per-tile digit offsets
 // and digit totals, and a downsweep (which scans the totals into the digits'
