@@ -101,6 +101,29 @@ def test_footprint_clamped_to_eight_tiles(orc, pkg, hdsr_lib):
     assert fr["proj_cache"].shape[1] == GOLDEN["compositor_constants"]["proj_stride_u32"]
 
 
+def test_sh_degree1_follows_the_projection_shader_not_the_cpu_witness(orc, pkg, hdsr_lib):
+    # The inputs of the reference's tests/renderer/shViewlight.test.mjs:9-33
+    # (DC 0.5, degree-1 coefficients, a view from +x and from -x). Its CPU
+    # witness uses the standard 3DGS signs (-C1 y, +C1 z, -C1 x) and asserts
+    # red(+x) > red(-x); gpu_project_splats.wgsl:300-314, which this path
+    # restates, adds +C1 (c0 y + c1 z + c2 x), so red swaps and green stays.
+    C1 = 0.4886025119029199
+    coeffs = np.array([[0.0, 0.0, 0.0, 0.0, 0.6, 0.0, -0.8, 0.0, -0.4]], np.float32)
+    colours = {}
+    for side in (1.0, -1.0):
+        scene = _one_splat_scene(pkg, (0.0, 0.0, 0.0), -2.0, color=(0.5, 0.5, 0.5))
+        scene.sh, scene.sh_degree = coeffs, 1
+        packed = pkg.splats.pack_splat_attributes(scene)
+        u, _ = _uniforms(pkg, 64, 64, 1, pkg.camera.look_from((5.0 * side, 0.0, 0.0)), sh_degree=1)
+        fr = orc.render_frame(u, packed, np.zeros(1, np.uint32), composite=False)
+        w = fr["proj_cache"][0]
+        colours[side] = orc.f16_to_f32(np.array([w[9] & 0xFFFF, w[9] >> 16, w[10] & 0xFFFF], np.uint16))
+    assert colours[1.0][0] < colours[-1.0][0]
+    assert colours[1.0][1] == colours[-1.0][1]
+    # the view direction is camera - centre: +x from the +x camera
+    assert abs(colours[1.0][0] - (0.5 + C1 * -0.8)) < 1e-3 and abs(colours[-1.0][0] - (0.5 - C1 * -0.8)) < 1e-3
+
+
 # --- arithmetic the canonical frame is defined with ------------------------
 
 def test_exp_accuracy(orc):
