@@ -1,6 +1,7 @@
 """The oracle, pinned: the reference's own known-answer vectors, the
 arithmetic it defines, and the frame-level invariants of the canonical order."""
 import json
+import math
 from pathlib import Path
 
 import numpy as np
@@ -122,6 +123,63 @@ def test_sh_degree1_follows_the_projection_shader_not_the_cpu_witness(orc, pkg, 
     assert colours[1.0][1] == colours[-1.0][1]
     # the view direction is camera - centre: +x from the +x camera
     assert abs(colours[1.0][0] - (0.5 + C1 * -0.8)) < 1e-3 and abs(colours[-1.0][0] - (0.5 - C1 * -0.8)) < 1e-3
+
+
+def _witness_rotate_axis(q, axis):
+    """rotateAxisWxyz of the reference's src/rendererFidelityProbes/conicProjection.js:31-50."""
+    n = max(math.sqrt(sum(c * c for c in q)), 1e-6)
+    w, ux, uy, uz = (c / n for c in q)
+    x, y, z = axis
+    cx, cy, cz = uy * z - uz * y, uz * x - ux * z, ux * y - uy * x
+    ix, iy, iz = cx + w * x, cy + w * y, cz + w * z
+    return (x + 2 * (uy * iz - uz * iy), y + 2 * (uz * ix - ux * iz), z + 2 * (ux * iy - uy * ix))
+
+
+def _witness_jacobian_covariance(pos, axes, focal):
+    """referenceJacobianCovariance (conicProjection.js:75-117): J S J^T with the
+    pinhole Jacobian, camera looking down +z, in double."""
+    x, y, z = pos
+    jx = (focal / z, 0.0, -focal * x / (z * z))
+    jy = (0.0, focal / z, -focal * y / (z * z))
+    S = np.zeros((3, 3))
+    for a in axes:
+        S += np.outer(a, a)
+    J = np.array([jx, jy])
+    return J @ S @ J.T
+
+
+def test_projected_covariance_matches_the_reference_jacobian_witness(orc, pkg, hdsr_lib):
+    # The projection's 2D covariance (before the +0.3 low-pass, recovered from
+    # the cache's inverse conic) against the reference's own EWA witness
+    # formula on the same splats: the camera at (0, 0, 5) looks down -z, so a
+    # view-space point (x, y, -d) is the witness's (x, y, d) and axis z flips.
+    rng = np.random.default_rng(11)
+    n = 64
+    pos = np.column_stack([rng.uniform(-1, 1, n), rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)]).astype(np.float32)
+    lsc = rng.uniform(-4.0, -2.0, (n, 3)).astype(np.float32)
+    q = rng.normal(0, 1, (n, 4)).astype(np.float32)
+    scene = pkg.splats.SplatAttributes(positions=pos, scales=lsc, rotations=q,
+                                       opacities=np.full(n, 0.8, np.float32),
+                                       colors=np.full((n, 3), 0.5, np.float32))
+    packed = pkg.splats.pack_splat_attributes(scene)
+    u, fr = _uniforms(pkg, 512, 512, n, pkg.camera.look_from((0.0, 0.0, 5.0)))
+    focal = float(np.float32(u[48]))
+    assert focal == float(np.float32(u[49]))
+    f = orc.render_frame(u, packed, np.arange(n, dtype=np.uint32), composite=False)
+    worst = 0.0
+    for r in range(n):
+        w = f["proj_cache"][r]
+        if w[7] == 0xFFFFFFFF:
+            continue
+        icx, icy, icz = (float(np.uint32(w[k]).view(np.float32)) for k in (2, 3, 4))
+        ours = np.linalg.inv(np.array([[icx, icy], [icy, icz]], np.float64)) - 0.3 * np.eye(2)
+        axes = []
+        for i, e in enumerate(((1, 0, 0), (0, 1, 0), (0, 0, 1))):
+            a = np.array(_witness_rotate_axis(q[r].astype(np.float64), e)) * math.exp(float(lsc[r, i]))
+            axes.append((a[0], a[1], -a[2]))
+        ref = _witness_jacobian_covariance((float(pos[r, 0]), float(pos[r, 1]), 5.0 - float(pos[r, 2])), axes, focal)
+        worst = max(worst, float(np.abs(ours - ref).max() / max(ref[0, 0], ref[1, 1])))
+    assert worst < 1e-4, worst  # measured: 7.9e-7
 
 
 # --- arithmetic the canonical frame is defined with ------------------------
