@@ -487,7 +487,8 @@ def run_ours(args, rank, world, local):
     if dom:
         b = pass_bytes(dom, N, P, Q, S, sh_floats)
         ach = b / (mean_pass[dom] / 1000.0) / 1e9
-        traffic = load_traffic(dom)
+        # the committed ncu table is of the default workload only
+        traffic = load_traffic(dom) if args.workload == "hot760k" else None
         roofline = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(ach / peak, 4), "traffic": traffic,
                     "algorithmic_bytes": int(b), "launch_ms": round(mean_pass[dom], 4),
