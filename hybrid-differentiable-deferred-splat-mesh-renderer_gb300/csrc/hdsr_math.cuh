@@ -149,6 +149,26 @@ HDSR_HD uint32_t pack2x16(float a, float b) { return f32_to_f16(a) | (f32_to_f16
 HDSR_HD float lo16(uint32_t w) { return f16_to_f32(w & 0xFFFFu); }
 HDSR_HD float hi16(uint32_t w) { return f16_to_f32(w >> 16); }
 
+// exp of the composite's power (the rasteriser, its f16 variant and the
+// adjoint): Cody-Waite reduction r = x - k ln2 (|r| <= ln2/2, ln2 split in
+// two), then a degree-5 polynomial in r fitted for least maximum relative
+// error on that interval (this project's own Remez fit: 7.5e-8 in exact
+// arithmetic, at most 2.6 ulp in f32 Horner steps against the true exp on
+// (-4, 0]). A pixel only takes a splat when the power is > -4, so the scale
+// 2^k, k in [-6, 0], is exact in one multiply; below that the value is unused.
+HDSR_HD float composite_expf(float x) {
+  const float k = rintf(x * 1.44269502162933349609375f);
+  float r = fmaf(k, -0.693145751953125f, x);
+  r = fmaf(k, -1.428606765330187045e-06f, r);
+  float p = 0x1.0fe5c6p-7f;
+  p = fmaf(p, r, 0x1.575eeep-5f);
+  p = fmaf(p, r, 0x1.555a18p-3f);
+  p = fmaf(p, r, 0x1.fffd1ap-2f);
+  p = fmaf(p, r, 0x1.fffff6p-1f);
+  p = fmaf(p, r, 0x1.000002p+0f);
+  return p * u2f((uint32_t)((int)k + 127) << 23);
+}
+
 // 16-bit x/y interleave, x on even bits (gpu_tile_splat_composite.wgsl:33-47).
 HDSR_HD uint32_t morton(uint32_t x, uint32_t y) {
   uint32_t a = x & 0xFFFFu;

@@ -85,25 +85,6 @@ __device__ __forceinline__ uint32_t oct_pack_norm(float x, float y, float z) {
   return pack2x16(px, py);
 }
 
-// exp for the rasteriser: a pixel only takes a splat when power > -4, and on
-// (-4, 0] this is hx_expf bit for bit (the scale 2^k, k in [-6, 0], is exact
-// in one multiply); outside that range the value is never used.
-__device__ __forceinline__ float raster_expf(float x) {
-  const float k = rintf(x * 1.44269502162933349609375f);
-  float r = fmaf(k, -0.693145751953125f, x);
-  r = fmaf(k, -1.428606765330187045e-06f, r);
-  float p = 1.98412701e-04f;
-  p = fmaf(p, r, 1.38888892e-03f);
-  p = fmaf(p, r, 8.33333377e-03f);
-  p = fmaf(p, r, 4.16666679e-02f);
-  p = fmaf(p, r, 1.66666672e-01f);
-  p = fmaf(p, r, 0.5f);
-  p = fmaf(p, r, 1.0f);
-  p = fmaf(p, r, 1.0f);
-  const int ki = (int)k;
-  return p * u2f((uint32_t)(ki + 127) << 23);
-}
-
 // The f16 composite variant (gpu_tile_splat_composite_f16.wgsl:53-54, 254):
 // its thresholds and background are f16 constants.
 __device__ __forceinline__ __half h16_bits(unsigned short b) { return __ushort_as_half(b); }
@@ -143,7 +124,7 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
   const bool emits = er != 0.0f || eg != 0.0f || eb != 0.0f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const float g = raster_expf(pw[k]);
+    const float g = composite_expf(pw[k]);
     const float al = mn(0.99f, op * g);
     float w;
     if (F16) {

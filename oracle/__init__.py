@@ -85,7 +85,8 @@ def lib() -> ctypes.CDLL:
         L.orc_sort_back_to_front.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p, c_int]
         L.orc_gpu_sort_prototype_order.restype = c_int
         L.orc_gpu_sort_prototype_order.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p]
-        for nm in ("orc_expf_n", "orc_logf_n", "orc_f16_rne_n", "orc_f16_trunc_n", "orc_f16_to_f32_n", "orc_f64_to_f16_n"):
+        for nm in ("orc_expf_n", "orc_logf_n", "orc_f16_rne_n", "orc_f16_trunc_n", "orc_f16_to_f32_n", "orc_f64_to_f16_n",
+                   "orc_composite_expf_n"):
             getattr(L, nm).argtypes = [c_void_p, c_void_p, c_uint64]
         L.orc_morton_n.argtypes = [c_void_p, c_void_p, c_void_p, c_uint64]
         L.orc_bucket_key20_n.argtypes = [c_void_p, c_uint64, c_uint32, c_uint32, c_void_p, c_void_p]
@@ -259,6 +260,10 @@ def _map(name, x, out_dtype, in_dtype=np.float32):
 
 def expf(x):
     return _map("orc_expf_n", x, np.float32)
+
+
+def composite_expf(x):
+    return _map("orc_composite_expf_n", x, np.float32)
 
 
 def logf(x):

@@ -98,6 +98,23 @@ float orc_logf(float x) {
   return fmaf(fe, LN2_HI, fmaf(fe, LN2_LO, lm));
 }
 
+/* exp of the composite's power, the same steps as the kernels' composite_expf:
+ * Cody-Waite reduction (ln2 in two parts), degree-5 polynomial fitted for least
+ * maximum relative error on |r| <= ln2/2 (own Remez fit), scale 2^k exact for
+ * k in [-6, 0] (the power range a pixel uses, (-4, 0]). */
+float orc_composite_expf(float x) {
+  const float k = rintf(x * 1.44269502162933349609375f);
+  float r = fmaf(k, -0.693145751953125f, x);
+  r = fmaf(k, -1.428606765330187045e-06f, r);
+  float p = 0x1.0fe5c6p-7f;
+  p = fmaf(p, r, 0x1.575eeep-5f);
+  p = fmaf(p, r, 0x1.555a18p-3f);
+  p = fmaf(p, r, 0x1.fffd1ap-2f);
+  p = fmaf(p, r, 0x1.fffff6p-1f);
+  p = fmaf(p, r, 0x1.000002p+0f);
+  return p * bitsf((uint32_t)((int)k + 127) << 23);
+}
+
 /* pack2x16float conversion: IEEE round-to-nearest-even, overflow -> inf,
  * NaN -> 0x7E00 (WGSL leaves NaN undefined; this fixes it). */
 uint16_t orc_f32_to_f16_rne(float f) {
@@ -817,7 +834,7 @@ static void composite_tile(const float* U, const uint32_t* pc, const uint32_t* d
         float sc = unpack_lo(c[13]);
         float er = unpack_lo(c[11]), eg = unpack_hi(c[11]), eb = unpack_lo(c[12]);
         for (int i = 0; i < 4; ++i) {
-          float g = orc_expf(pw[i]);
+          float g = orc_composite_expf(pw[i]);
           float a = fmin_(0.99f, op * g);
           float nT = T[i] * (1.0f - a);
           int valid = (pw[i] > -4.0f) && (a > (1.0f / 255.0f)) && (T[i] >= 0.001f);
@@ -911,7 +928,7 @@ static void composite_tile_f16(const float* U, const uint32_t* pc, const uint32_
         float sc = unpack_lo(c[13]);
         float er = unpack_lo(c[11]), eg = unpack_hi(c[11]), eb = unpack_lo(c[12]);
         for (int i = 0; i < 4; ++i) {
-          float g = orc_expf(pw[i]);
+          float g = orc_composite_expf(pw[i]);
           float a32 = fmin_(0.99f, op * g);
           float a16 = orc_f16_to_f32(orc_f32_to_f16_rne(a32));
           float nT = h16((double)T[i] * (double)h16(1.0 - (double)a16));
@@ -1205,6 +1222,7 @@ void orc_f16_rne_n(const float* in, uint16_t* out, uint64_t n) { for (uint64_t i
 void orc_f16_trunc_n(const float* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f32_to_f16_trunc(in[i]); }
 void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f16_to_f32(in[i]); }
 void orc_f64_to_f16_n(const double* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f64_to_f16_rne(in[i]); }
+void orc_composite_expf_n(const float* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_composite_expf(in[i]); }
 void orc_morton_n(const uint32_t* x, const uint32_t* y, uint32_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_morton(x[i], y[i]); }
 /* bucket (gpu_tile_bucket_sort.wgsl:250) and k20 of depths against one
  * tile's (min, max) depth bits; used to check bucket == k20 >> 13. */

@@ -197,6 +197,16 @@ def test_exp_accuracy(orc):
     assert orc.expf([0.0])[0] == 1.0
 
 
+def test_composite_exp_accuracy(orc):
+    # the composite's exp (degree-5 fit) on the power range a pixel uses
+    x = np.concatenate([np.linspace(-4.0, 0.0, 400001), -np.random.default_rng(5).uniform(0, 4, 200000)]).astype(np.float32)
+    got = orc.composite_expf(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    ulp = np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert np.max(np.abs(got - ref) / ulp) <= 3.0
+    assert orc.composite_expf(np.float32(0.0))[0] == np.float32(1.0) + np.float32(2.0 ** -23)
+
+
 def test_log_accuracy(orc):
     x = np.concatenate([np.geomspace(1e-30, 1e30, 200001), np.linspace(0.5, 2.0, 100001),
                         np.array([1e-6, 1.0, 2.0, 0.5], np.float64)]).astype(np.float32)
