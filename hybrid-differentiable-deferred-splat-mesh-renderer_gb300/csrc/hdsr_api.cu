@@ -537,11 +537,16 @@ static hdsr_status ensure_entries(hdsr_compositor* h, cudaStream_t s) {
 }
 
 // Frames go through the frame graph unless HDSR_CFG_NO_GRAPH, profiling (the
-// per-pass events need direct launches) or a legacy / per-thread default
-// stream (which cannot be captured) says otherwise.
+// per-pass events need direct launches), a legacy / per-thread default
+// stream (which cannot be captured) or a stream the caller is capturing
+// itself (the kernels then go straight into the caller's graph) says
+// otherwise.
 static bool use_graph(const hdsr_compositor* h, cudaStream_t s) {
-  return !(h->cfg.flags & HDSR_CFG_NO_GRAPH) && !h->profiling && s != nullptr && s != cudaStreamLegacy &&
-         s != cudaStreamPerThread;
+  if ((h->cfg.flags & HDSR_CFG_NO_GRAPH) || h->profiling || s == nullptr || s == cudaStreamLegacy ||
+      s == cudaStreamPerThread)
+    return false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone;
 }
 
 // Captures every kernel of a full frame on `s` (nothing runs) into

@@ -72,7 +72,8 @@ typedef struct hdsr_plan {
 #define HDSR_CFG_KEEP_SORTED_KEYS 0x1u  /* compute the 20-bit log-depth keys per entry */
 #define HDSR_CFG_NO_GRAPH         0x2u  /* launch every full frame's kernels directly; otherwise,
                                            on a stream other than the legacy or per-thread
-                                           default stream, the second full frame after a bind is
+                                           default stream and not under the caller's own
+                                           capture, the second full frame after a bind is
                                            captured into a CUDA graph that later frames replay */
 #define HDSR_CFG_BACKWARD         0x4u  /* allocate the adjoint's buffers (hdsr_encode_backward) */
 #define HDSR_CFG_TILE_ENTRIES     0x8u  /* write the per-tile entry lists in every full frame

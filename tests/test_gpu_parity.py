@@ -245,6 +245,33 @@ def test_frame_graph_replays_match_direct_frames(cuda, pkg, orc):
     res.destroy()
 
 
+def test_frame_inside_a_callers_graph_capture(cuda, pkg, orc):
+    # a caller that captures hdsr_encode_full into its own CUDA graph gets the
+    # kernels in its graph (the handle does not start a capture of its own
+    # on a stream that is capturing); replays render the same image
+    import torch
+
+    wl = pkg.workloads.plain50k()
+    g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height)  # one direct frame first
+    res = g["res"]
+    first = read_gpu(g)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            pkg.encode_full_compute_compositor_pipeline(s, res)
+    torch.cuda.synchronize()
+    g["color"].zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    again = read_gpu(g)
+    assert np.array_equal(again["color"].view(np.uint16), first["color"].view(np.uint16))
+    assert np.array_equal(again["material"], first["material"])
+    del graph
+    res.destroy()
+
+
 def test_tile_entries_on_demand(cuda, pkg, orc):
     # The rasteriser reads the superblock lists, so without
     # HDSR_CFG_TILE_ENTRIES / KEEP_SORTED_KEYS a frame writes no per-tile
