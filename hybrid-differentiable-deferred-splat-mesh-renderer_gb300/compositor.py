@@ -123,6 +123,12 @@ class TileSplatCompositorResources:
     def rank_bits(self) -> int:
         return int(self._lib.hdsr_rank_bits(self.handle))
 
+    def chunk_ranges(self):
+        """The hot-tile chunk table of the last full frame (chunkRanges of
+        gpu_tile_bucket_sort.wgsl:276-307), from the tile counts and offsets."""
+        return chunk_ranges_from_tiles(self.buffer("tile_counts").cpu().numpy().view(np.uint32),
+                                       self.buffer("tile_offsets").cpu().numpy().view(np.uint32))
+
     def set_profiling(self, enable: bool = True) -> None:
         _lib.check(self._lib.hdsr_set_profiling(self.handle, 1 if enable else 0), self.handle, "set_profiling")
 
@@ -168,6 +174,21 @@ class _DeviceView:
         import torch
 
         return torch.as_tensor(self, device="cuda")
+
+
+def chunk_ranges_from_tiles(tile_counts, tile_offsets, max_tile_entries: int = 4096) -> np.ndarray:
+    """(start, count) per chunk of every hot tile (more than 4096 entries), in
+    ascending Morton order, as the bucket cascade packs them
+    (gpu_tile_bucket_sort.wgsl:276-307: buckets in order, 4096 entries per
+    chunk, the last one partial). The entries of a tile are already in bucket
+    order at its offset, so chunk k is positions [4096 k, 4096 k + 4096) of it."""
+    counts = np.asarray(tile_counts, np.int64)
+    offsets = np.asarray(tile_offsets, np.int64)
+    rows = []
+    for t in np.nonzero(counts > max_tile_entries)[0]:
+        c, o = int(counts[t]), int(offsets[t])
+        rows.extend((o + k, min(max_tile_entries, c - k)) for k in range(0, c, max_tile_entries))
+    return np.asarray(rows, np.uint32).reshape(-1, 2)
 
 
 def create_tile_splat_compositor(plan: TileSplatCompositorPlan, pair_capacity: int = 0, f32_color: bool = False,

@@ -474,6 +474,20 @@ def test_hot_tile_threshold_and_chunks(orc, pkg, hdsr_lib, n, hot):
             assert max(k_of[x] for x in a.tolist()) <= min(k_of[x] for x in b.tolist())
 
 
+@pytest.mark.parametrize("n", [4097, 9000, 12288])
+def test_chunk_ranges_readback_matches_the_cascade(orc, pkg, hdsr_lib, n):
+    # the chunk table the host derives from tile counts and offsets equals the
+    # oracle's greedy chunk packing of the bucket cascade
+    scene = _stack_scene(pkg, n, pos=(0.72, -0.72, 0.0), depth_jitter=0.5, seed=n)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    u, fr = _uniforms(pkg, 64, 64, n, pkg.camera.look_from((0, 0, 5)))
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order, composite=False)
+    got = pkg.compositor.chunk_ranges_from_tiles(f["tile_counts"], f["tile_offsets"])
+    assert got.shape[0] == f["total_chunks"] == (n + 4095) // 4096
+    assert np.array_equal(got, f["chunk_ranges"])
+
+
 def test_equal_depth_ties_break_by_sort_rank(orc, pkg, hdsr_lib):
     scene = _stack_scene(pkg, 300, pos=(0.72, -0.72, 0.0), depth_jitter=0.0)
     packed = pkg.splats.pack_splat_attributes(scene)
