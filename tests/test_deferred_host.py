@@ -206,3 +206,52 @@ def test_oracle_env_chain_and_bloom_blur(orc, pkg):
     const = np.tile(orc.f16_rne(np.float32([0.5, 0.25, 1.0, 1.0])), (6, 9, 1)).astype(np.uint16)
     out = orc.f16_to_f32(orc.post_bloom_blur(const, 1 / 9, 0.0, 1 / 9, 1 / 6).reshape(-1)).reshape(6, 9, 4)
     np.testing.assert_allclose(out[..., :3], np.broadcast_to([0.5, 0.25, 1.0], (6, 9, 3)), rtol=2e-3)
+
+
+def test_sky_follows_the_reference_lighting_contracts(pkg, orc):
+    # tests/ibl.test.ts:7-27 of the reference (which match shader text):
+    # equirect sampling maps world +Y to the top of the HDR and -Y to its
+    # bottom, and exposure scales the colour before the Reinhard tonemap.
+    # Here as behaviour of the lighting pass on background (sky) pixels: an
+    # environment bright in its top half (4.0) and black in its bottom half.
+    D = pkg.deferred
+    W, H = 40, 32
+    cam = pkg.camera.OrbitCamera(azimuth=0.7, elevation=0.2, distance=3.0)
+    color = np.zeros((H, W, 4), np.float32)
+    depth = np.ones((H, W), np.float32)
+    normal = np.zeros((H, W), np.uint32)
+    material = np.zeros((H, W, 4), np.uint32)
+    inp, keep = orc.post_inputs(color, depth, normal, material)
+    env_img = np.zeros((32, 64, 4), np.float32)
+    env_img[:16, :, :3] = 4.0
+    env_img[..., 3] = 1.0
+    env = orc.post_env_chain(D.f32_to_f16_ibl(env_img.reshape(-1)).reshape(32, 64, 4))
+    ao = np.zeros((H, W, 4), np.uint16)
+    bloom = np.zeros(((H + 1) // 2, (W + 1) // 2, 4), np.uint16)
+    curves = np.stack([orc.post_curve_lut(1, 0, 1)] * 3)
+    # each pixel's world view direction, from the inverse view-projection
+    q = D.frame_params(cam, W, H, env_intensity=1.0, env_rotation=0.0)
+    inv = np.asarray(list(q.view_proj_inverse), np.float64).reshape(4, 4).T
+    ys, xs = np.mgrid[0:H, 0:W]
+    ndc = np.stack([(xs + 0.5) / W * 2 - 1, 1 - (ys + 0.5) / H * 2], -1)
+    near = np.einsum("ij,hwj->hwi", inv, np.concatenate([ndc, np.zeros((H, W, 1)), np.ones((H, W, 1))], -1))
+    far = np.einsum("ij,hwj->hwi", inv, np.concatenate([ndc, np.ones((H, W, 2))], -1))
+    vd = far[..., :3] / far[..., 3:] - near[..., :3] / near[..., 3:]
+    vy = vd[..., 1] / np.linalg.norm(vd, axis=-1)
+    up, down = vy > 0.2, vy < -0.2
+    assert up.sum() > 50 and down.sum() > 50
+    for exposure in (1.0, 2.0):
+        q = D.frame_params(cam, W, H, env_intensity=1.0, env_rotation=0.0, exposure=exposure)
+        lit = orc.post_lighting(inp, q, normal, ao, env, orc.post_brdf_lut(0, 0), bloom, curves)
+        rgb = orc.f16_to_f32(lit.reshape(-1)).reshape(H, W, 4)[..., :3]
+        e = 4.0 * exposure
+        expect = (e / (e + 1.0)) ** (1 / 2.2)
+        assert np.abs(rgb[up] - expect).max() < 2e-3, exposure
+        assert np.all(rgb[down] == 0.0)
+
+
+def test_bilateral_defaults_match_the_reference(pkg):
+    # tests/ibl.test.ts:161-166 of the reference: splatRenderer sets the
+    # bilateral filter's spatialSigma 3.0, normalSigma 1.5, kernelRadius 3
+    q = pkg.deferred.default_params()
+    assert q.bilateral_spatial_sigma == 3.0 and q.bilateral_normal_sigma == 1.5 and q.bilateral_radius == 3
