@@ -417,6 +417,66 @@ def test_f16_composite_variant(small_frame, orc):
     assert orc.f64_to_f16([1 / 255, 0.001, 0.02, 0.04]).tolist() == [0x1C04, 0x1419, 0x251F, 0x291F]
 
 
+def test_f16_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
+    # gpu_tile_splat_composite_f16.wgsl:186-259 once more, vectorised over the
+    # pixels of a tile with numpy float16 roundings, against the C oracle's
+    # colour bits. An entry invalid for a pixel leaves it unchanged (w = 0),
+    # so the quad skip and the early exit of the shader need no restating.
+    # f32 fused multiply-adds are emulated in double (exact products; a
+    # double rounding of the sum is the only, vanishingly rare, difference).
+    scene = pkg.workloads.plain_scene(600, seed=21)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    cam = pkg.camera.look_from((0.3, 0.2, 3.5))
+    W = H = 64
+    u, fr = _uniforms(pkg, W, H, scene.count, cam)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order, threads=2, f16=True)
+    pc = f["proj_cache"]
+    # (far below the support, where the exp's value is unused, it may overflow)
+    h16 = lambda v: np.asarray(v, np.float64).astype(np.float16).astype(np.float64)  # noqa: E731
+    fma32 = lambda a, b, c: (np.float64(a) * b + c).astype(np.float32)  # noqa: E731
+    th, cut = h16(1.0 / 255.0), h16(0.001)
+    bg = h16([0.02, 0.02, 0.04])
+    got = orc.f16_to_f32(f["color"].reshape(-1)).reshape(H, W, 4)
+    prev = np.seterr(over="ignore")
+    try:
+        _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H)
+    finally:
+        np.seterr(**prev)
+
+
+def _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H):
+    for ty in range(H // 16):
+        for tx in range(W // 16):
+            t = _morton(tx, ty)
+            ents = f["tile_entries"][f["tile_offsets"][t]: f["tile_offsets"][t] + f["tile_counts"][t]]
+            ys, xs = np.mgrid[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16]
+            px, py = (xs + 0.5).astype(np.float32), (ys + 0.5).astype(np.float32)
+            T = np.ones((16, 16))
+            col = np.zeros((16, 16, 3))
+            for r in ents.tolist():
+                w = pc[r]
+                cx, cy, ia, ib, ic = (np.uint32(w[k]).view(np.float32) for k in range(5))
+                ka, kb, kc = np.float32(ia * np.float32(-0.5)), np.float32(-ib), np.float32(ic * np.float32(-0.5))
+                op = orc.f16_to_f32(np.array([w[6] >> 16], np.uint16))[0]
+                rgb = orc.f16_to_f32(np.array([w[9] & 0xFFFF, w[9] >> 16, w[10] & 0xFFFF], np.uint16)).astype(np.float64)
+                dx, dy = (px - cx).astype(np.float32), (py - cy).astype(np.float32)
+                pw = fma32((kc * dy).astype(np.float32), dy, fma32((kb * dx).astype(np.float32), dy,
+                                                                   ((ka * dx).astype(np.float32) * dx).astype(np.float32)))
+                g = orc.composite_expf(pw).reshape(16, 16)
+                a32 = np.minimum(np.float32(0.99), (op * g).astype(np.float32))
+                a16 = h16(a32)
+                valid = (pw > -4.0) & (a32 > th) & (T >= cut)
+                nT = h16(T * h16(1.0 - a16))
+                w16 = np.where(valid, h16(a16 * T), 0.0)
+                col = h16(rgb[None, None, :] * w16[..., None] + col)
+                T = np.where(valid, nT, T)
+            out = h16(T[..., None] * bg[None, None, :] + col)
+            assert np.array_equal(out.astype(np.float32), got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, :3]), (tx, ty)
+            alpha = (np.float32(1.0) - T.astype(np.float32)).astype(np.float16).astype(np.float32)
+            assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
+
+
 def test_composite_close_to_fp64(small_frame, orc):
     f = small_frame["frame"]
     img = orc.f16_to_f32(f["color"].reshape(-1)).reshape(f["H"], f["W"], 4).astype(np.float64)
