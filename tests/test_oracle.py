@@ -477,6 +477,56 @@ def _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H):
             assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
 
 
+def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
+    # gpu_tile_splat_composite.wgsl:162-370 (the canonical f32 form: fused
+    # power and accumulations) restated with numpy over the pixels of each
+    # tile, against the C oracle's colour and alpha bits (see the f16 test for
+    # why the quad skip and early exit need no restating).
+    scene = pkg.workloads.plain_scene(600, seed=22)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    cam = pkg.camera.look_from((-0.2, 0.3, 3.5))
+    W = H = 64
+    u, fr = _uniforms(pkg, W, H, scene.count, cam)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+    f = orc.render_frame(u, packed, order, threads=2)
+    pc = f["proj_cache"]
+    got = orc.f16_to_f32(f["color"].reshape(-1)).reshape(H, W, 4)
+    fma32 = lambda a, b, c: (np.asarray(a, np.float64) * b + c).astype(np.float32)  # noqa: E731
+    bg = np.array([0.02, 0.02, 0.04], np.float32)
+    prev = np.seterr(over="ignore", invalid="ignore")
+    try:
+        for ty in range(H // 16):
+            for tx in range(W // 16):
+                t = _morton(tx, ty)
+                ents = f["tile_entries"][f["tile_offsets"][t]: f["tile_offsets"][t] + f["tile_counts"][t]]
+                ys, xs = np.mgrid[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16]
+                px, py = (xs + 0.5).astype(np.float32), (ys + 0.5).astype(np.float32)
+                T = np.ones((16, 16), np.float32)
+                col = np.zeros((16, 16, 3), np.float32)
+                for r in ents.tolist():
+                    w = pc[r]
+                    cx, cy, ia, ib, ic = (np.uint32(w[k]).view(np.float32) for k in range(5))
+                    ka, kb, kc = np.float32(ia * np.float32(-0.5)), np.float32(-ib), np.float32(ic * np.float32(-0.5))
+                    op = orc.f16_to_f32(np.array([w[6] >> 16], np.uint16))[0]
+                    rgb = orc.f16_to_f32(np.array([w[9] & 0xFFFF, w[9] >> 16, w[10] & 0xFFFF], np.uint16))
+                    dx, dy = (px - cx).astype(np.float32), (py - cy).astype(np.float32)
+                    pw = fma32((kc * dy).astype(np.float32), dy, fma32((kb * dx).astype(np.float32), dy,
+                                                                       ((ka * dx).astype(np.float32) * dx).astype(np.float32)))
+                    g = orc.composite_expf(pw).reshape(16, 16)
+                    al = np.minimum(np.float32(0.99), (op * g).astype(np.float32))
+                    nT = (T * (np.float32(1.0) - al).astype(np.float32)).astype(np.float32)
+                    valid = (pw > -4.0) & (al > np.float32(1.0) / np.float32(255.0)) & (T >= np.float32(0.001))
+                    wt = np.where(valid, (al * T).astype(np.float32), np.float32(0.0))
+                    col = fma32(rgb[None, None, :], wt[..., None], col)
+                    T = np.where(valid, nT, T)
+                out = fma32(T[..., None], bg[None, None, :], col).astype(np.float16).astype(np.float32)
+                assert np.array_equal(out, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, :3]), (tx, ty)
+                alpha = (np.float32(1.0) - T).astype(np.float16).astype(np.float32)
+                assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
+    finally:
+        np.seterr(**prev)
+
+
 def test_composite_close_to_fp64(small_frame, orc):
     f = small_frame["frame"]
     img = orc.f16_to_f32(f["color"].reshape(-1)).reshape(f["H"], f["W"], 4).astype(np.float64)
