@@ -477,6 +477,93 @@ def _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H):
             assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
 
 
+def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
+    # project_splats (gpu_project_splats.wgsl:112-232) restated with numpy f32
+    # arithmetic, one rounding per operation, sums left to right (the
+    # canonical form), the compositor's own exp: centre, depth, inverse
+    # conic, f16 (radius, opacity) and the tile box, bit for bit against the
+    # C oracle; splats behind the camera get the sentinel
+    scene = pkg.workloads.plain_scene(3000, seed=23)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    cam = pkg.camera.look_from((0.4, 0.3, 2.0))
+    W, H = 320, 240
+    u, fr = _uniforms(pkg, W, H, scene.count, cam)
+    order = np.arange(scene.count, dtype=np.uint32)
+    f = orc.render_frame(u, packed, order, threads=2, composite=False)
+    U = np.asarray(u, np.float32)
+    f32 = np.float32
+    P = packed.positions.reshape(-1, 3).astype(f32)
+    x, y, z = P[:, 0], P[:, 1], P[:, 2]
+    clip = [((U[0 + r] * x + U[4 + r] * y) + U[8 + r] * z) + U[12 + r] * f32(1.0) for r in range(4)]
+    vis = clip[3] > 0
+    safeW = np.maximum(clip[3], f32(0.0001))
+    ndcx, ndcy = clip[0] / safeW, clip[1] / safeW
+    cpx = (ndcx * f32(0.5) + f32(0.5)) * U[16]
+    cpy = (f32(1.0) - (ndcy * f32(0.5) + f32(0.5))) * U[17]
+    depth = clip[2] / safeW
+    sl = packed.scales.reshape(-1, 3).astype(f32)
+    q = packed.rotations.reshape(-1, 4).astype(f32)
+    scale = [orc.expf(sl[:, k]) * U[24] for k in range(3)]
+    qn = q / np.maximum(np.sqrt(((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]) + q[:, 2] * q[:, 2]) + q[:, 3] * q[:, 3]),
+                        f32(0.000001))[:, None]
+    ux, uy, uz, qw = qn[:, 1], qn[:, 2], qn[:, 3], qn[:, 0]
+
+    def cross(a, b):
+        return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+    def dot(a, b):
+        return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
+
+    axes = []
+    for k, e in enumerate(((1, 0, 0), (0, 1, 0), (0, 0, 1))):
+        ev = tuple(np.full_like(x, f32(c)) for c in e)
+        cu = cross((ux, uy, uz), ev)
+        inner = tuple(cu[i] + qw * ev[i] for i in range(3))
+        c2 = cross((ux, uy, uz), inner)
+        axes.append(tuple((ev[i] + f32(2.0) * c2[i]) * scale[k] for i in range(3)))
+    vc = [((U[32 + r] * x + U[36 + r] * y) + U[40 + r] * z) + U[44 + r] * f32(1.0) for r in range(3)]
+    vz = np.minimum(vc[2], f32(-0.001))
+    J1x, J1y = U[48] / vz, U[49] / vz
+    J2x, J2y = (-J1x / vz) * vc[0], (-J1y / vz) * vc[1]
+    w0, w1, w2 = (U[32], U[36], U[40]), (U[33], U[37], U[41]), (U[34], U[38], U[42])
+    tt0 = tuple(J1x * w0[i] + J2x * w2[i] for i in range(3))
+    tt1 = tuple(J1y * w1[i] + J2y * w2[i] for i in range(3))
+    b0 = tuple(dot(a, tt0) for a in axes)
+    b1 = tuple(dot(a, tt1) for a in axes)
+    cxx, cxy, cyy = dot(b0, b0), dot(b0, b1), dot(b1, b1)
+    detO = cxx * cyy - cxy * cxy
+    cXX, cYY = cxx + f32(0.3), cyy + f32(0.3)
+    detB = cXX * cYY - cxy * cxy
+    aa = np.sqrt(np.maximum(detO / np.maximum(detB, f32(0.000001)), f32(0.0)))
+    mid = f32(0.5) * (cXX + cYY)
+    lam = mid + np.sqrt(np.maximum(mid * mid - np.maximum(detB, f32(0.1)), f32(0.1)))
+    radius = np.ceil(f32(3.0) * np.sqrt(lam))
+    vis &= radius > 0
+    dinv = f32(1.0) / np.maximum(detB, f32(0.000001))
+    ic = (cYY * dinv, -cxy * dinv, cXX * dinv)
+    op = np.clip(packed.opacities.astype(f32) * aa, f32(0.0), f32(0.99))
+    ts = np.maximum(U[18], f32(1.0))
+    gx, gy = (int(np.asarray(U[20:22], np.float32).view(np.uint32)[k]) for k in range(2))
+    cr = np.minimum(radius, ts * f32(8.0))
+    lo = (np.maximum(cpx - cr, f32(0.0)), np.maximum(cpy - cr, f32(0.0)))
+    hi = (np.minimum(cpx + cr, U[16]), np.minimum(cpy + cr, U[17]))
+    sat = lambda v, m: np.minimum(np.clip(np.floor(v), 0, 2.0 ** 32 - 1).astype(np.uint64), m)  # noqa: E731
+    t0x, t0y = sat(lo[0] / ts, max(gx, 1) - 1), sat(lo[1] / ts, max(gy, 1) - 1)
+    t1x = sat(np.maximum((hi[0] - f32(0.000000001)) / ts, f32(0.0)), max(gx, 1) - 1)
+    t1y = sat(np.maximum((hi[1] - f32(0.000000001)) / ts, f32(0.0)), max(gy, 1) - 1)
+    box = (t0x & 0xFF) | ((t0y & 0xFF) << 8) | ((t1x & 0xFF) << 16) | ((t1y & 0xFF) << 24)
+    pc = f["proj_cache"]
+    bits = lambda v: np.asarray(v, np.float32).view(np.uint32)  # noqa: E731
+    assert vis.sum() > 1000 and (~vis).sum() > 0
+    assert np.all(pc[~vis, 7] == 0xFFFFFFFF)
+    for word, val in ((0, cpx), (1, cpy), (2, ic[0]), (3, ic[1]), (4, ic[2])):
+        assert np.array_equal(pc[vis, word], bits(val)[vis]), word
+    assert np.array_equal(f["depth"][vis], bits(depth)[vis])
+    packed6 = orc.f16_rne(radius).astype(np.uint32) | (orc.f16_rne(op).astype(np.uint32) << 16)
+    assert np.array_equal(pc[vis, 6], packed6[vis])
+    assert np.array_equal(pc[vis, 7], box.astype(np.uint32)[vis])
+
+
 def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
     # gpu_tile_splat_composite.wgsl:162-370 (the canonical f32 form: fused
     # power and accumulations) restated with numpy over the pixels of each
