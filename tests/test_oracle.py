@@ -564,11 +564,37 @@ def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, 
     assert np.array_equal(pc[vis, 7], box.astype(np.uint32)[vis])
 
 
+def _oct_decode_np(e):
+    """octDecode (gpu_tile_splat_composite.wgsl:143-149) on one f16 pair, f32 steps."""
+    f32 = np.float32
+    x, y = f32(e[0]), f32(e[1])
+    z = (f32(1.0) - abs(x)) - abs(y)
+    if z < 0:
+        x, y = (f32(1.0) - abs(y)) * (f32(1.0) if x >= 0 else f32(-1.0)), (f32(1.0) - abs(x)) * (f32(1.0) if y >= 0 else f32(-1.0))
+    ln = np.sqrt((x * x + y * y) + z * z)
+    return np.array([x / ln, y / ln, z / ln], np.float32)
+
+
+def _oct_encode_np(v):
+    """octEncode(normalize(v)) (gpu_tile_splat_composite.wgsl:134-141), vectorised, f32 steps."""
+    f32 = np.float32
+    x, y, z = v[..., 0], v[..., 1], v[..., 2]
+    ln = np.sqrt((x * x + y * y) + z * z)
+    x, y, z = x / ln, y / ln, z / ln
+    s = (np.abs(x) + np.abs(y)) + np.abs(z)
+    px, py = x / s, y / s
+    sx, sy = np.where(px >= 0, f32(1.0), f32(-1.0)), np.where(py >= 0, f32(1.0), f32(-1.0))
+    nx, ny = (f32(1.0) - np.abs(py)) * sx, (f32(1.0) - np.abs(px)) * sy
+    neg = z < 0
+    return np.where(neg, nx, px).astype(np.float32), np.where(neg, ny, py).astype(np.float32)
+
+
 def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
-    # gpu_tile_splat_composite.wgsl:162-370 (the canonical f32 form: fused
+    # gpu_tile_splat_composite.wgsl:134-370 (the canonical f32 form: fused
     # power and accumulations) restated with numpy over the pixels of each
-    # tile, against the C oracle's colour and alpha bits (see the f16 test for
-    # why the quad skip and early exit need no restating).
+    # tile, against the C oracle's colour, alpha, depth, normal and material
+    # bits (see the f16 test for why the quad skip and early exit need no
+    # restating).
     scene = pkg.workloads.plain_scene(600, seed=22)
     packed = pkg.splats.pack_splat_attributes(scene)
     cam = pkg.camera.look_from((-0.2, 0.3, 3.5))
@@ -590,6 +616,8 @@ def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_l
                 px, py = (xs + 0.5).astype(np.float32), (ys + 0.5).astype(np.float32)
                 T = np.ones((16, 16), np.float32)
                 col = np.zeros((16, 16, 3), np.float32)
+                gd, gW, gc = (np.zeros((16, 16), np.float32) for _ in range(3))
+                mat, nrm, em = np.zeros((16, 16, 2), np.float32), np.zeros((16, 16, 3), np.float32), np.zeros((16, 16, 3), np.float32)
                 for r in ents.tolist():
                     w = pc[r]
                     cx, cy, ia, ib, ic = (np.uint32(w[k]).view(np.float32) for k in range(5))
@@ -606,10 +634,35 @@ def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_l
                     wt = np.where(valid, (al * T).astype(np.float32), np.float32(0.0))
                     col = fma32(rgb[None, None, :], wt[..., None], col)
                     T = np.where(valid, nT, T)
+                    gw = np.where(wt > np.float32(0.01), wt, np.float32(0.0))
+                    sd = np.uint32(f["depth"][r]).view(np.float32)
+                    mr = orc.f16_to_f32(np.array([w[5] & 0xFFFF, w[5] >> 16], np.uint16))
+                    sn = _oct_decode_np(orc.f16_to_f32(np.array([w[8] & 0xFFFF, w[8] >> 16], np.uint16)))
+                    sc = orc.f16_to_f32(np.array([w[13] & 0xFFFF], np.uint16))[0]
+                    er = orc.f16_to_f32(np.array([w[11] & 0xFFFF, w[11] >> 16, w[12] & 0xFFFF], np.uint16))
+                    gd = fma32(gw, sd, gd)
+                    gW = (gW + gw).astype(np.float32)
+                    mat = fma32(mr[None, None, :], gw[..., None], mat)
+                    nrm = fma32(sn[None, None, :], gw[..., None], nrm)
+                    gc = fma32(sc, gw, gc)
+                    em = fma32(er[None, None, :], wt[..., None], em)
                 out = fma32(T[..., None], bg[None, None, :], col).astype(np.float16).astype(np.float32)
                 assert np.array_equal(out, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, :3]), (tx, ty)
                 alpha = (np.float32(1.0) - T).astype(np.float16).astype(np.float32)
                 assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
+                sw = np.maximum(gW, np.float32(0.0001))
+                sl = np.s_[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16]
+                assert np.array_equal((gd / sw).astype(np.float32), f["out_depth"][sl]), (tx, ty)
+                nn = nrm + np.array([0.0, 0.0001, 0.0], np.float32)
+                ox, oy = _oct_encode_np(nn)
+                pk = lambda a, b: orc.f16_rne(a.reshape(-1)).astype(np.uint32) | (orc.f16_rne(b.reshape(-1)).astype(np.uint32) << 16)  # noqa: E731
+                assert np.array_equal(pk(ox, oy), f["normal"][sl].reshape(-1)), (tx, ty)
+                zero = np.zeros((16, 16), np.float32)
+                m = f["material"][sl].reshape(-1, 4)
+                assert np.array_equal(pk((mat[..., 0] / sw).astype(np.float32), (mat[..., 1] / sw).astype(np.float32)), m[:, 0])
+                assert np.array_equal(pk(em[..., 0], em[..., 1]), m[:, 1])
+                assert np.array_equal(pk(em[..., 2], zero), m[:, 2])
+                assert np.array_equal(pk((gc / sw).astype(np.float32), zero), m[:, 3])
     finally:
         np.seterr(**prev)
 
