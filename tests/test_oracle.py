@@ -478,11 +478,11 @@ def _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H):
 
 
 def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
-    # project_splats (gpu_project_splats.wgsl:112-232) restated with numpy f32
+    # project_splats (gpu_project_splats.wgsl:112-357) restated with numpy f32
     # arithmetic, one rounding per operation, sums left to right (the
-    # canonical form), the compositor's own exp: centre, depth, inverse
-    # conic, f16 (radius, opacity) and the tile box, bit for bit against the
-    # C oracle; splats behind the camera get the sentinel
+    # canonical form), the projection's own exp: every word of the cache row
+    # and the depth, bit for bit against the C oracle; splats behind the
+    # camera get the sentinel
     scene = pkg.workloads.plain_scene(3000, seed=23)
     packed = pkg.splats.pack_splat_attributes(scene)
     cam = pkg.camera.look_from((0.4, 0.3, 2.0))
@@ -562,6 +562,37 @@ def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, 
     packed6 = orc.f16_rne(radius).astype(np.uint32) | (orc.f16_rne(op).astype(np.uint32) << 16)
     assert np.array_equal(pc[vis, 6], packed6[vis])
     assert np.array_equal(pc[vis, 7], box.astype(np.uint32)[vis])
+    # the rest of the row (:233-357): covariance normal (no baked normals in
+    # this scene), face-forward, confidence, lighting-frame oct normal; SH
+    # degree 0 colour; emissive and material pass-through
+    assert packed.normals is None and scene.sh_degree == 0
+
+    def norm(v):
+        ln = np.sqrt(dot(v, v))
+        return tuple(c / ln for c in v)
+
+    lens = [dot(a, a) for a in axes]
+    mn = np.minimum(lens[0], np.minimum(lens[1], lens[2]))
+    pick = lambda i: np.where(lens[0] == mn, axes[0][i], np.where(lens[1] == mn, axes[1][i], axes[2][i]))  # noqa: E731
+    local = norm(tuple(pick(i) for i in range(3)))
+    nvd = norm(tuple(U[28 + i] - P[:, i] for i in range(3)))
+    fn, fv = norm(local), norm(nvd)
+    flip = dot(fn, fv) < 0
+    faced = tuple(np.where(flip, -c, c) for c in fn)
+    conf = np.clip(dot(faced, nvd), f32(0.0), f32(1.0))
+    wn = norm(tuple((U[52 + k] * faced[0] + U[56 + k] * faced[1]) + U[60 + k] * faced[2] for k in range(3)))
+    ox, oy = _oct_encode_np(np.stack(wn, -1), normalize=False)
+    pk = lambda a, b: orc.f16_rne(a).astype(np.uint32) | (orc.f16_rne(b).astype(np.uint32) << 16)  # noqa: E731
+    zero = np.zeros_like(x)
+    assert np.array_equal(pc[vis, 8], pk(ox, oy)[vis])
+    assert np.array_equal(pc[vis, 13], pk(conf, zero)[vis])
+    sh = packed.sh_data.reshape(scene.count, -1).astype(f32)
+    rgb = np.clip(sh[:, 0:3], f32(0.0), f32(1.0))
+    assert np.array_equal(pc[vis, 9], pk(rgb[:, 0], rgb[:, 1])[vis])
+    assert np.array_equal(pc[vis, 10], pk(rgb[:, 2], zero)[vis])
+    assert np.array_equal(pc[vis, 11], pk(sh[:, 3], sh[:, 4])[vis])
+    assert np.array_equal(pc[vis, 12], pk(sh[:, 5], zero)[vis])
+    assert np.array_equal(pc[vis, 5], packed.material.reshape(-1)[vis])
 
 
 def _oct_decode_np(e):
@@ -575,12 +606,14 @@ def _oct_decode_np(e):
     return np.array([x / ln, y / ln, z / ln], np.float32)
 
 
-def _oct_encode_np(v):
-    """octEncode(normalize(v)) (gpu_tile_splat_composite.wgsl:134-141), vectorised, f32 steps."""
+def _oct_encode_np(v, normalize=True):
+    """octEncode(normalize(v)) (gpu_tile_splat_composite.wgsl:134-141), or octEncode(v)
+    for an already unit v, vectorised, f32 steps."""
     f32 = np.float32
     x, y, z = v[..., 0], v[..., 1], v[..., 2]
-    ln = np.sqrt((x * x + y * y) + z * z)
-    x, y, z = x / ln, y / ln, z / ln
+    if normalize:
+        ln = np.sqrt((x * x + y * y) + z * z)
+        x, y, z = x / ln, y / ln, z / ln
     s = (np.abs(x) + np.abs(y)) + np.abs(z)
     px, py = x / s, y / s
     sx, sy = np.where(px >= 0, f32(1.0), f32(-1.0)), np.where(py >= 0, f32(1.0), f32(-1.0))
