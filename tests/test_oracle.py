@@ -477,23 +477,33 @@ def _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H):
             assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
 
 
-def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
-    # project_splats (gpu_project_splats.wgsl:112-357) restated with numpy f32
-    # arithmetic, one rounding per operation, sums left to right (the
-    # canonical form), the projection's own exp: every word of the cache row
-    # and the depth, bit for bit against the C oracle; splats behind the
-    # camera get the sentinel
-    scene = pkg.workloads.plain_scene(3000, seed=23)
-    packed = pkg.splats.pack_splat_attributes(scene)
-    cam = pkg.camera.look_from((0.4, 0.3, 2.0))
-    W, H = 320, 240
-    u, fr = _uniforms(pkg, W, H, scene.count, cam)
-    order = np.arange(scene.count, dtype=np.uint32)
-    f = orc.render_frame(u, packed, order, threads=2, composite=False)
-    U = np.asarray(u, np.float32)
+def _np_project(orc, U, packed, n):
+    """See _np_project_body; branches the shader does not take may divide by
+    zero in the vectorised form (their values are discarded)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return _np_project_body(orc, U, packed, n)
+
+
+def _np_project_body(orc, U, packed, n):
+    """project_splats (gpu_project_splats.wgsl:112-357) restated with numpy f32
+    arithmetic for splat ids 0..n-1 in order: one rounding per operation, sums
+    left to right (the canonical form), the projection's own exp. Returns the
+    expected cache words, depth and the visibility mask."""
     f32 = np.float32
+    U = np.asarray(U, np.float32)
     P = packed.positions.reshape(-1, 3).astype(f32)
     x, y, z = P[:, 0], P[:, 1], P[:, 2]
+
+    def dot(a, b):
+        return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
+
+    def cross(a, b):
+        return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+    def norm(v):
+        ln = np.sqrt(dot(v, v))
+        return tuple(c / ln for c in v)
+
     clip = [((U[0 + r] * x + U[4 + r] * y) + U[8 + r] * z) + U[12 + r] * f32(1.0) for r in range(4)]
     vis = clip[3] > 0
     safeW = np.maximum(clip[3], f32(0.0001))
@@ -506,20 +516,12 @@ def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, 
     scale = [orc.expf(sl[:, k]) * U[24] for k in range(3)]
     qn = q / np.maximum(np.sqrt(((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]) + q[:, 2] * q[:, 2]) + q[:, 3] * q[:, 3]),
                         f32(0.000001))[:, None]
-    ux, uy, uz, qw = qn[:, 1], qn[:, 2], qn[:, 3], qn[:, 0]
-
-    def cross(a, b):
-        return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
-
-    def dot(a, b):
-        return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
-
+    u3, qw = (qn[:, 1], qn[:, 2], qn[:, 3]), qn[:, 0]
     axes = []
     for k, e in enumerate(((1, 0, 0), (0, 1, 0), (0, 0, 1))):
         ev = tuple(np.full_like(x, f32(c)) for c in e)
-        cu = cross((ux, uy, uz), ev)
-        inner = tuple(cu[i] + qw * ev[i] for i in range(3))
-        c2 = cross((ux, uy, uz), inner)
+        cu = cross(u3, ev)
+        c2 = cross(u3, tuple(cu[i] + qw * ev[i] for i in range(3)))
         axes.append(tuple((ev[i] + f32(2.0) * c2[i]) * scale[k] for i in range(3)))
     vc = [((U[32 + r] * x + U[36 + r] * y) + U[40 + r] * z) + U[44 + r] * f32(1.0) for r in range(3)]
     vz = np.minimum(vc[2], f32(-0.001))
@@ -528,8 +530,7 @@ def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, 
     w0, w1, w2 = (U[32], U[36], U[40]), (U[33], U[37], U[41]), (U[34], U[38], U[42])
     tt0 = tuple(J1x * w0[i] + J2x * w2[i] for i in range(3))
     tt1 = tuple(J1y * w1[i] + J2y * w2[i] for i in range(3))
-    b0 = tuple(dot(a, tt0) for a in axes)
-    b1 = tuple(dot(a, tt1) for a in axes)
+    b0, b1 = tuple(dot(a, tt0) for a in axes), tuple(dot(a, tt1) for a in axes)
     cxx, cxy, cyy = dot(b0, b0), dot(b0, b1), dot(b1, b1)
     detO = cxx * cyy - cxy * cxy
     cXX, cYY = cxx + f32(0.3), cyy + f32(0.3)
@@ -552,47 +553,131 @@ def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, 
     t1x = sat(np.maximum((hi[0] - f32(0.000000001)) / ts, f32(0.0)), max(gx, 1) - 1)
     t1y = sat(np.maximum((hi[1] - f32(0.000000001)) / ts, f32(0.0)), max(gy, 1) - 1)
     box = (t0x & 0xFF) | ((t0y & 0xFF) << 8) | ((t1x & 0xFF) << 16) | ((t1y & 0xFF) << 24)
-    pc = f["proj_cache"]
-    bits = lambda v: np.asarray(v, np.float32).view(np.uint32)  # noqa: E731
-    assert vis.sum() > 1000 and (~vis).sum() > 0
-    assert np.all(pc[~vis, 7] == 0xFFFFFFFF)
-    for word, val in ((0, cpx), (1, cpy), (2, ic[0]), (3, ic[1]), (4, ic[2])):
-        assert np.array_equal(pc[vis, word], bits(val)[vis]), word
-    assert np.array_equal(f["depth"][vis], bits(depth)[vis])
-    packed6 = orc.f16_rne(radius).astype(np.uint32) | (orc.f16_rne(op).astype(np.uint32) << 16)
-    assert np.array_equal(pc[vis, 6], packed6[vis])
-    assert np.array_equal(pc[vis, 7], box.astype(np.uint32)[vis])
-    # the rest of the row (:233-357): covariance normal (no baked normals in
-    # this scene), face-forward, confidence, lighting-frame oct normal; SH
-    # degree 0 colour; emissive and material pass-through
-    assert packed.normals is None and scene.sh_degree == 0
-
-    def norm(v):
-        ln = np.sqrt(dot(v, v))
-        return tuple(c / ln for c in v)
-
+    # normals (:233-291)
     lens = [dot(a, a) for a in axes]
     mn = np.minimum(lens[0], np.minimum(lens[1], lens[2]))
     pick = lambda i: np.where(lens[0] == mn, axes[0][i], np.where(lens[1] == mn, axes[1][i], axes[2][i]))  # noqa: E731
-    local = norm(tuple(pick(i) for i in range(3)))
+    sn = norm(tuple(pick(i) for i in range(3)))
+    nd = np.zeros(0, f32) if packed.normals is None else packed.normals.reshape(-1).astype(f32)
+    if nd.size >= 3 * n:
+        bk = (nd[0:3 * n:3], nd[1:3 * n:3], nd[2:3 * n:3])
+        bl = np.sqrt(dot(bk, bk))
+        sn = tuple(np.where(bl > f32(0.001), bk[i] / bl, sn[i]) for i in range(3))
+    if nd.size >= 6 * n:
+        dt = (nd[3 * n::3], nd[3 * n + 1::3], nd[3 * n + 2::3])
+        dl = np.sqrt(dot(dt, dt))
+        big0 = (lens[0] >= lens[1]) & (lens[0] >= lens[2])
+        big1 = lens[1] >= lens[2]
+        tc = tuple(np.where(big0, axes[0][i], np.where(big1, axes[1][i], axes[2][i])) for i in range(3))
+        d = dot(tc, sn)
+        tp = tuple(tc[i] - sn[i] * d for i in range(3))
+        tl = np.sqrt(dot(tp, tp))
+        T = tuple(tp[i] / tl for i in range(3))
+        B = cross(sn, T)
+        dn = tuple(dt[i] / dl for i in range(3))
+        m = norm(tuple((T[i] * dn[0] + B[i] * dn[1]) + sn[i] * dn[2] for i in range(3)))
+        use = (dl > f32(0.001)) & (tl > f32(0.001))
+        sn = tuple(np.where(use, m[i], sn[i]) for i in range(3))
     nvd = norm(tuple(U[28 + i] - P[:, i] for i in range(3)))
-    fn, fv = norm(local), norm(nvd)
+    fn, fv = norm(sn), norm(nvd)
     flip = dot(fn, fv) < 0
     faced = tuple(np.where(flip, -c, c) for c in fn)
     conf = np.clip(dot(faced, nvd), f32(0.0), f32(1.0))
     wn = norm(tuple((U[52 + k] * faced[0] + U[56 + k] * faced[1]) + U[60 + k] * faced[2] for k in range(3)))
     ox, oy = _oct_encode_np(np.stack(wn, -1), normalize=False)
+    # SH colour (:293-351) and emissive (:353-357)
+    deg = packed.sh_degree
+    sh = packed.sh_data.reshape(n, -1).astype(f32)
+    K = (deg + 1) * (deg + 1) - 1
+    col = [sh[:, c].copy() for c in range(3)]
+    if deg >= 1:
+        vd = norm(tuple(U[28 + i] - P[:, i] for i in range(3)))
+        vx, vy, vzz = vd
+        c = lambda j, ch: sh[:, 3 + 3 * j + ch]  # noqa: E731
+        C1 = f32(0.4886025119029199)
+        for ch in range(3):
+            col[ch] = col[ch] + C1 * ((c(0, ch) * vy + c(1, ch) * vzz) + c(2, ch) * vx)
+        if deg >= 2:
+            xx, yy, zz = vx * vx, vy * vy, vzz * vzz
+            xy, yz, xz = vx * vy, vy * vzz, vx * vzz
+            b2 = [f32(1.0925484305920792) * xy, f32(1.0925484305920792) * yz,
+                  f32(0.31539156525252005) * ((f32(2.0) * zz - xx) - yy), f32(1.0925484305920792) * xz,
+                  f32(0.5462742152960396) * (xx - yy)]
+            for ch in range(3):
+                acc = c(3, ch) * b2[0]
+                for j in range(1, 5):
+                    acc = acc + c(3 + j, ch) * b2[j]
+                col[ch] = col[ch] + acc
+            if deg >= 3:
+                b3 = [f32(0.5900435899266435) * vy * (f32(3.0) * xx - yy), f32(2.890611442640554) * vx * vy * vzz,
+                      f32(0.4570457994644658) * vy * ((f32(4.0) * zz - xx) - yy),
+                      f32(0.3731763325901154) * vzz * ((f32(2.0) * zz - f32(3.0) * xx) - f32(3.0) * yy),
+                      f32(0.4570457994644658) * vx * ((f32(4.0) * zz - xx) - yy),
+                      f32(1.445305721320277) * vzz * (xx - yy), f32(0.5900435899266435) * vx * (xx - f32(3.0) * yy)]
+                for ch in range(3):
+                    acc = c(8, ch) * b3[0]
+                    for j in range(1, 7):
+                        acc = acc + c(8 + j, ch) * b3[j]
+                    col[ch] = col[ch] + acc
+    col = [np.clip(v, f32(0.0), f32(1.0)) for v in col]
+    em = sh[:, 3 + 3 * K: 6 + 3 * K]
     pk = lambda a, b: orc.f16_rne(a).astype(np.uint32) | (orc.f16_rne(b).astype(np.uint32) << 16)  # noqa: E731
     zero = np.zeros_like(x)
-    assert np.array_equal(pc[vis, 8], pk(ox, oy)[vis])
-    assert np.array_equal(pc[vis, 13], pk(conf, zero)[vis])
-    sh = packed.sh_data.reshape(scene.count, -1).astype(f32)
-    rgb = np.clip(sh[:, 0:3], f32(0.0), f32(1.0))
-    assert np.array_equal(pc[vis, 9], pk(rgb[:, 0], rgb[:, 1])[vis])
-    assert np.array_equal(pc[vis, 10], pk(rgb[:, 2], zero)[vis])
-    assert np.array_equal(pc[vis, 11], pk(sh[:, 3], sh[:, 4])[vis])
-    assert np.array_equal(pc[vis, 12], pk(sh[:, 5], zero)[vis])
-    assert np.array_equal(pc[vis, 5], packed.material.reshape(-1)[vis])
+    bits = lambda v: np.asarray(v, np.float32).view(np.uint32)  # noqa: E731
+    words = {0: bits(cpx), 1: bits(cpy), 2: bits(ic[0]), 3: bits(ic[1]), 4: bits(ic[2]),
+             5: packed.material.reshape(-1).astype(np.uint32), 6: pk(radius, op), 7: box.astype(np.uint32),
+             8: pk(ox, oy), 9: pk(col[0], col[1]), 10: pk(col[2], zero), 11: pk(em[:, 0], em[:, 1]),
+             12: pk(em[:, 2], zero), 13: pk(conf, zero)}
+    return words, bits(depth), vis
+
+
+def _check_projection(orc, f, words, depth, vis):
+    pc = f["proj_cache"]
+    assert np.all(pc[~vis, 7] == 0xFFFFFFFF)
+    for word, val in words.items():
+        assert np.array_equal(pc[vis, word], val[vis]), word
+    assert np.array_equal(f["depth"][vis], depth[vis])
+
+
+def test_projection_geometry_matches_an_independent_numpy_restatement(orc, pkg, hdsr_lib):
+    # every word of the cache row and the depth, bit for bit against the C
+    # oracle; splats behind the camera get the sentinel (SH 0, no normals)
+    scene = pkg.workloads.plain_scene(3000, seed=23)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    cam = pkg.camera.look_from((0.4, 0.3, 2.0))
+    u, fr = _uniforms(pkg, 320, 240, scene.count, cam)
+    f = orc.render_frame(u, packed, np.arange(scene.count, dtype=np.uint32), threads=2, composite=False)
+    words, depth, vis = _np_project(orc, u, packed, scene.count)
+    assert vis.sum() > 1000 and (~vis).sum() > 0
+    _check_projection(orc, f, words, depth, vis)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_projection_sh_and_normals_match_an_independent_numpy_restatement(orc, pkg, hdsr_lib, deg):
+    # the same with SH degrees 1-3, baked normals (some zero: the covariance
+    # normal is kept) and tangent-space detail normals, emissive, materials
+    rng = np.random.default_rng(30 + deg)
+    scene = pkg.workloads.plain_scene(2000, seed=24)
+    n = scene.count
+    scene.sh_degree = deg
+    scene.sh = rng.normal(0, 0.3, (n, 3 * ((deg + 1) ** 2 - 1))).astype(np.float32)
+    nrm = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    nrm[::7] = 0.0
+    scene.normals = nrm
+    det = np.column_stack([rng.normal(0, 0.3, (n, 2)), np.ones(n)]).astype(np.float32)
+    det[::5] = 0.0
+    scene.detail_normals = det
+    scene.emissive = rng.uniform(0, 2, (n, 3)).astype(np.float32)
+    scene.roughness = rng.uniform(0, 1, n).astype(np.float32)
+    scene.metalness = rng.uniform(0, 1, n).astype(np.float32)
+    packed = pkg.splats.pack_splat_attributes(scene)
+    assert packed.normals is not None and packed.normals.size == 6 * n
+    cam = pkg.camera.look_from((0.6, 0.4, 2.5))
+    u, fr = _uniforms(pkg, 320, 240, n, cam, sh_degree=deg)
+    f = orc.render_frame(u, packed, np.arange(n, dtype=np.uint32), threads=2, composite=False)
+    words, depth, vis = _np_project(orc, u, packed, n)
+    assert vis.sum() > 500
+    _check_projection(orc, f, words, depth, vis)
 
 
 def _oct_decode_np(e):
