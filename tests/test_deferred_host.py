@@ -255,3 +255,43 @@ def test_bilateral_defaults_match_the_reference(pkg):
     # bilateral filter's spatialSigma 3.0, normalSigma 1.5, kernelRadius 3
     q = pkg.deferred.default_params()
     assert q.bilateral_spatial_sigma == 3.0 and q.bilateral_normal_sigma == 1.5 and q.bilateral_radius == 3
+
+
+def test_bloom_threshold_matches_an_independent_numpy_restatement(pkg, orc):
+    # bloom_threshold.wgsl restated with numpy f32 steps: 2x2 box of the
+    # material image's emissive (loads past the edge clamp to it), soft
+    # threshold, rgba16f store; bit for bit against the oracle
+    D = pkg.deferred
+    rng = np.random.default_rng(8)
+    W, H = 37, 29
+    color = np.zeros((H, W, 4), np.float32)
+    depth = np.full((H, W), 0.5, np.float32)
+    normal = np.zeros((H, W), np.uint32)
+    em = rng.uniform(0, 3, (H, W, 3)).astype(np.float32)
+    em[rng.uniform(0, 1, (H, W)) < 0.5] = 0.0
+    h = orc.f16_rne(em.reshape(-1)).reshape(H, W, 3).astype(np.uint32)
+    material = np.zeros((H, W, 4), np.uint32)
+    material[..., 1] = h[..., 0] | (h[..., 1] << 16)
+    material[..., 2] = h[..., 2]
+    inp, keep = orc.post_inputs(color, depth, normal, material)
+    cam = pkg.camera.OrbitCamera(azimuth=0.0, elevation=0.0, distance=3.0)
+    q = D.frame_params(cam, W, H, bloom_threshold=0.8, bloom_soft_knee=0.5, emissive_intensity=1.7)
+    got = orc.f16_to_f32(orc.post_bloom_threshold(inp, q).reshape(-1)).reshape((H + 1) // 2, (W + 1) // 2, 4)
+    f32 = np.float32
+    emf = orc.f16_to_f32(h.astype(np.uint16).reshape(-1)).reshape(H, W, 3)
+    hh, hw = (H + 1) // 2, (W + 1) // 2
+    ys, xs = np.mgrid[0:hh, 0:hw]
+    acc = np.zeros((hh, hw, 3), np.float32)
+    for dy in (0, 1):
+        for dx in (0, 1):
+            acc = (acc + emf[np.minimum(2 * ys + dy, H - 1), np.minimum(2 * xs + dx, W - 1)]).astype(f32)
+    e = (acc * f32(0.25)).astype(f32) * f32(q.emissive_intensity)
+    lum = (e[..., 0] * f32(0.2126) + e[..., 1] * f32(0.7152)) + e[..., 2] * f32(0.0722)
+    knee = f32(q.bloom_threshold) * f32(q.bloom_soft_knee)
+    soft = (lum - f32(q.bloom_threshold)) + knee
+    contrib = np.maximum(soft, f32(0.0)) / np.maximum(knee * f32(2.0), f32(0.0001))
+    wgt = np.minimum(contrib * contrib, f32(1.0))
+    want = (e * wgt[..., None]).astype(np.float16).astype(np.float32)
+    assert np.array_equal(got[..., :3], want)
+    assert np.all(got[..., 3] == 1.0)
+    assert (want > 0).any() and (want == 0).any()
