@@ -295,3 +295,29 @@ def test_bloom_threshold_matches_an_independent_numpy_restatement(pkg, orc):
     assert np.array_equal(got[..., :3], want)
     assert np.all(got[..., 3] == 1.0)
     assert (want > 0).any() and (want == 0).any()
+
+
+def test_gtao_prefilter_matches_an_independent_numpy_restatement(pkg, orc):
+    # gtao_depth_prefilter.wgsl with numpy f32 steps: linear depth
+    # near*far / (far - d (far - near)) per pixel (reads past the edge clamp
+    # to it), then 2x2 and 4x4 minima inside each 16x16 block
+    D = pkg.deferred
+    rng = np.random.default_rng(9)
+    W, H = 37, 29
+    depth = rng.uniform(0.2, 0.999, (H, W)).astype(np.float32)
+    inp, keep = orc.post_inputs(np.zeros((H, W, 4), np.float32), depth, np.zeros((H, W), np.uint32),
+                                np.zeros((H, W, 4), np.uint32))
+    cam = pkg.camera.OrbitCamera(azimuth=0.0, elevation=0.0, distance=3.0)
+    q = D.frame_params(cam, W, H)
+    m0, m1, m2 = orc.post_gtao_prefilter(inp, q)
+    f32 = np.float32
+    nr, fr_ = f32(q.near_plane), f32(q.far_plane)
+    Hp, Wp = (H + 15) // 16 * 16, (W + 15) // 16 * 16
+    ys, xs = np.mgrid[0:Hp, 0:Wp]
+    d = depth[np.minimum(ys, H - 1), np.minimum(xs, W - 1)]
+    lin = (nr * fr_) / (fr_ - d * (fr_ - nr))
+    assert np.array_equal(m0, lin[:H, :W])
+    l1 = np.minimum(np.minimum(lin[0::2, 0::2], lin[0::2, 1::2]), np.minimum(lin[1::2, 0::2], lin[1::2, 1::2]))
+    l2 = np.minimum(np.minimum(l1[0::2, 0::2], l1[0::2, 1::2]), np.minimum(l1[1::2, 0::2], l1[1::2, 1::2]))
+    assert np.array_equal(m1, l1[:m1.shape[0], :m1.shape[1]])
+    assert np.array_equal(m2, l2[:m2.shape[0], :m2.shape[1]])
