@@ -321,3 +321,47 @@ def test_gtao_prefilter_matches_an_independent_numpy_restatement(pkg, orc):
     l2 = np.minimum(np.minimum(l1[0::2, 0::2], l1[0::2, 1::2]), np.minimum(l1[1::2, 0::2], l1[1::2, 1::2]))
     assert np.array_equal(m1, l1[:m1.shape[0], :m1.shape[1]])
     assert np.array_equal(m2, l2[:m2.shape[0], :m2.shape[1]])
+
+
+def _bilinear_np(img, u, v):
+    """A filtering sampler on an rgba16f image (clamp to edge), the canonical
+    f32 form: texel = uv * size - 0.5, rows mixed t0 (1 - a) + t1 a, then by
+    (1 - b), b."""
+    f32 = np.float32
+    h, w = img.shape[:2]
+    fx, fy = (u * f32(w) - f32(0.5)).astype(f32), (v * f32(h) - f32(0.5)).astype(f32)
+    x0f, y0f = np.floor(fx), np.floor(fy)
+    ax, ay = (fx - x0f).astype(f32), (fy - y0f).astype(f32)
+    x0, y0 = x0f.astype(np.int64), y0f.astype(np.int64)
+    cx = lambda i: np.clip(i, 0, w - 1)  # noqa: E731
+    cy = lambda i: np.clip(i, 0, h - 1)  # noqa: E731
+    t00, t10 = img[cy(y0), cx(x0)], img[cy(y0), cx(x0 + 1)]
+    t01, t11 = img[cy(y0 + 1), cx(x0)], img[cy(y0 + 1), cx(x0 + 1)]
+    bx, by = (f32(1.0) - ax)[..., None], (f32(1.0) - ay)[..., None]
+    ax, ay = ax[..., None], ay[..., None]
+    return ((t00 * bx + t10 * ax) * by + (t01 * bx + t11 * ax) * ay).astype(f32)
+
+
+@pytest.mark.parametrize("horizontal", [True, False])
+def test_bloom_blur_matches_an_independent_numpy_restatement(orc, horizontal):
+    # bloom_blur.wgsl: centre tap plus 6 symmetric pairs along `direction`,
+    # each a bilinear sample (clamp), weights of its WEIGHTS table; rgba16f out
+    f32 = np.float32
+    rng = np.random.default_rng(10)
+    hh, hw = 15, 19
+    img16 = orc.f16_rne(rng.uniform(0, 2, (hh * hw * 4)).astype(np.float32)).reshape(hh, hw, 4)
+    img = orc.f16_to_f32(img16.reshape(-1)).reshape(hh, hw, 4)
+    tx, ty = f32(1.0) / f32(hw), f32(1.0) / f32(hh)
+    dx, dy = (tx, f32(0.0)) if horizontal else (f32(0.0), ty)
+    got = orc.f16_to_f32(orc.post_bloom_blur(img16, float(dx), float(dy), float(tx), float(ty)).reshape(-1)).reshape(hh, hw, 4)
+    wts = np.array([0.1112202001, 0.1077983143, 0.0981514821, 0.0839534116, 0.0674584614, 0.0509203181,
+                    0.0361079124], np.float32)
+    ys, xs = np.mgrid[0:hh, 0:hw]
+    u, v = ((xs + f32(0.5)) * tx).astype(f32), ((ys + f32(0.5)) * ty).astype(f32)
+    r = (_bilinear_np(img, u, v)[..., :3] * wts[0]).astype(f32)
+    for i in range(1, 7):
+        ox, oy = f32(dx * f32(i)), f32(dy * f32(i))
+        r = (r + _bilinear_np(img, (u + ox).astype(f32), (v + oy).astype(f32))[..., :3] * wts[i]).astype(f32)
+        r = (r + _bilinear_np(img, (u - ox).astype(f32), (v - oy).astype(f32))[..., :3] * wts[i]).astype(f32)
+    assert np.array_equal(got[..., :3], r.astype(np.float16).astype(np.float32))
+    assert np.all(got[..., 3] == 1.0)
