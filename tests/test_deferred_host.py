@@ -365,3 +365,97 @@ def test_bloom_blur_matches_an_independent_numpy_restatement(orc, horizontal):
         r = (r + _bilinear_np(img, (u - ox).astype(f32), (v - oy).astype(f32))[..., :3] * wts[i]).astype(f32)
     assert np.array_equal(got[..., :3], r.astype(np.float16).astype(np.float32))
     assert np.all(got[..., 3] == 1.0)
+
+
+def _np3(f):
+    return lambda a, b: tuple(f(a[i], b[i]) for i in range(3))
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_screen_space_normals_match_an_independent_numpy_restatement(pkg, orc, mode):
+    # gpu_screen_space_normals.wgsl:55-119 with numpy f32 steps (view
+    # positions from the inverse view-projection, one-sided differences
+    # toward the closer neighbour depth, face-forward, recovery modes 0/1/2,
+    # background pass-through), bit for bit against the oracle
+    D = pkg.deferred
+    f32 = np.float32
+    rng = np.random.default_rng(11 + mode)
+    W, H = 23, 17
+    ys, xs = np.mgrid[0:H, 0:W]
+    depth = (0.9 + 0.002 * xs + 0.001 * ys + rng.normal(0, 0.0005, (H, W))).astype(np.float32)
+    depth[:, :2] = 1.0
+    src = rng.normal(0, 1, (H, W, 3)).astype(np.float32)
+    src /= np.linalg.norm(src, axis=-1, keepdims=True)
+    s_abs = np.abs(src).sum(-1)
+    ox, oy = src[..., 0] / s_abs, src[..., 1] / s_abs
+    neg = src[..., 2] < 0
+    ox, oy = (np.where(neg, (1 - np.abs(oy)) * np.where(ox >= 0, 1, -1), ox),
+              np.where(neg, (1 - np.abs(ox)) * np.where(oy >= 0, 1, -1), oy))
+    word = orc.f16_rne(ox.astype(np.float32).reshape(-1)).astype(np.uint32) | (
+        orc.f16_rne(oy.astype(np.float32).reshape(-1)).astype(np.uint32) << 16)
+    normal = word.reshape(H, W)
+    inp, keep = orc.post_inputs(np.zeros((H, W, 4), np.float32), depth, normal, np.zeros((H, W, 4), np.uint32))
+    cam = pkg.camera.OrbitCamera(azimuth=0.3, elevation=0.2, distance=3.0)
+    q = D.frame_params(cam, W, H, normal_recovery_mode=mode, grazing_start=0.1, grazing_end=0.4)
+    got = orc.post_ss_normals(inp, q).reshape(H, W)
+    M = np.asarray(list(q.view_proj_inverse), np.float32)
+    cam_p = np.asarray(list(q.camera_pos), np.float32)
+    dot = lambda a, b: (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]  # noqa: E731
+    sub = _np3(lambda a, b: a - b)
+
+    def nrm(v):
+        ln = np.sqrt(dot(v, v))
+        return tuple(c / ln for c in v)
+
+    def recon(px, py, d):
+        nx = (px / f32(W)) * f32(2.0) - f32(1.0)
+        ny = f32(1.0) - (py / f32(H)) * f32(2.0)
+        w = [((M[r] * nx + M[4 + r] * ny) + M[8 + r] * d) + M[12 + r] * f32(1.0) for r in range(4)]
+        return tuple(w[i] / w[3] for i in range(3))
+
+    def face(n, v):
+        n, v = nrm(n), nrm(v)
+        flip = dot(n, v) < 0
+        return tuple(np.where(flip, -c, c) for c in n)
+
+    with np.errstate(divide="ignore", invalid="ignore"):
+        cx, cy = (xs + f32(0.5)).astype(f32), (ys + f32(0.5)).astype(f32)
+        pc = recon(cx, cy, depth)
+        dL, dR = depth[ys, np.maximum(xs - 1, 0)], depth[ys, np.minimum(xs + 1, W - 1)]
+        dU, dD = depth[np.maximum(ys - 1, 0), xs], depth[np.minimum(ys + 1, H - 1), xs]
+        left = np.abs(dL - depth) < np.abs(dR - depth)
+        pL, pR = recon(cx - f32(1.0), cy, dL), recon(cx + f32(1.0), cy, dR)
+        ddx = tuple(np.where(left, pc[i] - pL[i], pR[i] - pc[i]) for i in range(3))
+        up = np.abs(dU - depth) < np.abs(dD - depth)
+        pU, pD = recon(cx, cy - f32(1.0), dU), recon(cx, cy + f32(1.0), dD)
+        ddy = tuple(np.where(up, pc[i] - pU[i], pD[i] - pc[i]) for i in range(3))
+        vd = nrm(sub(tuple(np.full_like(cx, cam_p[i]) for i in range(3)), pc))
+        cr = (ddy[1] * ddx[2] - ddy[2] * ddx[1], ddy[2] * ddx[0] - ddy[0] * ddx[2], ddy[0] * ddx[1] - ddy[1] * ddx[0])
+        screen = face(nrm(cr), vd)
+        e = orc.f16_to_f32(np.stack([normal & 0xFFFF, normal >> 16], -1).astype(np.uint16).reshape(-1)).reshape(H, W, 2)
+        ex, ey = e[..., 0], e[..., 1]
+        ez = (f32(1.0) - np.abs(ex)) - np.abs(ey)
+        zn = ez < 0
+        dx_ = np.where(zn, (f32(1.0) - np.abs(ey)) * np.where(ex >= 0, f32(1.0), f32(-1.0)), ex)
+        dy_ = np.where(zn, (f32(1.0) - np.abs(ex)) * np.where(ey >= 0, f32(1.0), f32(-1.0)), ey)
+        source = face(nrm((dx_, dy_, ez)), vd)
+        if mode == 2:
+            n = source
+        elif mode == 1:
+            ndv = np.maximum(dot(source, vd), f32(0.0))
+            t = np.clip((ndv - f32(q.grazing_start)) / (f32(q.grazing_end) - f32(q.grazing_start)), f32(0.0), f32(1.0))
+            blend = f32(1.0) - t * t * (f32(3.0) - f32(2.0) * t)
+            n = nrm(tuple(source[i] * (f32(1.0) - blend) + screen[i] * blend for i in range(3)))
+        else:
+            n = screen
+        sm = (np.abs(n[0]) + np.abs(n[1])) + np.abs(n[2])
+        px_, py_ = n[0] / sm, n[1] / sm
+        nz = n[2] < 0
+        ox2 = np.where(nz, (f32(1.0) - np.abs(py_)) * np.where(px_ >= 0, f32(1.0), f32(-1.0)), px_)
+        oy2 = np.where(nz, (f32(1.0) - np.abs(px_)) * np.where(py_ >= 0, f32(1.0), f32(-1.0)), py_)
+    want = orc.f16_rne(ox2.astype(np.float32).reshape(-1)).astype(np.uint32) | (
+        orc.f16_rne(oy2.astype(np.float32).reshape(-1)).astype(np.uint32) << 16)
+    want = want.reshape(H, W)
+    bg = depth >= 0.9999
+    want[bg] = normal[bg] if mode > 0 else 0
+    assert np.array_equal(got, want)
