@@ -459,3 +459,76 @@ def test_screen_space_normals_match_an_independent_numpy_restatement(pkg, orc, m
     bg = depth >= 0.9999
     want[bg] = normal[bg] if mode > 0 else 0
     assert np.array_equal(got, want)
+
+
+def _np_oct_decode(word, orc):
+    f32 = np.float32
+    e = orc.f16_to_f32(np.stack([word & 0xFFFF, word >> 16], -1).astype(np.uint16).reshape(-1)).reshape(word.shape + (2,))
+    ex, ey = e[..., 0], e[..., 1]
+    ez = (f32(1.0) - np.abs(ex)) - np.abs(ey)
+    zn = ez < 0
+    x = np.where(zn, (f32(1.0) - np.abs(ey)) * np.where(ex >= 0, f32(1.0), f32(-1.0)), ex)
+    y = np.where(zn, (f32(1.0) - np.abs(ex)) * np.where(ey >= 0, f32(1.0), f32(-1.0)), ey)
+    ln = np.sqrt((x * x + y * y) + ez * ez)
+    return x / ln, y / ln, ez / ln
+
+
+def _np_oct_word(n, orc):
+    f32 = np.float32
+    sm = (np.abs(n[0]) + np.abs(n[1])) + np.abs(n[2])
+    px, py = n[0] / sm, n[1] / sm
+    nz = n[2] < 0
+    ox = np.where(nz, (f32(1.0) - np.abs(py)) * np.where(px >= 0, f32(1.0), f32(-1.0)), px)
+    oy = np.where(nz, (f32(1.0) - np.abs(px)) * np.where(py >= 0, f32(1.0), f32(-1.0)), py)
+    shape = ox.shape
+    return (orc.f16_rne(ox.astype(np.float32).reshape(-1)).astype(np.uint32)
+            | (orc.f16_rne(oy.astype(np.float32).reshape(-1)).astype(np.uint32) << 16)).reshape(shape)
+
+
+def test_bilateral_filter_matches_an_independent_numpy_restatement(pkg, orc):
+    # bilateral_normal_filter.wgsl:39-86 with numpy f32 steps, the oracle's
+    # exp and log (pow = exp(y log x) with its special cases), clamped taps;
+    # bit for bit against the oracle
+    D = pkg.deferred
+    f32 = np.float32
+    rng = np.random.default_rng(12)
+    W, H = 21, 15
+    ys, xs = np.mgrid[0:H, 0:W]
+    depth = (0.9 + 0.003 * xs + rng.normal(0, 0.002, (H, W))).astype(np.float32)
+    depth[:, :2] = 1.0
+    n = rng.normal(0, 1, (H, W, 3)) + np.array([0, 0, 2.0])
+    n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
+    ssn = _np_oct_word((n[..., 0], n[..., 1], n[..., 2]), orc)
+    inp, keep = orc.post_inputs(np.zeros((H, W, 4), np.float32), depth, np.zeros((H, W), np.uint32),
+                                np.zeros((H, W, 4), np.uint32))
+    cam = pkg.camera.OrbitCamera(azimuth=0.0, elevation=0.0, distance=3.0)
+    q = D.frame_params(cam, W, H)
+    got = orc.post_bilateral(inp, q, ssn).reshape(H, W)
+    R, ss, sdv = int(q.bilateral_radius), f32(q.bilateral_spatial_sigma), f32(q.bilateral_depth_sigma)
+    ne = f32(1.0) / np.maximum(f32(q.bilateral_normal_sigma), f32(0.01))
+    cn = _np_oct_decode(ssn, orc)
+    acc = [np.zeros((H, W), np.float32) for _ in range(3)]
+    total = np.zeros((H, W), np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for dy in range(-R, R + 1):
+            for dx in range(-R, R + 1):
+                sy, sx = np.clip(ys + dy, 0, H - 1), np.clip(xs + dx, 0, W - 1)
+                sn = _np_oct_decode(ssn[sy, sx], orc)
+                sd = depth[sy, sx]
+                dist2 = f32(dx * dx + dy * dy)
+                spatial = orc.expf(np.full((H, W), -dist2 / ((f32(2.0) * ss) * ss), np.float32)).reshape(H, W)
+                dd = np.abs(depth - sd) / np.maximum(depth, f32(0.001))
+                dw = orc.expf(((-dd) * dd) / ((f32(2.0) * sdv) * sdv)).reshape(H, W)
+                x = np.maximum((cn[0] * sn[0] + cn[1] * sn[1]) + cn[2] * sn[2], f32(0.0))
+                pw = orc.expf(ne * orc.logf(np.maximum(x, f32(1e-30)).reshape(-1)).reshape(H, W)).reshape(H, W)
+                pw = np.where(x == f32(1.0), f32(1.0), np.where(x == f32(0.0), f32(0.0), pw))
+                w = (spatial * dw) * pw
+                acc = [(acc[i] + sn[i] * w).astype(np.float32) for i in range(3)]
+                total = (total + w).astype(np.float32)
+        t = np.maximum(total, f32(0.0001))
+        v = tuple(acc[i] / t for i in range(3))
+        ln = np.sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
+        want = _np_oct_word(tuple(c / ln for c in v), orc)
+    bg = depth >= 0.9999
+    want[bg] = ssn[bg]
+    assert np.array_equal(got, want)
