@@ -532,3 +532,34 @@ def test_bilateral_filter_matches_an_independent_numpy_restatement(pkg, orc):
     bg = depth >= 0.9999
     want[bg] = ssn[bg]
     assert np.array_equal(got, want)
+
+
+def test_gtao_denoise_matches_an_independent_numpy_restatement(pkg, orc):
+    # gtao_denoise.wgsl: the 3x3 neighbourhood (clamped) weighted by
+    # exp(-|dz| / max(z, 0.001) * strength), the centre with weight 1; rgba16f
+    D = pkg.deferred
+    f32 = np.float32
+    rng = np.random.default_rng(13)
+    W, H = 19, 13
+    mip0 = rng.uniform(0.5, 8.0, (H, W)).astype(np.float32)
+    raw = orc.f16_rne(rng.uniform(0, 1, (H * W * 4)).astype(np.float32)).reshape(H, W, 4)
+    depth = np.full((H, W), 0.5, np.float32)
+    inp, keep = orc.post_inputs(np.zeros((H, W, 4), np.float32), depth, np.zeros((H, W), np.uint32),
+                                np.zeros((H, W, 4), np.uint32))
+    cam = pkg.camera.OrbitCamera(azimuth=0.0, elevation=0.0, distance=3.0)
+    q = D.frame_params(cam, W, H, ao_denoise_strength=3.5)
+    got = orc.f16_to_f32(orc.post_gtao_denoise(inp, q, raw, mip0).reshape(-1)).reshape(H, W, 4)
+    a = orc.f16_to_f32(raw.reshape(-1)).reshape(H, W, 4)
+    ys, xs = np.mgrid[0:H, 0:W]
+    acc, total = a.copy(), np.ones((H, W), np.float32)
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            if dx == 0 and dy == 0:
+                continue
+            sy, sx = np.clip(ys + dy, 0, H - 1), np.clip(xs + dx, 0, W - 1)
+            dd = np.abs(mip0 - mip0[sy, sx]) / np.maximum(mip0, f32(0.001))
+            w = orc.expf(((-dd) * f32(q.ao_denoise_strength)).reshape(-1)).reshape(H, W)
+            total = (total + w).astype(np.float32)
+            acc = (acc + a[sy, sx] * w[..., None]).astype(np.float32)
+    want = (acc / total[..., None]).astype(np.float16).astype(np.float32)
+    assert np.array_equal(got, want)
