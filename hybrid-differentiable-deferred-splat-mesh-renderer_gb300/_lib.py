@@ -187,6 +187,7 @@ SIGNATURES = {
     "hdsr_pass_times": (c_int, [c_void_p, POINTER(c_float), POINTER(c_uint32), c_uint32, POINTER(c_uint32)]),
     "hdsr_pass_name": (c_char_p, [c_uint32]),
     "hdsr_launch_count": (c_uint64, [c_void_p]),
+    "hdsr_set_scan_wait": (c_int, [c_void_p, c_uint32, c_uint32]),
     "hdsr_post_create": (c_int, [c_uint32, c_uint32, POINTER(c_void_p)]),
     "hdsr_post_destroy": (None, [c_void_p]),
     "hdsr_post_default_params": (None, [POINTER(PostParams)]),

@@ -125,12 +125,18 @@ class TileSplatCompositorResources:
 
     def chunk_ranges(self):
         """The hot-tile chunk table of the last full frame (chunkRanges of
-        gpu_tile_bucket_sort.wgsl:276-307), from the tile counts and offsets."""
+        gpu_tile_bucket_sort.wgsl:110-143), from the tile counts and offsets."""
         return chunk_ranges_from_tiles(self.buffer("tile_counts").cpu().numpy().view(np.uint32),
                                        self.buffer("tile_offsets").cpu().numpy().view(np.uint32))
 
     def set_profiling(self, enable: bool = True) -> None:
         _lib.check(self._lib.hdsr_set_profiling(self.handle, 1 if enable else 0), self.handle, "set_profiling")
+
+    def set_scan_wait(self, spin_limit: int = 0, withheld_tile: int | None = None) -> None:
+        """Bound of the scans' decoupled-lookback waits (0: the default 2^22
+        spins) and the test hook that keeps one scan tile from posting."""
+        tile = 0xFFFFFFFF if withheld_tile is None else int(withheld_tile)
+        _lib.check(self._lib.hdsr_set_scan_wait(self.handle, int(spin_limit), tile), self.handle, "set_scan_wait")
 
     def pass_times(self) -> list[tuple[str, float]]:
         """(pass name, ms) of the last profiled encode, in launch order."""
@@ -179,7 +185,7 @@ class _DeviceView:
 def chunk_ranges_from_tiles(tile_counts, tile_offsets, max_tile_entries: int = 4096) -> np.ndarray:
     """(start, count) per chunk of every hot tile (more than 4096 entries), in
     ascending Morton order, as the bucket cascade packs them
-    (gpu_tile_bucket_sort.wgsl:276-307: buckets in order, 4096 entries per
+    (gpu_tile_bucket_sort.wgsl:110-143: buckets in order, 4096 entries per
     chunk, the last one partial). The entries of a tile are already in bucket
     order at its offset, so chunk k is positions [4096 k, 4096 k + 4096) of it."""
     counts = np.asarray(tile_counts, np.int64)

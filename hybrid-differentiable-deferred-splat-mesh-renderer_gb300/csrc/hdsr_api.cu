@@ -197,6 +197,8 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   a.color_f32 = h->cfg.color_format == HDSR_COLOR_RGBA32F;
   a.log_keys = (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) ? 1u : 0u;
   a.composite_f16 = (h->cfg.flags & HDSR_CFG_F16_COMPOSITE) ? 1u : 0u;
+  a.spin_limit = kSpinLimit;
+  a.withheld_scan_tile = kNoWithheldTile;
   const uint64_t sb_cap = (uint64_t)N * 9u;  // a tile box (<= 17 tiles a side) meets <= 3x3 superblocks
   a.sb_cap = sb_cap;
   a.seg_cap = (uint32_t)((sb_cap + kSegEntries - 1u) / kSegEntries + a.num_sb);
@@ -768,6 +770,14 @@ hdsr_status hdsr_pass_times(hdsr_compositor* h, float* ms, uint32_t* ids, uint32
 const char* hdsr_pass_name(uint32_t id) { return id < kNumPassNames ? kPassNames[id] : "unknown"; }
 
 uint64_t hdsr_launch_count(const hdsr_compositor* h) { return h ? h->launches : 0u; }
+
+hdsr_status hdsr_set_scan_wait(hdsr_compositor* h, uint32_t spin_limit, uint32_t withheld_tile) {
+  if (!h) return HDSR_ERR_INVALID_ARG;
+  h->args.spin_limit = spin_limit ? spin_limit : kSpinLimit;
+  h->args.withheld_scan_tile = withheld_tile;
+  drop_graph(h);  // a frame graph holds the old arguments
+  return HDSR_OK;
+}
 
 }  // extern "C"
 

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
   __shared__ float4 s_pay[kBwdWarps][32][kBRows];
   __shared__ uint32_t s_queue[kBwdWarps][kWalkQueue];
   const FrameArgs& a = b.f;
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   float4 (*s)[kBRows] = s_pay[warp];
   const uint32_t items = 2u * a.tile_count;

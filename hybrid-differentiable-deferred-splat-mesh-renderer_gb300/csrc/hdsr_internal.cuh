@@ -139,6 +139,8 @@ struct FrameArgs {
   unsigned long long* scan_status_n; // per kScanTile-element tile of the N scan
   unsigned long long* scan_status_m;
   uint32_t* ctl;
+  uint32_t spin_limit;            // bound of each decoupled-lookback wait (spins of ~100 ns)
+  uint32_t withheld_scan_tile;    // test hook: this tile of each scan never posts its status (~0u: none)
   // outputs (borrowed)
   void* out_color;
   uint64_t color_pitch;
@@ -302,8 +304,15 @@ struct TileWalk {
   }
 };
 
-// Bounded spin for decoupled-lookback waits (iterations of ~100 ns).
+// Default bound of a decoupled-lookback wait (iterations of ~100 ns);
+// a handle can lower it (hdsr_set_scan_wait).
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr uint32_t kNoWithheldTile = 0xFFFFFFFFu;
+
+// Frame flags after which the frame's later kernels return at once:
+// overflow (0x1, the lists do not fit) and timeout (0x2, a scan wait gave up
+// and its offsets are not trustworthy).
+constexpr uint32_t kSkipFlags = 0x3u;
 
 // Lookback status word: epoch (30 bits) | flag (2 bits) | value (32 bits).
 constexpr unsigned long long kFlagAgg = 1ull;

@@ -195,7 +195,7 @@ HDSR_HD uint32_t morton_even(uint32_t m) {
 }
 
 // Per-tile log-depth mapping of the hot-tile bucket cascade
-// (gpu_tile_bucket_sort.wgsl:240-244), scaled to 2^20 keys instead of 128
+// (gpu_tile_bucket_sort.wgsl:75-85), scaled to 2^20 keys instead of 128
 // buckets: keyScale = 1048576/R = 8192 * (128/R) exactly, so a key's top
 // seven bits are the reference bucket.
 HDSR_HD float2 tile_log_params(uint32_t dmin_bits, uint32_t dmax_bits) {

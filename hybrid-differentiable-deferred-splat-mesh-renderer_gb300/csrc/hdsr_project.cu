@@ -14,7 +14,7 @@
 // to the superblock; the lists replace scatter_tile_refs and the cooperative
 // large-splat scatter (gpu_large_splat_scatter.wgsl). When the 20-bit log-depth keys are
 // requested, k_depth_range keeps the per-tile depth min/max of the hot-tile
-// bucket mapping (gpu_tile_bucket_sort.wgsl:232-237).
+// bucket mapping (gpu_tile_bucket_sort.wgsl:67-72).
 #include "hdsr_internal.cuh"
 
 namespace hdsr {

@@ -240,7 +240,7 @@ template <bool F16>
 __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(FrameArgs a) {
   __shared__ float4 s_pay[kWarps][32][kRows];
   __shared__ uint32_t s_queue[kWarps][kWalkQueue];
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   float4 (*s)[kRows] = s_pay[warp];
   const uint32_t items = 2u * a.tile_count;

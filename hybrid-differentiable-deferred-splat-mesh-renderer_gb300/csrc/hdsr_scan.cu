@@ -1,7 +1,7 @@
 // hdsr_scan.cu — single-pass exclusive scans with decoupled lookback.
 //
 // Replaces the reference's three-pass Hillis-Steele scan (scan,
-// scan_block_sums, add_block_sums in gpu_prefix_sum.wgsl:169-240, driven by
+// scan_block_sums, add_block_sums in gpu_prefix_sum.wgsl:14-85, driven by
 // gpuTileSplatCompositor.ts:1063-1088) with one launch per array:
 //   - per-splat superblock counts, taken in ascending (depth, sortRank)
 //     order from bits 24-31 of the depth-order words (N) -> each splat's
@@ -32,7 +32,7 @@ __device__ __forceinline__ void st_volatile(unsigned long long* p, unsigned long
 // prefix in the window ends the walk, else the 32 aggregates are added and
 // the window moves back. Positions before tile 0 count as an inclusive 0.
 __device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t epoch, uint32_t* ctl,
-                             uint32_t lane) {
+                             uint32_t lane, uint32_t spin_limit) {
   uint32_t prefix = 0;
   for (int base = (int)tile - 1;; base -= 32) {
     const int t = base - (int)lane;
@@ -42,7 +42,7 @@ __device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t
       for (;;) {
         st = ld_volatile(status + t);
         if ((uint32_t)(st >> 34) == (epoch & 0x3FFFFFFFu) && ((st >> 32) & 3ull) != 0ull) break;
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicOr(ctl + kCtlFlags, 0x2u);
           st = make_status(epoch, kFlagInc, 0u);
           break;
@@ -85,7 +85,7 @@ __device__ __forceinline__ void emit_superblock_entries(const FrameArgs& a, uint
 // depth-order words), emitting every splat's list entries at its offset.
 struct SbScan {
   // an overflowed frame skipped the depth sort: order holds no permutation
-  static __device__ bool skip(const FrameArgs& a) { return (a.ctl[kCtlFlags] & 0x1u) != 0u; }
+  static __device__ bool skip(const FrameArgs& a) { return (a.ctl[kCtlFlags] & kSkipFlags) != 0u; }
   static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
@@ -137,7 +137,7 @@ struct TileScan {
     if (a.log_keys) a.tile_log[i] = tile_log_params(a.tile_dmin[i], a.tile_dmax[i]);
     if (c > kMaxTileEntries) {
       // hot tile: the reference's bucket cascade splits it into 4096-entry
-      // chunks (gpu_tile_bucket_sort.wgsl:276-307)
+      // chunks (gpu_tile_bucket_sort.wgsl:110-143)
       atomicAdd(a.ctl + kCtlHotTiles, 1u);
       atomicAdd(a.ctl + kCtlChunks, (c + kMaxTileEntries - 1u) / kMaxTileEntries);
     }
@@ -202,12 +202,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(FrameArgs a) {
       if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
       const uint32_t total = __shfl_sync(0xFFFFFFFFu, wi, kScanThreads / 32 - 1);
       uint32_t prefix = 0u;
+      // a withheld tile (test hook) computes its prefix but posts nothing:
+      // its successors' waits run out and flag the frame
+      const bool post = tile != a.withheld_scan_tile;
       if (tile == 0) {
-        if (lane == 0) st_volatile(status + tile, make_status(epoch, kFlagInc, total));
+        if (lane == 0 && post) st_volatile(status + tile, make_status(epoch, kFlagInc, total));
       } else {
-        if (lane == 0) st_volatile(status + tile, make_status(epoch, kFlagAgg, total));
-        prefix = lookback(status, tile, epoch, a.ctl, lane);
-        if (lane == 0) st_volatile(status + tile, make_status(epoch, kFlagInc, prefix + total));
+        if (lane == 0 && post) st_volatile(status + tile, make_status(epoch, kFlagAgg, total));
+        prefix = lookback(status, tile, epoch, a.ctl, lane, a.spin_limit);
+        if (lane == 0 && post) st_volatile(status + tile, make_status(epoch, kFlagInc, prefix + total));
       }
       if (lane == 0) {
         s_prefix = prefix;

@@ -3,9 +3,9 @@
 //
 // Per-tile order. Every tile's entries end in ascending (depth bits,
 // sortRank) order: the order of tile_depth_sort (gpu_tile_depth_sort.wgsl:
-// 114-165) and chunk_sort (gpu_tile_chunk_sort.wgsl:345-395) with sortRank
+// 28-79) and chunk_sort (gpu_tile_chunk_sort.wgsl:36-89) with sortRank
 // breaking their ties, and — because the 128 log-depth buckets of the
-// hot-tile cascade (gpu_tile_bucket_sort.wgsl:240-307) are monotone in the
+// hot-tile cascade (gpu_tile_bucket_sort.wgsl:75-107) are monotone in the
 // depth — also the cascade's order when a bucket keeps (depth, sortRank)
 // order. So the frame's sort is one stable LSD radix over the composite key
 // (Morton tile, depth bits, sortRank), done in two stages:
@@ -39,7 +39,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-__device__ __forceinline__ bool skipped(const RadixJob& j) { return (*j.flags & 0x1u) != 0u; }
+__device__ __forceinline__ bool skipped(const RadixJob& j) { return (*j.flags & kSkipFlags) != 0u; }
 
 // Upsweep: per block-tile digit counts, bin-major (tile_digits[bin*cap+tile]).
 __global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(256) k_seg_count(FrameArgs a) {
   constexpr uint32_t kGrid = 9u * 9u;
   __shared__ int s_diff[8][kGrid + 3u];
   __shared__ SegTables tables;
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   seg_tables_load(a, tables);
   const uint32_t lane = threadIdx.x & 31u;
   int* d = s_diff[threadIdx.x >> 5];
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256) k_seg_count(FrameArgs a) {
 __global__ void __launch_bounds__(1024) k_seg_scan(FrameArgs a) {
   constexpr uint32_t G = 16;
   __shared__ uint32_t s_part[G][kSbTiles];
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   const uint32_t sb = blockIdx.x, j = threadIdx.x & (kSbTiles - 1u), g = threadIdx.x / kSbTiles;
   const uint32_t f0 = a.seg_first[sb], f1 = a.seg_first[sb + 1u];
   const uint32_t per = (f1 - f0 + G - 1u) / G;
@@ -358,7 +358,7 @@ constexpr int kScatterStep = HDSR_SCATTER_STEP;
 __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
   constexpr uint32_t C = kSegEntries / 32u;
   __shared__ SegTables tables;
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   seg_tables_load(a, tables);
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt = lanemask_lt();
@@ -430,10 +430,10 @@ __global__ void __launch_bounds__(256) k_seg_scatter(FrameArgs a) {
 
 // Verification readback of the 20-bit log-depth keys: for every final entry
 // i of tile t, sorted_keys[i] = t << (20+R) | k20 << R | sortRank (k20: the
-// tile's log-depth mapping, gpu_tile_bucket_sort.wgsl:240-250, scaled to
+// tile's log-depth mapping, gpu_tile_bucket_sort.wgsl:75-85, scaled to
 // 2^20). One warp per tile.
 __global__ void __launch_bounds__(256) k_log_depth_keys(FrameArgs a) {
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -488,7 +488,7 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
 // the union over both: a reader then visits a chunk that may hold none of its
 // tile's entries, which costs time only.
 __global__ void __launch_bounds__(256) k_chunk_masks(FrameArgs a) {
-  if (a.ctl[kCtlFlags] & 0x1u) return;
+  if (a.ctl[kCtlFlags] & kSkipFlags) return;
   const uint32_t Q = a.ctl[kCtlSbPairs];
   const uint32_t chunks = (Q + kChunkEntries - 1u) / kChunkEntries;
   const uint32_t lane = threadIdx.x & 31u;

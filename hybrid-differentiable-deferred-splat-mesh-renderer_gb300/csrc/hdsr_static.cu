@@ -11,7 +11,10 @@
 //     grids are rejected with HDSR_ERR_UNSUPPORTED before any device work;
 //   - set-up: the first call on a device, with that device current, looks
 //     the array's device address up once (cudaGetSymbolAddress) and keeps it
-//     per device; that first call should come before any stream capture;
+//     per device; that first call should come before any stream capture.
+//     The kept address belongs to the device's primary context: after
+//     cudaDeviceReset it is stale, so callers must not use the entry point
+//     again in that process;
 //   - nothing has to start at zero: every call zeroes the grid words it uses
 //     and the whole output in its first kernel;
 //   - calls on one device share the scratch: two calls whose kernels overlap
@@ -28,7 +31,7 @@ namespace {
 constexpr uint32_t kStaticDiffWords = 256u * 256u;
 constexpr int kStaticMaxDevices = 64;
 
-__device__ __align__(256) int g_static_diff[kStaticDiffWords];
+static __device__ __align__(256) int g_static_diff[kStaticDiffWords];
 
 std::mutex g_static_mu;
 int* g_static_ptr[kStaticMaxDevices] = {};

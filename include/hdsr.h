@@ -224,6 +224,18 @@ const char* hdsr_pass_name(uint32_t id);
 /* Number of kernels this handle has queued since creation. */
 uint64_t hdsr_launch_count(const hdsr_compositor* h);
 
+/* Bounded device waits (no reference counterpart: WebGPU has no
+ * inter-workgroup waits; the reference's three-pass scan,
+ * gpu_prefix_sum.wgsl:14-85, needs none). Each scan tile waits for its
+ * predecessors' status words at most `spin_limit` spins of about 100 ns
+ * (0 selects the default, 2^22); a wait that runs out sets HDSR_DEV_TIMEOUT,
+ * every later kernel of the frame returns without writing (the output images
+ * keep their previous contents), and hdsr_query_status returns
+ * HDSR_ERR_TIMEOUT. `withheld_tile` (test hook; 0xFFFFFFFF = none) makes that
+ * tile of each scan compute its prefix but post nothing, so that its
+ * successors' waits run out. Drops the handle's frame graph. */
+hdsr_status hdsr_set_scan_wait(hdsr_compositor* h, uint32_t spin_limit, uint32_t withheld_tile);
+
 /* Gradients of one frame (no reference counterpart: the reference renders
  * only). Input: dL/d(color output) as rgba f32 per pixel. Outputs, written
  * (not accumulated), in the layouts of hdsr_scene_views, indexed by splat id:
@@ -318,14 +330,19 @@ const char* hdsr_server_last_error(const hdsr_server* s);
  * without any device allocation and without a handle. No reference
  * counterpart: the reference only counts inside its full pipeline.
  *   tile_boxes: device u32 tile boxes (u8 x0, y0, x1, y1; 0xFFFFFFFF =
- *     invisible), one every box_stride_words words (1: packed; 2: the
- *     handle's HDSR_BUF_CACHE_AUX stream; 14: the reference cache rows);
+ *     invisible), one every box_stride_words words, tile_boxes pointing at
+ *     the first box (1: packed; 2: the handle's HDSR_BUF_CACHE_AUX stream;
+ *     14: the reference's projection cache rows, whose box is word 7, so
+ *     tile_boxes = cache + 7);
  *   tile_counts: device, tile_counts_len >= the plan's morton_tile_count
  *     words; written in Morton order, every other word set to 0.
  * Scratch is a static 256 KiB device array (a grid of <= 256 x 256 words):
  * tile grids beyond 255 x 255 tiles return HDSR_ERR_UNSUPPORTED. The first
- * call on a device (made with that device current) looks the scratch up;
- * make it before capturing a stream. Nothing needs to start at zero. Calls
+ * call on a device (made with that device current) looks the scratch up and
+ * keeps its address for the life of the process; make it before capturing a
+ * stream. After cudaDeviceReset (or anything else that destroys the device's
+ * primary context) the kept address is stale: do not call this function
+ * again in that process. Nothing needs to start at zero. Calls
  * on one device share the scratch: calls that may run concurrently race.
  * Asynchronous on `stream`; returns launch errors only. */
 hdsr_status hdsr_count_tile_refs_static(const uint32_t* tile_boxes, uint32_t box_stride_words,

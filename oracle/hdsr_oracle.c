@@ -536,7 +536,7 @@ static int cmp_bucket_entry(const void* a, const void* b) {
 }
 
 /* Per-tile log-depth mapping shared by the bucket cascade and the k20 keys
- * (gpu_tile_bucket_sort.wgsl:240-244). */
+ * (gpu_tile_bucket_sort.wgsl:75-79, bucket :85). */
 typedef struct { float logMin; float bucketScale; float keyScale; } tile_log;
 
 static tile_log tile_log_params(uint32_t dminBits, uint32_t dmaxBits) {
@@ -688,7 +688,7 @@ int orc_render_frame(const float* U, const orc_scene* s, orc_frame* f, int threa
     for (uint32_t b = 0; b < NUM_BUCKETS; ++b) bucketOffsets[b + 1] = bucketOffsets[b] + bucketCounts[b];
     for (uint32_t i = 0; i < count; ++i) e[i] = (uint32_t)tmp[i].key;
     free(tmp);
-    /* phase 5: greedy chunk pack (gpu_tile_bucket_sort.wgsl:276-307) */
+    /* phase 5: greedy chunk pack (gpu_tile_bucket_sort.wgsl:110-143) */
     uint32_t chunkStart = 0, cur = 0;
     for (uint32_t b = 0; b < NUM_BUCKETS; ++b) {
       uint32_t rem = bucketOffsets[b + 1] - bucketOffsets[b];
@@ -1224,7 +1224,7 @@ void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n) { for (uint64_
 void orc_f64_to_f16_n(const double* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f64_to_f16_rne(in[i]); }
 void orc_composite_expf_n(const float* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_composite_expf(in[i]); }
 void orc_morton_n(const uint32_t* x, const uint32_t* y, uint32_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_morton(x[i], y[i]); }
-/* bucket (gpu_tile_bucket_sort.wgsl:250) and k20 of depths against one
+/* bucket (gpu_tile_bucket_sort.wgsl:85) and k20 of depths against one
  * tile's (min, max) depth bits; used to check bucket == k20 >> 13. */
 void orc_bucket_key20_n(const uint32_t* depth_bits, uint64_t n, uint32_t dmin, uint32_t dmax,
                         uint32_t* buckets, uint32_t* keys) {

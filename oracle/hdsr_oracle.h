@@ -10,12 +10,12 @@
  *   src/shaders/gpu_project_splats.wgsl:75-358          project_splats
  *   src/shaders/gpu_classify_large_splats.wgsl:33-66     classify_large_splats
  *   src/shaders/gpu_tile_splat_composite.wgsl:33-119     morton, count, scatter
- *   src/shaders/gpu_large_splat_scatter.wgsl:118-155     cooperative scatter
- *   src/shaders/gpu_prefix_sum.wgsl:169-240              3-pass exclusive scan
+ *   src/shaders/gpu_large_splat_scatter.wgsl:52-89       cooperative scatter
+ *   src/shaders/gpu_prefix_sum.wgsl:14-85                3-pass exclusive scan
  *   src/shaders/gpu_tile_classify.wgsl:44-86             small / hot tile lists
- *   src/shaders/gpu_tile_depth_sort.wgsl:114-165         per-tile bitonic
- *   src/shaders/gpu_tile_bucket_sort.wgsl:206-309        hot-tile cascade
- *   src/shaders/gpu_tile_chunk_sort.wgsl:345-406         chunk sort
+ *   src/shaders/gpu_tile_depth_sort.wgsl:28-79           per-tile bitonic
+ *   src/shaders/gpu_tile_bucket_sort.wgsl:41-144         hot-tile cascade
+ *   src/shaders/gpu_tile_chunk_sort.wgsl:36-97           chunk sort
  *   src/shaders/gpu_tile_splat_composite.wgsl:162-370    composite
  *   src/gpuTileSplatCompositor.ts:109-139                 plan
  *   src/splatSort.ts:32-55,178-195                        CPU depth sort (baseline)
@@ -27,8 +27,17 @@
  * tests (tests/cpuDepthSort.test.ts, tests/renderer/
  * computeCompositorLifecycle.test.mjs); the compositor passes themselves
  * (tile counts, offsets, per-tile order, pixels) are "parity unpinned": no
- * reference test or fixture fixes them, so this file is a transcription
- * checked by review and by property tests only.
+ * reference test or fixture fixes them. This file is a transcription of the
+ * shaders, checked three ways: by review against the shader text; by
+ * independent NumPy restatements written from the same shaders, which the
+ * CPU test suite compares with this file bit for bit (the projection cache
+ * row and depth at SH degrees 0-3 with baked and detail normals, emissive and
+ * material; the f32 composite's colour, alpha and G-buffer votes; the f16
+ * composite's colour and alpha); and by property tests (known-answer
+ * vectors, exp/log accuracy, Morton codes, bucket = k20 >> 13, the 4096/4097
+ * hot-tile threshold, ties, near-plane depths, every tile in (depth, rank)
+ * order, the FP64 twin). The projected covariance is also checked against
+ * the reference's own EWA witness (rendererFidelityProbes/conicProjection.js).
  *
  * Canonical order. The reference bins with atomics, so its per-tile order is
  * not reproducible when keys tie. This restatement fixes every such choice
@@ -61,10 +70,10 @@ extern "C" {
 #endif
 
 /* Reference-cap flags reported in orc_frame.flags. */
-#define ORC_FLAG_LARGE_SPLAT_CAP   1u  /* >65,535 large splats (classify_large_splats:52) */
-#define ORC_FLAG_REF_BUDGET_DROP   2u  /* total refs > maxTotalTileRefs (scatter:114)      */
-#define ORC_FLAG_OVERFLOW_SKIP     4u  /* bucket scratch overflow skip (bucket_sort:219)    */
-#define ORC_FLAG_CHUNK_CAP         8u  /* >1,024 chunks (chunk_sort:351)                    */
+#define ORC_FLAG_LARGE_SPLAT_CAP   1u  /* >65,535 large splats (classify_large_splats:52)  */
+#define ORC_FLAG_REF_BUDGET_DROP   2u  /* total refs > maxTotalTileRefs (scatter_tile_refs:114)  */
+#define ORC_FLAG_OVERFLOW_SKIP     4u  /* bucket scratch overflow skip (bucket_sort:54) */
+#define ORC_FLAG_CHUNK_CAP         8u  /* >1,024 chunks (bucket_sort:126,138)           */
 #define ORC_FLAG_BUCKET_KEY_MISMATCH 16u /* bucket != k20>>13 (must never happen)           */
 
 typedef struct {

@@ -13,7 +13,7 @@ to tests/golden/first_smoke_subset/:
     bounds are made (min, max, their midpoint, half the diagonal);
   - a "subset" record: the source manifest, its payload's sha256, the seed and
     the sha256 of every written sidecar.
-Usage: python tests/golden/make_first_smoke_subset.py [reference_root] [count]
+Usage: python tests/golden/make_first_smoke_subset.py <reference_root> [count]
 """
 from __future__ import annotations
 
@@ -95,5 +95,6 @@ def main(ref_root: Path, count: int) -> None:
 
 
 if __name__ == "__main__":
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    main(root, int(sys.argv[2]) if len(sys.argv) > 2 else 4096)
+    if len(sys.argv) not in (2, 3):
+        sys.exit("usage: make_first_smoke_subset.py <path of the reference checkout> [rows, default 4096]")
+    main(Path(sys.argv[1]), int(sys.argv[2]) if len(sys.argv) > 2 else 4096)

@@ -7,7 +7,7 @@ and cannot run here) and writes reference_kats.json:
   - tests/renderer/computeCompositorLifecycle.test.mjs: the compositor
     constants it asserts (dispatch-safe ref cap, 8-tile footprint clamp,
     projection-cache stride).
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py <reference_root>
 """
 from __future__ import annotations
 
@@ -89,4 +89,6 @@ def main(ref_root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference checkout>")
+    main(Path(sys.argv[1]))

@@ -387,14 +387,24 @@ def test_hot760k_full_frame_parity(cuda, pkg, orc):
     g = render_gpu(pkg, wl.scene, wl.cameras[0], wl.width, wl.height, pair_capacity=48_000_000)
     gpu, ref = assert_frame_parity(orc, g, check_keys=False)
     assert ref["hot_tiles"] >= 20
-    # radix output: sorted, and a permutation of the pair multiset (size-
-    # independent properties; the oracle's own key list is checked on the
-    # smaller frames above)
+    # every (Morton tile, 20-bit log-depth key, sortRank) of the ~40M pairs,
+    # bit for bit against the oracle's key list. The oracle orders a tile's
+    # keys by (k20, sortRank); the GPU list is in the frame's (depth bits,
+    # sortRank) order, whose k20 is non-decreasing (the log is monotone), so
+    # the GPU list sorted as u64 words must equal the oracle's words.
     gk = gpu["sorted_keys"]
-    assert np.all(gk[1:] >= gk[:-1])
     R = np.uint64(gpu["rank_bits"])
-    tiles = (gk >> (R + np.uint64(20))).astype(np.int64)
-    assert np.array_equal(np.bincount(tiles, minlength=len(ref["tile_counts"])), ref["tile_counts"].astype(np.int64))
+    assert np.array_equal((gk & ((np.uint64(1) << R) - np.uint64(1))).astype(np.uint32), ref["tile_entries"])
+    assert np.all((gk >> R)[1:] >= (gk >> R)[:-1])
+    keys, vals = orc.sorted_keys20(g["u"], ref["proj_cache"], ref["depth"])
+    assert len(keys) == len(gk) == ref["total_pairs"]
+    want = (keys << R) | vals.astype(np.uint64)
+    del keys, vals
+    assert np.all(want[1:] > want[:-1])
+    got = np.sort(gk)
+    bad = np.flatnonzero(got != want)
+    assert bad.size == 0, f"{bad.size} of {len(want)} keys differ, first at {bad[:5].tolist()}"
+    del got, want
     err, psnr = _fp64_error(orc, g, gpu, ref)
     assert psnr >= 50.0, (err, psnr)
     g["res"].destroy()

@@ -47,8 +47,13 @@ def test_static_counts_match_full_frame_two_calls_in_a_row(cuda, pkg, orc, hdsr_
         plan = g["plan"]
         aux = g["res"].buffer("cache_aux", count=2 * plan.splat_count)
         out = torch.full((plan.morton_tile_count,), -1, dtype=torch.int32, device="cuda")
+        # the fill above ran on the current stream: order the side stream
+        # after it, and keep both tensors alive for the side stream's use
+        stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(stream):
             rc = _static_counts(pkg, hdsr_lib, aux.data_ptr(), 2, plan.splat_count, plan, out, stream)
+        out.record_stream(stream)
+        aux.record_stream(stream)
         assert rc == 0
         outs.append(out)
     stream.synchronize()
@@ -66,6 +71,19 @@ def test_static_counts_match_full_frame_two_calls_in_a_row(cuda, pkg, orc, hdsr_
         assert _static_counts(pkg, hdsr_lib, aux.data_ptr(), 2, plan.splat_count, plan, out) == 0
         torch.cuda.synchronize()
         assert np.array_equal(u32(out), u32(g["res"].buffer("tile_counts")))
+    # the reference's 14-word projection cache rows: the tile box is word 7,
+    # so the caller passes the address of row 0's word 7 with stride 14
+    g = frames[0]
+    plan = g["plan"]
+    aux = g["res"].buffer("cache_aux", count=2 * plan.splat_count).view(-1, 2)
+    rows = torch.zeros((plan.splat_count, 14), dtype=torch.int32, device="cuda")
+    rows[:, 7] = aux[:, 0]
+    rows[:, 0:7] = -1  # other words hold unrelated bits
+    rows[:, 8:] = -1
+    out = torch.full((plan.morton_tile_count,), 3, dtype=torch.int32, device="cuda")
+    assert _static_counts(pkg, hdsr_lib, rows.data_ptr() + 7 * 4, 14, plan.splat_count, plan, out) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(u32(out), u32(g["res"].buffer("tile_counts")))
     for g in frames:
         g["res"].destroy()
 
