@@ -308,6 +308,34 @@ def plan(W, H, tile, N, mult=16.0) -> np.ndarray:
     return out
 
 
+def frame_uniforms(plan_words, view_proj, splat_scale=1.0, sh_degree=0, camera_pos=None, view_matrix=None,
+                   proj_matrix=None, normal_matrix=None) -> np.ndarray:
+    """writeTileSplatFrameUniforms (gpuTileSplatCompositor.ts:730-774) over the
+    9 words of plan(): the 64-float block, u32 fields stored as their bits.
+    The focal terms are JS double products stored to f32 (:765-766)."""
+    W, H, tile, cols, rows, _, _, N, budget = (int(x) for x in plan_words)
+    t = np.zeros(64, np.float32)
+    tu = t.view(np.uint32)
+    t[0:16] = np.asarray(view_proj, np.float32).reshape(-1)
+    t[16], t[17], t[18], t[19] = W, H, tile, 0.0
+    tu[20], tu[21], tu[22], tu[23] = cols, rows, N, budget
+    t[24] = splat_scale
+    tu[25] = sh_degree
+    if camera_pos is not None:
+        t[28:31] = np.asarray(camera_pos, np.float32).reshape(-1)[:3]
+    if view_matrix is not None:
+        t[32:48] = np.asarray(view_matrix, np.float32).reshape(-1)
+    if proj_matrix is not None:
+        pm = np.asarray(proj_matrix, np.float32).reshape(-1)
+        t[48] = np.float32(float(W) * float(pm[0]) * 0.5)
+        t[49] = np.float32(float(H) * float(pm[5]) * 0.5)
+    nm = [1, 0, 0, 0, 1, 0, 0, 0, 1] if normal_matrix is None else np.asarray(normal_matrix, np.float32).reshape(-1)
+    for c in range(3):
+        t[52 + 4 * c: 55 + 4 * c] = nm[3 * c: 3 * c + 3]
+        t[55 + 4 * c] = 0.0
+    return t
+
+
 # ---------------------------------------------------------------------------
 # deferred frame tail (hdsr_post_oracle.c)
 # ---------------------------------------------------------------------------

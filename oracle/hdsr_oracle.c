@@ -1104,6 +1104,9 @@ int orc_render_frame_f64(const float* U, const orc_scene* s, const uint32_t* cou
       for (uint32_t px = tx * 16; px < tx * 16 + 16 && px < W; ++px) {
         double T = 1.0, c[3] = {0, 0, 0};
         for (uint32_t k = 0; k < counts[t]; ++k) {
+          /* T never grows, so once below the cutoff no later entry is valid:
+           * stopping here changes nothing */
+          if (!(T >= 0.001)) break;
           const proj64* g = &pj[entries[(uint64_t)offsets[t] + k]];
           double dx = px + 0.5 - g->cx, dy = py + 0.5 - g->cy;
           double pw = -0.5 * g->ia * dx * dx - 0.5 * g->ic * dy * dy - g->ib * dx * dy;

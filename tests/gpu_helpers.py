@@ -76,7 +76,8 @@ def cache_words(gpu: dict) -> np.ndarray:
 def assert_frame_parity(orc, g, gpu=None, check_keys=True):
     """Bit-exact comparison of every stage with the oracle's canonical frame."""
     gpu = gpu or read_gpu(g)
-    ref = orc.render_frame(g["u"], g["packed"], g["order"], f16=g.get("f16", False))
+    # the GPU's pair count sizes the oracle's entry list (one pass, no regrow)
+    ref = orc.render_frame(g["u"], g["packed"], g["order"], f16=g.get("f16", False), cap=gpu["P"] + 16)
     assert gpu["status"]["status"] == 0, gpu["status"]
     assert gpu["P"] == ref["total_pairs"]
     # projection cache (visible splats: every word; invisible: the sentinel)

@@ -408,3 +408,47 @@ def test_hot760k_full_frame_parity(cuda, pkg, orc):
     err, psnr = _fp64_error(orc, g, gpu, ref)
     assert psnr >= 50.0, (err, psnr)
     g["res"].destroy()
+
+
+def test_sh3_3m_4k_orbit_parity_and_fp64_error_per_view(cuda, pkg, orc):
+    """3M Gaussians, SH degree 3 (48 coefficients), 3840x2160, 8-camera orbit
+    at radius 6. View 0: every stage against the oracle, bit for bit (about
+    500M pairs). Every view: the image against the FP64 twin over the frame's
+    own entry lists (max |err| and PSNR per view; threshold PSNR >= 50 dB)."""
+    import torch
+
+    wl = pkg.workloads.sh3_3m()
+    packed = pkg.splats.pack_splat_attributes(wl.scene)
+    plan = pkg.plan_tile_splat_compositor(wl.width, wl.height, 16, wl.scene.count)
+    res = pkg.create_tile_splat_compositor(plan, pair_capacity=640_000_000)
+    color, gb = pkg.create_output_textures(plan)
+    errors = []
+    for i, cam in enumerate(wl.cameras):
+        u, fr = pkg.frame_uniforms_for(plan, cam, sh_degree=3)
+        order = pkg.splats.back_to_front_order(packed.positions, fr["view"])
+        bufs = pkg.splats.upload_splat_attribute_buffers(packed, order)
+        pkg.create_tile_splat_bind_groups(res, bufs, color, gb)
+        pkg.write_frame_uniform_buffer(res, u)
+        pkg.encode_full_compute_compositor_pipeline(None, res)
+        torch.cuda.synchronize()
+        g = dict(res=res, plan=plan, u=u, packed=packed, order=order, color=color, gb=gb, bufs=bufs)
+        gpu = read_gpu(g)
+        assert gpu["status"]["status"] == 0, gpu["status"]
+        if i == 0:
+            gpu, ref = assert_frame_parity(orc, g, gpu=gpu)
+            assert ref["hot_tiles"] > 0
+            del ref
+        frame = dict(tile_counts=gpu["tile_counts"], tile_offsets=gpu["tile_offsets"],
+                     tile_entries=gpu["tile_entries"])
+        f64 = orc.render_frame_f64(u, packed, order, frame)
+        got = gpu["color"].astype(np.float64)
+        err = float(np.abs(got - f64).max())
+        mse = float(np.mean((got[..., :3] - f64[..., :3]) ** 2))
+        psnr = 10.0 * math.log10(1.0 / max(mse, 1e-30))
+        errors.append((i, gpu["P"], err, psnr))
+        del gpu, f64, got, bufs
+    print("sh3_3m per view (view, pairs, max |err| vs FP64, PSNR dB):", errors)
+    for i, P, err, psnr in errors:
+        assert P > 100_000_000, (i, P)
+        assert psnr >= 50.0, (i, err, psnr)
+    res.destroy()

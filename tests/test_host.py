@@ -85,6 +85,18 @@ def test_frame_uniform_layout(pkg):
     assert u[60:63].tolist() == [56, 57, 58] and u[63] == 0
 
 
+@pytest.mark.parametrize("W,H,N,deg", [(1920, 1080, 760_000, 0), (3840, 2160, 3_000_000, 3), (203, 117, 7, 1)])
+def test_oracle_frame_uniforms_match_the_c_abi(pkg, orc, W, H, N, deg):
+    # the reference arm of the benchmark builds its uniform blocks with the
+    # oracle (no product library): the same 64 words as the C ABI's writer
+    plan = pkg.plan_tile_splat_compositor(W, H, 16, N)
+    cam = pkg.camera.OrbitCamera(azimuth=0.7, elevation=0.3, distance=5.5)
+    u, fr = pkg.frame_uniforms_for(plan, cam, sh_degree=deg)
+    o = orc.frame_uniforms(orc.plan(W, H, 16, N), fr["view_proj"], 1.0, deg, fr["camera_pos"], fr["view"],
+                           fr["proj"], None)
+    assert np.array_equal(o.view(np.uint32), u.view(np.uint32))
+
+
 def test_frame_uniform_defaults(pkg):
     plan = pkg.plan_tile_splat_compositor(800, 600, 16, 10)
     u = pkg.write_tile_splat_frame_uniforms(None, np.eye(4, dtype=np.float32).reshape(-1), plan)
