@@ -239,6 +239,10 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
   ALLOC(a.tile_digits, (uint64_t)a.radix_tiles_cap * kRadixBins, "tile_digits");
   ALLOC(a.bin_base, (uint64_t)kRadixBins, "bin_base");
+  a.dsort_tiles_cap = depth_sort_tiles(N);
+  ALLOC(a.dsort_hist0, (uint64_t)depth_sort_bins() * a.dsort_tiles_cap, "depth_sort_counts_0");
+  ALLOC(a.dsort_hist1, (uint64_t)depth_sort_bins() * a.dsort_tiles_cap, "depth_sort_counts_1");
+  ALLOC(a.dsort_total, (uint64_t)depth_sort_bins(), "depth_sort_totals");
   ALLOC(a.scan_status_n, scan_tiles_n, "scan_status_n");
   ALLOC(a.scan_status_m, scan_tiles_m, "scan_status_m");
   ALLOC(a.ctl, (uint64_t)kCtlWords, "ctl");
@@ -454,24 +458,16 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   if ((e = launch_scan_tiles(a, ts)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
   mark(h, s, 5);
   if (fork && (e = cudaEventRecord(h->join_ev, ts)) != cudaSuccess) return cuda_fail(h, e, "fork");
-  // splats: 4 passes over the 32 depth bits -> order (sortRanks by depth)
+  // splats: as many 9-bit passes as the frame's depth range needs -> order
+  // (sortRanks by depth)
+  if ((e = launch_depth_sort(a, s)) != cudaSuccess) return cuda_fail(h, e, "depth_sort");
+  mark(h, s, 6);
   RadixJob dj{};
-  dj.count = a.ctl + kCtlSplats;
   dj.flags = a.ctl + kCtlFlags;
   dj.tile_digits = a.tile_digits;
   dj.bin_base = a.bin_base;
   dj.tiles_cap = a.radix_tiles_cap;
-  dj.out_low = a.order;
   dj.low_mask = 0xFFFFFFFFull;
-  for (uint32_t p = 0; p < kDepthPasses; ++p) {
-    dj.in = (p & 1u) ? a.dkeys_b : a.dkeys_a;
-    dj.out = (p & 1u) ? a.dkeys_a : a.dkeys_b;
-    dj.shift = 32u + 8u * p;
-    dj.bits = 8u;
-    if ((e = launch_radix_pass(dj, p + 1 == kDepthPasses, a.num_sms, s)) != cudaSuccess)
-      return cuda_fail(h, e, "depth_sort");
-  }
-  mark(h, s, 6);
   // the superblock lists need the tile scan's totals and overflow flag
   if (fork && (e = cudaStreamWaitEvent(s, h->join_ev, 0)) != cudaSuccess) return cuda_fail(h, e, "join");
   // superblock lists in depth order, sorted by superblock (stable)
@@ -501,7 +497,7 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
     if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
     h->launches += 2;
   }
-  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 3 * kDepthPasses + 1 +
+  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 9 * n_splat_launch + 1 +
                  3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 1 : 0);
   return HDSR_OK;
 }

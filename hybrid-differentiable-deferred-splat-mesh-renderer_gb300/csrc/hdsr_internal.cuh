@@ -17,6 +17,10 @@ enum Ctl : int {
   kCtlSplats = 4,      // N, the depth sort's key count (constant per handle)
   kCtlSbPairs = 10,    // Q, (superblock, splat) list entries of the frame
   kCtlSegments = 11,   // 256-entry segments of the superblock lists
+  kCtlDepthMin = 12,   // depth sort: least depth bits of a visible splat (starts at 0xFFFFFFFF)
+  kCtlDepthMax = 13,   // depth sort: greatest
+  kCtlDepthBase = 14,  // depth sort: subtracted from visible keys
+  kCtlDepthPasses = 15,// depth sort: 9-bit passes this frame (1-4)
   kCtlHotTiles = 5,
   kCtlChunks = 6,
   kCtlVisible = 7,
@@ -136,6 +140,10 @@ struct FrameArgs {
   uint32_t* tile_digits;
   uint32_t* bin_base;
   uint32_t radix_tiles_cap;
+  uint32_t* dsort_hist0;          // depth sort: per-block digit counts -> offsets, bin-major (even passes)
+  uint32_t* dsort_hist1;          // (odd passes)
+  uint32_t* dsort_total;          // per digit: the pass's total
+  uint32_t dsort_tiles_cap;       // blocks of kRadixTile keys (+1)
   unsigned long long* scan_status_n; // per kScanTile-element tile of the N scan
   unsigned long long* scan_status_m;
   uint32_t* ctl;
@@ -331,6 +339,10 @@ cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
 cudaError_t launch_chunk_masks(const FrameArgs& a, cudaStream_t s);   // 1 launch
 cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 3 launches
+// the frame's depth sort (hdsr_dsort.cu): a.dkeys_a -> a.order, 9 launches
+cudaError_t launch_depth_sort(const FrameArgs& a, cudaStream_t s);
+uint32_t depth_sort_tiles(uint32_t N);  // blocks of its tables (dsort_tiles_cap)
+uint32_t depth_sort_bins();             // digits of a pass
 cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 // back-to-front order of the bound positions for a view matrix (row 2 of the
 // view transform: view[2], view[6], view[10], view[14]) into `out`

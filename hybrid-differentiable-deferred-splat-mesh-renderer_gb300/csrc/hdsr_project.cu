@@ -68,6 +68,7 @@ __global__ void k_frame_init(FrameArgs a) {
     a.ctl[kCtlEpoch] += 1u;
     for (int k = 1; k < kCtlWords; ++k) a.ctl[k] = 0u;
     a.ctl[kCtlSplats] = a.N;
+    a.ctl[kCtlDepthMin] = 0xFFFFFFFFu;
   }
   if (i < a.M) {
     a.tile_cnt[i] = 0u;

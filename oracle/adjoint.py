@@ -214,16 +214,19 @@ def project_dual(U, packed, order):
     return screen, visible, lay
 
 
-def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray) -> np.ndarray:
+def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray, with_abs: bool = False):
     """dL/d(cx, cy, ia, ib, ic, op, r, g, b) per sortRank for dL/d(output
     rgba) = d_out (H, W, 4), over the frame's entry lists; FP64 values of
-    the screen parameters come from `screen`."""
+    the screen parameters come from `screen`. With `with_abs`, also the sums
+    of the absolute per-pixel terms (the magnitude an fp32 sum of those terms
+    is rounded against)."""
     U = np.asarray(U, np.float32)
     Uu = U.view(np.uint32)
     cols, rows = int(Uu[20]), int(Uu[21])
     W, H = int(U[16]), int(U[17])
     par = np.stack([screen[k].v for k in ("cx", "cy", "ia", "ib", "ic", "op", "r", "g", "b")], 1)
     g2d = np.zeros_like(par)
+    gabs = np.zeros_like(par)
     counts, offs, ents = frame["tile_counts"], frame["tile_offsets"], frame["tile_entries"]
     bg = np.array([0.02, 0.02, 0.04])
     gy, gx = np.mgrid[0:16, 0:16]
@@ -267,34 +270,52 @@ def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray) -> np.nda
             dL_da = np.where(valid & ~capped, dL_da, 0.0)
             dL_dcol = (wgt[:, :, None] * dC[None, :, :]).sum(1)      # (K, 3)
             dL_dpw = dL_da * a
+            terms = [dL_dpw * (ia * dx + ib * dy), dL_dpw * (ic * dy + ib * dx), dL_dpw * (-0.5 * dx * dx),
+                     dL_dpw * (-dx * dy), dL_dpw * (-0.5 * dy * dy), dL_da * ex]
             g = np.zeros((K, 9))
-            g[:, 0] = (dL_dpw * (ia * dx + ib * dy)).sum(1)
-            g[:, 1] = (dL_dpw * (ic * dy + ib * dx)).sum(1)
-            g[:, 2] = (dL_dpw * (-0.5 * dx * dx)).sum(1)
-            g[:, 3] = (dL_dpw * (-dx * dy)).sum(1)
-            g[:, 4] = (dL_dpw * (-0.5 * dy * dy)).sum(1)
-            g[:, 5] = (dL_da * ex).sum(1)
+            for j, tm in enumerate(terms):
+                g[:, j] = tm.sum(1)
             g[:, 6:9] = dL_dcol
             np.add.at(g2d, e, g)
-    return g2d
+            if with_abs:
+                ga = np.zeros((K, 9))
+                for j, tm in enumerate(terms):
+                    ga[:, j] = np.abs(tm).sum(1)
+                ga[:, 6:9] = (wgt[:, :, None] * np.abs(dC)[None, :, :]).sum(1)
+                np.add.at(gabs, e, ga)
+    return (g2d, gabs) if with_abs else g2d
 
 
-def reference_gradient(U, packed, order, frame: dict, d_out: np.ndarray) -> dict:
+def reference_gradient(U, packed, order, frame: dict, d_out: np.ndarray, with_scale: bool = False):
     """dL/d(parameters) per splat id in the layouts of hdsr_scene_views, for
-    dL/d(output rgba) = d_out, in FP64."""
+    dL/d(output rgba) = d_out, in FP64. With `with_scale`, also (second
+    value) per parameter the sum over pixels of the absolute value of each
+    pixel's contribution (through the same chain rule, term by term): the
+    magnitude against which an fp32 evaluation of the gradient's sums is
+    rounded, used to bound the error such an evaluation may carry."""
     screen, visible, lay = project_dual(U, packed, order)
-    g2d = composite_adjoint(U, screen, frame, np.asarray(d_out, np.float64))
+    res = composite_adjoint(U, screen, frame, np.asarray(d_out, np.float64), with_abs=with_scale)
+    g2d, gabs = res if with_scale else (res, None)
     keys = ("cx", "cy", "ia", "ib", "ic", "op", "r", "g", "b")
-    per_rank = sum(screen[k].d * g2d[:, i:i + 1] for i, k in enumerate(keys))
-    per_rank[~visible] = 0.0
     n = int(packed.count)
-    per_id = np.zeros_like(per_rank)
-    per_id[np.asarray(order, np.int64)] = per_rank
-    out = {name: per_id[:, lay[name]] for name in ("positions", "log_scales", "rotations", "opacities", "sh")}
-    out["opacities"] = out["opacities"].reshape(n)
-    out["sh"] = out["sh"].copy()
-    out["sh"][:, lay["sh_width"] - 3:] = 0.0  # emissive slots: no effect on the colour output
-    return out
+    ids = np.asarray(order, np.int64)
+
+    def per_splat(rows, absolute):
+        if absolute:
+            pr = sum(np.abs(screen[k].d) * rows[:, i:i + 1] for i, k in enumerate(keys))
+        else:
+            pr = sum(screen[k].d * rows[:, i:i + 1] for i, k in enumerate(keys))
+        pr[~visible] = 0.0
+        per_id = np.zeros_like(pr)
+        per_id[ids] = pr
+        out = {name: per_id[:, lay[name]] for name in ("positions", "log_scales", "rotations", "opacities", "sh")}
+        out["opacities"] = out["opacities"].reshape(n)
+        out["sh"] = out["sh"].copy()
+        out["sh"][:, lay["sh_width"] - 3:] = 0.0  # emissive slots: no effect on the colour output
+        return out
+
+    grads = per_splat(g2d, False)
+    return (grads, per_splat(gabs, True)) if with_scale else grads
 
 
 def _morton(x: int, y: int) -> int:

@@ -140,7 +140,7 @@ def test_gradients_match_the_fp64_reference_gradient(cuda, pkg, orc):
     weights = rng.standard_normal((plan.viewport_height, plan.viewport_width, 4)).astype(np.float32)
     G = _gpu_gradients(pkg, renderer, tens, u, weights)
     frame = orc.render_frame(u, packed, order)
-    R = adjoint.reference_gradient(u, packed, order, frame, weights.astype(np.float64))
+    R, Rabs = adjoint.reference_gradient(u, packed, order, frame, weights.astype(np.float64), with_scale=True)
     par = orc.project_f64(u, packed, order)
     flagged = adjoint.threshold_adjacent_ranks(u, par, frame)
     ids = np.asarray(order, np.int64)
@@ -151,9 +151,15 @@ def test_gradients_match_the_fp64_reference_gradient(cuda, pkg, orc):
     for gname, width in (("positions", 3), ("log_scales", 3), ("rotations", 4), ("opacities", 1), ("sh", 12)):
         g = G[gname].reshape(sc.count, -1)[clean][:, :width].astype(np.float64)
         r = R[gname].reshape(sc.count, -1)[clean][:, :width]
+        ra = Rabs[gname].reshape(sc.count, -1)[clean][:, :width]
         scale = np.sqrt(np.mean(r ** 2))
         rel = np.abs(g - r) / np.maximum(np.abs(r), 1e-2 * scale)
         report[gname] = (int(rel.size), float(rel.max()), float(np.median(rel)))
+        worst = np.argsort(rel.reshape(-1))[-4:]
+        print(gname, "worst: rel, |r|/rms, |g-r|/sum|terms|, sum|terms|/|r|",
+              [(float(rel.reshape(-1)[i]), float(np.abs(r).reshape(-1)[i] / scale),
+                float(np.abs(g - r).reshape(-1)[i] / max(ra.reshape(-1)[i], 1e-300)),
+                float(ra.reshape(-1)[i] / max(abs(r.reshape(-1)[i]), 1e-300))) for i in worst])
     print("GPU adjoint vs FP64 reference gradient (parameters, max rel, median rel):", report)
     for gname, (cnt, worst, _) in report.items():
         assert worst <= 1e-3, (gname, worst)
