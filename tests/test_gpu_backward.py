@@ -128,8 +128,12 @@ def test_gradients_match_the_fp64_reference_gradient(cuda, pkg, orc):
     sub-scene against the oracle's analytic FP64 gradient (forward-mode
     projection, reverse composite: oracle/adjoint.py, itself pinned to FP64
     central differences on the CPU). Masked: only the threshold-adjacent
-    splats. Tolerance: 1e-3 relative per parameter, floored at 1e-2 of the
-    group's RMS gradient (the fp32 sums over pixels carry ~1e-5 of it)."""
+    splats. Tolerance: 1e-3 relative per parameter. The denominator is
+    floored at 1e-2 of the group's RMS gradient and at 1e-3 of S, the sum of
+    the absolute per-pixel terms the gradient adds up (returned by the
+    reference): an fp32 sum of such terms is rounded against S, not against
+    its result, so a gradient that cancels to far below S is held to 1e-6 S
+    absolute (about 16 ulps of S) rather than to a fraction of itself."""
     from oracle import adjoint
 
     sc, packed, plan, u, order = _sub_scene(pkg)
@@ -153,7 +157,7 @@ def test_gradients_match_the_fp64_reference_gradient(cuda, pkg, orc):
         r = R[gname].reshape(sc.count, -1)[clean][:, :width]
         ra = Rabs[gname].reshape(sc.count, -1)[clean][:, :width]
         scale = np.sqrt(np.mean(r ** 2))
-        rel = np.abs(g - r) / np.maximum(np.abs(r), 1e-2 * scale)
+        rel = np.abs(g - r) / np.maximum(np.maximum(np.abs(r), 1e-2 * scale), 1e-3 * ra)
         report[gname] = (int(rel.size), float(rel.max()), float(np.median(rel)))
         worst = np.argsort(rel.reshape(-1))[-4:]
         print(gname, "worst: rel, |r|/rms, |g-r|/sum|terms|, sum|terms|/|r|",
@@ -192,12 +196,19 @@ def test_autograd_matches_the_c_abi_and_trains(cuda, pkg):
                            torch.sigmoid(params[3]).detach(), params[4].detach(), srt, u)
     pkg.encode_backward(None, renderer.res, d_color, direct)
     torch.cuda.synchronize()
+    # float atomics add in a different order from run to run: equal up to
+    # that rounding, measured against each gradient array's scale (a
+    # gradient that cancels to near zero, such as the radial component of a
+    # quaternion's, is all rounding)
+    def close(a, b):
+        return torch.allclose(a, b, rtol=1e-4, atol=1e-5 * float(b.abs().max()))
+
     for p, k in zip(params[:3], ("positions", "log_scales", "rotations")):
         assert torch.isfinite(p.grad).all()
-        assert torch.allclose(p.grad, direct[k], rtol=1e-4, atol=1e-9), k
+        assert close(p.grad, direct[k]), k
     s = torch.sigmoid(params[3]).detach()
-    assert torch.allclose(params[3].grad, direct["opacities"] * s * (1 - s), rtol=1e-4, atol=1e-9)
-    assert torch.allclose(params[4].grad, direct["sh"], rtol=1e-4, atol=1e-9)
+    assert close(params[3].grad, direct["opacities"] * s * (1 - s))
+    assert close(params[4].grad, direct["sh"])
     assert float(params[0].grad.abs().sum()) > 0
     # the gradient is a descent direction: normalised steps on the positions
     # (at most 5e-4 per coordinate) lower the loss

@@ -1,9 +1,9 @@
 """Bounded device waits of the decoupled-lookback scans.
 
 A scan tile waits for its predecessors' status words; every such wait is
-bounded. The test hook of hdsr_set_scan_wait keeps one tile of each scan from
-posting its status, with a short spin limit, so the next tile's wait runs
-out: the frame must end (no hang), report HDSR_ERR_TIMEOUT with the timeout
+bounded. The test hook of hdsr_set_scan_wait keeps one tile of the tile scan
+from posting its status, with a short spin limit, so the next tile's wait
+runs out: the frame must end (no hang), report HDSR_ERR_TIMEOUT with the timeout
 device flag, leave the outputs untouched (the kernels after the scan return
 at once), and the same handle must render the exact frame again once the hook
 is cleared.
@@ -21,9 +21,10 @@ pytestmark = pytest.mark.gpu
 def test_withheld_scan_tile_times_out_and_the_handle_recovers(cuda, pkg, orc):
     import torch
 
-    # 20,000 splats: the per-splat scan has 10 tiles of 2,048 items
+    # 800x600: 3,364 Morton tiles, so the tile scan has 2 scan tiles of 2,048;
+    # tile 1 waits on tile 0
     scene = pkg.workloads.plain_scene(20_000, seed=5)
-    g = render_gpu(pkg, scene, pkg.camera.look_from((0.1, 0.2, 4.0)), 320, 240)
+    g = render_gpu(pkg, scene, pkg.camera.look_from((0.1, 0.2, 4.0)), 800, 600)
     res = g["res"]
     assert_frame_parity(orc, g)
     color = g["color"].clone()
@@ -31,7 +32,7 @@ def test_withheld_scan_tile_times_out_and_the_handle_recovers(cuda, pkg, orc):
     g["color"].fill_(0.25)
     g["gb"]["material"].fill_(7)
     torch.cuda.synchronize()
-    res.set_scan_wait(spin_limit=1000, withheld_tile=2)
+    res.set_scan_wait(spin_limit=1000, withheld_tile=0)
     t0 = time.perf_counter()
     pkg.encode_full_compute_compositor_pipeline(None, res)
     st = res.query_status()
@@ -53,10 +54,10 @@ def test_withheld_scan_tile_times_out_and_the_handle_recovers(cuda, pkg, orc):
 
 def test_withheld_last_tile_needs_no_wait(cuda, pkg, orc):
     # nobody waits on the last tile of a scan: withholding it changes nothing
-    scene = pkg.workloads.plain_scene(5_000, seed=6)  # 3 tiles of the per-splat scan
-    g = render_gpu(pkg, scene, pkg.camera.look_from((0.0, 0.1, 4.0)), 160, 128)
+    scene = pkg.workloads.plain_scene(5_000, seed=6)
+    g = render_gpu(pkg, scene, pkg.camera.look_from((0.0, 0.1, 4.0)), 800, 600)  # 2 scan tiles
     res = g["res"]
-    res.set_scan_wait(spin_limit=1000, withheld_tile=2)
+    res.set_scan_wait(spin_limit=1000, withheld_tile=1)
     pkg.encode_full_compute_compositor_pipeline(None, res)
     st = res.query_status()
     assert st["status"] == 0 and not (st["device_flags"] & pkg._lib.DEV_TIMEOUT), st
