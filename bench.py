@@ -418,6 +418,8 @@ def run_serve(pkg, args, dev) -> dict:
 
     # plain per-frame path
     handles = {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    device_ms = [0.0]
 
     def plain(sid, W, H, u, out):
         sc, bufs = scenes[sid]
@@ -427,8 +429,11 @@ def run_serve(pkg, args, dev) -> dict:
             handles[(sid, W, H)] = res
         pkg.create_tile_splat_bind_groups(res, bufs, out[0], out[1])
         pkg.write_frame_uniform_buffer(res, u)
+        ev0.record()
         pkg.encode_full_compute_compositor_pipeline(None, res)
+        ev1.record()
         st = res.query_status()
+        device_ms[0] += ev0.elapsed_time(ev1)
         if st["status"] == pkg._lib.HDSR_ERR_OVERFLOW:
             need = int(st["total_pairs"])
             res.destroy()
@@ -442,10 +447,21 @@ def run_serve(pkg, args, dev) -> dict:
     for sid, W, H, u in reqs:  # size every handle on the requests themselves
         plain(sid, W, H, u, outs[(W, H)][0])
     torch.cuda.synchronize()
+    device_ms[0] = 0.0
     t0 = time.perf_counter()
     for i, (sid, W, H, u) in enumerate(reqs):
         plain(sid, W, H, u, outs[(W, H)][i % ring])
     plain_s = time.perf_counter() - t0
+    plain_device_s = device_ms[0] / 1000.0
+    # the plain path per key (sequential frames of one key, the same handle)
+    key_plain = {}
+    for key in keys:
+        cams = [q[3] for q in reqs if q[:3] == key][:8]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for j, u in enumerate(cams):
+            plain(key[0], key[1], key[2], u, outs[(key[1], key[2])][j])
+        key_plain[key] = ((time.perf_counter() - t1) / len(cams), cams)
     for res in handles.values():
         res.destroy()
     handles.clear()
@@ -487,6 +503,23 @@ def run_serve(pkg, args, dev) -> dict:
                 tickets.append(server.submit(sid, u, color, gb))
             for t in tickets:
                 server.wait(t)
+    # concurrency ceiling per key: the same key's frames all queued at once
+    # (as many slots as max_in_flight) against its sequential plain frames;
+    # frames of one key overlap at least as well as a mixed batch can, so the
+    # mix's speedup is bounded by sum(plain) / sum(homogeneous) over its
+    # requests' keys
+    key_served = {}
+    for key, (t_plain, cams) in key_plain.items():
+        tickets = []
+        t1 = time.perf_counter()
+        for j, u in enumerate(cams):
+            color, gb = outs[(key[1], key[2])][j]
+            tickets.append(server.submit(key[0], u, color, gb))
+        for t in tickets:
+            server.wait(t)
+        key_served[key] = (time.perf_counter() - t1) / len(cams)
+    ceil_plain = sum(key_plain[q[:3]][0] for q in reqs)
+    ceil_served = sum(key_served[q[:3]] for q in reqs)
     log("serving: saturated run")
     sat_s, sat_res = run_batch()
     log(f"serving: {n_req / sat_s:.1f} frames/s saturated; Poisson run")
@@ -503,7 +536,17 @@ def run_serve(pkg, args, dev) -> dict:
             "speedup_vs_plain": round(plain_s / sat_s, 2), "offered_rps": round(rate, 1),
             "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
             "slots": st["slots"], "graphs": st["graphs"], "evictions": st["evictions"], "reruns": st["reruns"],
-            "slot_gb": round(st["slot_bytes"] / 2 ** 30, 2), "failed": bad, "max_in_flight": in_flight}
+            "slot_gb": round(st["slot_bytes"] / 2 ** 30, 2), "failed": bad, "max_in_flight": in_flight,
+            "plain_device_busy": round(plain_device_s / plain_s, 3),
+            "plain_device_ms_per_frame": round(plain_device_s * 1000.0 / n_req, 4),
+            "homogeneous_speedup_by_resolution": {
+                f"{w}x{h}": round(sum(key_plain[k][0] for k in keys if k[1:] == (w, h)) /
+                                  sum(key_served[k] for k in keys if k[1:] == (w, h)), 2) for w, h in SERVE_RESOLUTIONS},
+            "speedup_ceiling_from_homogeneous": round(ceil_plain / ceil_served, 2),
+            "ceiling_note": "frames of each (scene, viewport) key queued all at once through the server against the "
+                            "same frames one by one on the plain path (8 per key); the mix's bound is the sum of "
+                            "the per-key plain times over its requests divided by the sum of the per-key served "
+                            "times"}
 
 
 def run_ours(args, rank, world, local):

@@ -16,8 +16,7 @@ from pathlib import Path
 PKG_DIR = Path(__file__).resolve().parent
 CSRC = PKG_DIR / "csrc"
 LIB_NAME = "libhdsr.so"
-SOURCES = ["hdsr_api.cu", "hdsr_project.cu", "hdsr_scan.cu", "hdsr_sort.cu", "hdsr_dsort.cu", "hdsr_sblists.cu",
-           "hdsr_raster.cu",
+SOURCES = ["hdsr_api.cu", "hdsr_project.cu", "hdsr_scan.cu", "hdsr_sort.cu", "hdsr_dsort.cu", "hdsr_raster.cu",
            "hdsr_static.cu", "hdsr_backward.cu", "hdsr_backward_prep.cu", "hdsr_serve.cu",
            "hdsr_post.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

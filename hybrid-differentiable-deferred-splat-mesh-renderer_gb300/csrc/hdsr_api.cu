@@ -202,7 +202,8 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   const uint64_t sb_cap = (uint64_t)N * 9u;  // a tile box (<= 17 tiles a side) meets <= 3x3 superblocks
   a.sb_cap = sb_cap;
   a.seg_cap = (uint32_t)((sb_cap + kSegEntries - 1u) / kSegEntries + a.num_sb);
-  a.radix_tiles_cap = (uint32_t)(((uint64_t)N + kRadixTile - 1) / kRadixTile + 1);  // the back-to-front sort
+  a.radix_tiles_cap = (uint32_t)((sb_cap + kRadixTile - 1) / kRadixTile + 1);
+  const uint64_t scan_tiles_n = (N + kScanTile - 1) / kScanTile + 1;
   const uint64_t scan_tiles_m = (M + kScanTile - 1) / kScanTile + 1;
   hdsr_status s = HDSR_OK;
   float* U = nullptr;
@@ -220,9 +221,8 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.order, N, "depth_order");
   ALLOC(a.nsb, N, "superblock_counts");
   ALLOC(a.sb_off, N, "superblock_offsets");
-  ALLOC(a.sbk_b, sb_cap, "superblock_lists");
-  a.sb_tiles_cap = superblock_list_tiles(N);
-  ALLOC(a.sb_tab, (uint64_t)(a.num_sb + 1u) * a.sb_tiles_cap, "superblock_list_offsets");
+  ALLOC(a.sbk_a, sb_cap, "superblock_keys_a");
+  ALLOC(a.sbk_b, sb_cap, "superblock_keys_b");
   ALLOC(a.tile_diff, (uint64_t)(plan->tile_columns + 1) * (plan->tile_rows + 1), "tile_diff");
   ALLOC(a.sb_diff, (uint64_t)(a.sb_cols + 1) * (a.sb_rows + 1), "superblock_diff");
   ALLOC(a.sb_start, (uint64_t)a.num_sb + 1u, "superblock_starts");
@@ -243,6 +243,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.dsort_hist0, (uint64_t)depth_sort_bins() * a.dsort_tiles_cap, "depth_sort_counts_0");
   ALLOC(a.dsort_hist1, (uint64_t)depth_sort_bins() * a.dsort_tiles_cap, "depth_sort_counts_1");
   ALLOC(a.dsort_total, (uint64_t)depth_sort_bins(), "depth_sort_totals");
+  ALLOC(a.scan_status_n, scan_tiles_n, "scan_status_n");
   ALLOC(a.scan_status_m, scan_tiles_m, "scan_status_m");
   ALLOC(a.ctl, (uint64_t)kCtlWords, "ctl");
   if (h->cfg.flags & HDSR_CFG_BACKWARD) {
@@ -252,11 +253,12 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
 #undef ALLOC
   if (s != HDSR_OK) { free_all(h); delete h; return s; }
   a.U = U;
-  a.sbk_sorted = a.sbk_b;
+  a.sbk_sorted = a.sb_bits > kRadixBits ? a.sbk_a : a.sbk_b;  // where the last superblock pass writes
   // status words start at epoch 0, which no frame uses. The clears run on the
   // legacy stream and are complete when create returns: the caller's stream
   // may be a non-blocking one, which does not wait for the legacy stream.
-  e = cudaMemsetAsync(a.scan_status_m, 0, scan_tiles_m * 8, cudaStreamLegacy);
+  e = cudaMemsetAsync(a.scan_status_n, 0, scan_tiles_n * 8, cudaStreamLegacy);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.scan_status_m, 0, scan_tiles_m * 8, cudaStreamLegacy);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.ctl, 0, kCtlWords * 4, cudaStreamLegacy);
   if (e == cudaSuccess) e = cudaMemsetAsync(U, 0, 256, cudaStreamLegacy);
   if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
@@ -460,12 +462,29 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   // (sortRanks by depth)
   if ((e = launch_depth_sort(a, s)) != cudaSuccess) return cuda_fail(h, e, "depth_sort");
   mark(h, s, 6);
-  // the superblock lists need the tile scan's totals, its overflow flag and
-  // the list starts of the tile-count pass
+  RadixJob dj{};
+  dj.flags = a.ctl + kCtlFlags;
+  dj.tile_digits = a.tile_digits;
+  dj.bin_base = a.bin_base;
+  dj.tiles_cap = a.radix_tiles_cap;
+  dj.low_mask = 0xFFFFFFFFull;
+  // the superblock lists need the tile scan's totals and overflow flag
   if (fork && (e = cudaStreamWaitEvent(s, h->join_ev, 0)) != cudaSuccess) return cuda_fail(h, e, "join");
-  // every list entry written once, at its final position (stable: each list
-  // in depth order)
-  if ((e = launch_superblock_lists(a, s)) != cudaSuccess) return cuda_fail(h, e, "superblock_lists");
+  // superblock lists in depth order, sorted by superblock (stable)
+  if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
+  RadixJob sj = dj;
+  sj.count = a.ctl + kCtlSbPairs;
+  sj.out_low = nullptr;
+  const uint32_t sb_passes = a.sb_bits > kRadixBits ? 2u : 1u;
+  for (uint32_t p = 0; p < sb_passes; ++p) {
+    sj.in = (p & 1u) ? a.sbk_b : a.sbk_a;
+    sj.out = (p & 1u) ? nullptr : a.sbk_b;
+    sj.out_keys = (p & 1u) ? a.sbk_a : a.sbk_b;
+    sj.shift = kSbKeyShift + kRadixBits * p;
+    sj.bits = p == 0 ? (a.sb_bits < kRadixBits ? a.sb_bits : kRadixBits) : a.sb_bits - kRadixBits;
+    if ((e = launch_radix_pass(sj, p + 1 == sb_passes, a.num_sms, s)) != cudaSuccess)
+      return cuda_fail(h, e, "superblock_sort");
+  }
   mark(h, s, 7);
   if ((e = launch_chunk_masks(a, s)) != cudaSuccess) return cuda_fail(h, e, "chunk_masks");
   mark(h, s, 9);
@@ -478,8 +497,8 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
     if ((e = launch_log_depth_keys(a, s)) != cudaSuccess) return cuda_fail(h, e, "log_depth_keys");
     h->launches += 2;
   }
-  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 9 * n_splat_launch + 3 * n_splat_launch +
-                 (a.tile_count ? 1 : 0);
+  h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 9 * n_splat_launch + 1 +
+                 3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 1 : 0);
   return HDSR_OK;
 }
 

@@ -98,6 +98,23 @@ __device__ __forceinline__ uint32_t warp_sum9(const float (&g)[9], uint32_t lane
   return ((lane >> 1) & 1u) | (((lane >> 2) & 1u) << 1) | (((lane >> 3) & 1u) << 2) | (((lane >> 4) & 1u) << 3);
 }
 
+// Colour sums of the adjoint raster as two floats (1) or one (0); see pass A.
+#ifndef HDSR_BWD_COMPENSATED
+#define HDSR_BWD_COMPENSATED 1
+#endif
+
+// c + v, its rounding error added to e (kept only with HDSR_BWD_COMPENSATED)
+__device__ __forceinline__ float comp_add(float c, float v, float& e) {
+#if HDSR_BWD_COMPENSATED
+  float r;
+  const float s = two_sum(c, v, r);
+  e += r;
+  return s;
+#else
+  return c + v;
+#endif
+}
+
 __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
   __shared__ float4 s_pay[kBwdWarps][32][kBRows];
   __shared__ uint32_t s_queue[kBwdWarps][kWalkQueue];
@@ -163,11 +180,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
             const float w = al * T[k];
             const float cw[3] = {r1.z * w, r1.w * w, s[i][2].x * w};
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              float e;
-              C[k][c] = two_sum(C[k][c], cw[c], e);
-              Ce[k][c] += e;
-            }
+            for (int c = 0; c < 3; ++c) C[k][c] = comp_add(C[k][c], cw[c], Ce[k][c]);
             T[k] = T[k] * (1.0f - al);
           }
         }
@@ -188,9 +201,8 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       const float bgc[3] = {kBgR, kBgG, kBgB};
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float e;
-        R[k][c] = two_sum(C[k][c], T[k] * bgc[c], e);
-        Re[k][c] = Ce[k][c] + e;
+        Re[k][c] = Ce[k][c];
+        R[k][c] = comp_add(C[k][c], T[k] * bgc[c], Re[k][c]);
       }
       const uint32_t px = bx + (uint32_t)(k & 1), py = by + (uint32_t)(k >> 1);
       float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -233,9 +245,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
           float behind[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            float e;
-            R[k][c] = two_sum(R[k][c], -cw[c], e);
-            Re[k][c] += e;
+            R[k][c] = comp_add(R[k][c], -cw[c], Re[k][c]);
             behind[c] = R[k][c] + Re[k][c];
           }
           const float inv1m = 1.0f / (1.0f - al);

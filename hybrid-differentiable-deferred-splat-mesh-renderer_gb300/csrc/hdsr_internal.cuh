@@ -24,7 +24,8 @@ enum Ctl : int {
   kCtlHotTiles = 5,
   kCtlChunks = 6,
   kCtlVisible = 7,
-  kCtlScanMTile = 9,   // dynamic tile counter of the tile scan
+  kCtlScanNTile = 8,   // dynamic tile counters of the scans
+  kCtlScanMTile = 9,
   kCtlRasterTile = 19, // dynamic tile counter of the rasteriser
   kCtlBwdTile = 20,    // dynamic tile counter of the adjoint rasteriser
   kCtlSortCount = 21,  // key count of the back-to-front sort (hdsr_sort_back_to_front)
@@ -116,8 +117,9 @@ struct FrameArgs {
   uint32_t* order;                // sortRanks in ascending (depth, sortRank)
   uint32_t* nsb;                  // superblocks touched per sortRank
   uint32_t* sb_off;               // exclusive prefix of nsb in depth order
-  unsigned long long* sbk_b;      // superblock list entries (see kSbKeyShift), list after list
-  const unsigned long long* sbk_sorted;  // = sbk_b: read-only view of the lists
+  unsigned long long* sbk_a;      // superblock list entries in depth order (see kSbKeyShift)
+  unsigned long long* sbk_b;
+  const unsigned long long* sbk_sorted;  // sbk_a or sbk_b: the entries stably sorted by superblock
   int* tile_diff;                 // (cols+1) x (rows+1) 2D difference grid of tile counts
   int* sb_diff;                   // (sb_cols+1) x (sb_rows+1) grid of superblock list lengths
   uint32_t* sb_start;             // num_sb + 1: first entry of each superblock's list
@@ -142,14 +144,11 @@ struct FrameArgs {
   uint32_t* dsort_hist1;          // (odd passes)
   uint32_t* dsort_total;          // per digit: the pass's total
   uint32_t dsort_tiles_cap;       // blocks of kRadixTile keys (+1)
-  uint32_t* sb_tab;               // (num_sb + 1) x sb_tiles_cap: per 2,048-position tile of the depth
-                                  // order, entries per superblock -> their first positions (last row:
-                                  // entries per tile -> the tile's first entry)
-  uint32_t sb_tiles_cap;
+  unsigned long long* scan_status_n; // per kScanTile-element tile of the N scan
   unsigned long long* scan_status_m;
   uint32_t* ctl;
   uint32_t spin_limit;            // bound of each decoupled-lookback wait (spins of ~100 ns)
-  uint32_t withheld_scan_tile;    // test hook: this tile of the tile scan never posts its status (~0u: none)
+  uint32_t withheld_scan_tile;    // test hook: this tile of each scan never posts its status (~0u: none)
   // outputs (borrowed)
   void* out_color;
   uint64_t color_pitch;
@@ -335,9 +334,7 @@ cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_project(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_counts(const FrameArgs& a, cudaStream_t s);   // 2 launches
 cudaError_t launch_depth_range(const FrameArgs& a, cudaStream_t s);
-// the superblock lists (hdsr_sblists.cu): a.order -> a.sbk_b, 3 launches
-cudaError_t launch_superblock_lists(const FrameArgs& a, cudaStream_t s);
-uint32_t superblock_list_tiles(uint32_t N);  // tiles of its table (sb_tiles_cap)
+cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
 cudaError_t launch_chunk_masks(const FrameArgs& a, cudaStream_t s);   // 1 launch

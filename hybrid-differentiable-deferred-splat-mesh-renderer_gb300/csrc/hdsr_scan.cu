@@ -2,7 +2,10 @@
 //
 // Replaces the reference's three-pass Hillis-Steele scan (scan,
 // scan_block_sums, add_block_sums in gpu_prefix_sum.wgsl:14-85, driven by
-// gpuTileSplatCompositor.ts:1063-1088) with one launch:
+// gpuTileSplatCompositor.ts:1063-1088) with one launch per array:
+//   - per-splat superblock counts, taken in ascending (depth, sortRank)
+//     order from bits 24-31 of the depth-order words (N) -> each splat's
+//     superblock list entries written at its offset, and Q, their total;
 //   - per-tile counts (M) -> tile offsets (bit-identical to the reference's
 //     tileOffsets), the hot-tile statistics of classify_tiles
 //     (gpu_tile_classify.wgsl:44-86) and, when requested, the per-tile
@@ -57,6 +60,50 @@ __device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t
   }
   return prefix;
 }
+
+// Superblock lists: splat i of the depth order writes one entry per
+// superblock its tile box touches, superblock << 36 | local rect << 24 |
+// sortRank, starting at its exclusive prefix o of the counts in depth order.
+__device__ __forceinline__ void emit_superblock_entries(const FrameArgs& a, uint32_t r, uint32_t box, uint32_t o) {
+  if (box == kSentinel) return;
+  const uint32_t x0 = box & 0xFFu, y0 = (box >> 8) & 0xFFu, x1 = (box >> 16) & 0xFFu, y1 = box >> 24;
+  for (uint32_t sy = y0 >> kSbShift; sy <= y1 >> kSbShift; ++sy) {
+    const uint32_t by = sy << kSbShift;
+    const uint32_t ly0 = y0 > by ? y0 - by : 0u, ly1 = y1 - by < 7u ? y1 - by : 7u;
+    for (uint32_t sx = x0 >> kSbShift; sx <= x1 >> kSbShift; ++sx) {
+      const uint32_t bx = sx << kSbShift;
+      const uint32_t lx0 = x0 > bx ? x0 - bx : 0u, lx1 = x1 - bx < 7u ? x1 - bx : 7u;
+      const uint32_t rect = lx0 | (lx1 << 3) | (ly0 << 6) | (ly1 << 9);
+      if (o < a.sb_cap)
+        a.sbk_a[o] = ((unsigned long long)(sy * a.sb_cols + sx) << kSbKeyShift) | ((unsigned long long)rect << 24) | r;
+      ++o;
+    }
+  }
+}
+
+// Scan of the superblock counts in depth order (read from bits 24-31 of the
+// depth-order words), emitting every splat's list entries at its offset.
+struct SbScan {
+  // an overflowed frame skipped the depth sort: order holds no permutation
+  static __device__ bool skip(const FrameArgs& a) { return (a.ctl[kCtlFlags] & kSkipFlags) != 0u; }
+  static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
+  static __device__ uint32_t counter() { return kCtlScanNTile; }
+  static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
+  static __device__ uint32_t load(const FrameArgs& a, uint32_t i) { return a.order[i] >> 24; }
+  // what store needs, loaded for all of a thread's items before any store
+  struct Pre {
+    uint32_t r, box;
+  };
+  static __device__ Pre pre(const FrameArgs& a, uint32_t i) {
+    const uint32_t r = checked_rank(a.order[i] & 0xFFFFFFu, a.N, a.ctl);
+    return Pre{r, a.aux[r].x};
+  }
+  static __device__ void store(const FrameArgs& a, uint32_t i, uint32_t excl, const Pre& p) {
+    a.sb_off[i] = excl;
+    emit_superblock_entries(a, p.r, p.box, excl);
+  }
+  static __device__ void finish(const FrameArgs& a, uint32_t total) { a.ctl[kCtlSbPairs] = total; }
+};
 
 struct TileScan {
   static __device__ bool skip(const FrameArgs&) { return false; }  // it decides the overflow
@@ -204,6 +251,11 @@ int scan_grid(const FrameArgs& a, uint32_t n) {
 }
 
 }  // namespace
+
+cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s) {
+  k_scan<SbScan><<<scan_grid(a, a.N), kScanThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s) {
   k_scan<TileScan><<<scan_grid(a, a.M), kScanThreads, 0, s>>>(a);

@@ -232,9 +232,8 @@ uint64_t hdsr_launch_count(const hdsr_compositor* h);
  * every later kernel of the frame returns without writing (the output images
  * keep their previous contents), and hdsr_query_status returns
  * HDSR_ERR_TIMEOUT. `withheld_tile` (test hook; 0xFFFFFFFF = none) makes that
- * tile of the tile-offset scan (2,048 Morton tiles per scan tile) compute its
- * prefix but post nothing, so that its successors' waits run out. Drops the
- * handle's frame graph. */
+ * tile of each scan compute its prefix but post nothing, so that its
+ * successors' waits run out. Drops the handle's frame graph. */
 hdsr_status hdsr_set_scan_wait(hdsr_compositor* h, uint32_t spin_limit, uint32_t withheld_tile);
 
 /* Gradients of one frame (no reference counterpart: the reference renders

@@ -286,14 +286,26 @@ def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray, with_abs:
     return (g2d, gabs) if with_abs else g2d
 
 
-def reference_gradient(U, packed, order, frame: dict, d_out: np.ndarray, with_scale: bool = False):
+def reference_gradient(U, packed, order, frame: dict, d_out: np.ndarray, with_scale: bool = False,
+                       screen_f32: bool = False):
     """dL/d(parameters) per splat id in the layouts of hdsr_scene_views, for
     dL/d(output rgba) = d_out, in FP64. With `with_scale`, also (second
     value) per parameter the sum over pixels of the absolute value of each
     pixel's contribution (through the same chain rule, term by term): the
     magnitude against which an fp32 evaluation of the gradient's sums is
-    rounded, used to bound the error such an evaluation may carry."""
+    rounded, used to bound the error such an evaluation may carry.
+
+    With `screen_f32`, the composite reads the screen-space parameters
+    (centre, conic, opacity, colour) rounded to f32, as the projection cache
+    holds them (its centre and conic words are f32), the derivatives of the
+    projection staying FP64: the FP64 gradient of the frame as the fp32
+    cache defines it. Splat centres lie hundreds to thousands of pixels from
+    the origin, where an f32 centre is good to ~1e-4 px, which alone moves
+    some gradients by up to ~1e-2 relative (where a gradient sums many
+    opposing pixel terms)."""
     screen, visible, lay = project_dual(U, packed, order)
+    if screen_f32:
+        screen = {k: Dual(v.v.astype(np.float32).astype(np.float64), v.d) for k, v in screen.items()}
     res = composite_adjoint(U, screen, frame, np.asarray(d_out, np.float64), with_abs=with_scale)
     g2d, gabs = res if with_scale else (res, None)
     keys = ("cx", "cy", "ia", "ib", "ic", "op", "r", "g", "b")

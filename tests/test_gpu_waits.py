@@ -1,9 +1,9 @@
 """Bounded device waits of the decoupled-lookback scans.
 
 A scan tile waits for its predecessors' status words; every such wait is
-bounded. The test hook of hdsr_set_scan_wait keeps one tile of the tile scan
-from posting its status, with a short spin limit, so the next tile's wait
-runs out: the frame must end (no hang), report HDSR_ERR_TIMEOUT with the timeout
+bounded. The test hook of hdsr_set_scan_wait keeps one tile of each scan from
+posting its status, with a short spin limit, so the next tile's wait runs
+out: the frame must end (no hang), report HDSR_ERR_TIMEOUT with the timeout
 device flag, leave the outputs untouched (the kernels after the scan return
 at once), and the same handle must render the exact frame again once the hook
 is cleared.
@@ -22,7 +22,7 @@ def test_withheld_scan_tile_times_out_and_the_handle_recovers(cuda, pkg, orc):
     import torch
 
     # 800x600: 3,364 Morton tiles, so the tile scan has 2 scan tiles of 2,048;
-    # tile 1 waits on tile 0
+    # 20,000 splats: the per-splat scan has 10. Tile 1 of each waits on tile 0.
     scene = pkg.workloads.plain_scene(20_000, seed=5)
     g = render_gpu(pkg, scene, pkg.camera.look_from((0.1, 0.2, 4.0)), 800, 600)
     res = g["res"]
@@ -54,8 +54,9 @@ def test_withheld_scan_tile_times_out_and_the_handle_recovers(cuda, pkg, orc):
 
 def test_withheld_last_tile_needs_no_wait(cuda, pkg, orc):
     # nobody waits on the last tile of a scan: withholding it changes nothing
-    scene = pkg.workloads.plain_scene(5_000, seed=6)
-    g = render_gpu(pkg, scene, pkg.camera.look_from((0.0, 0.1, 4.0)), 800, 600)  # 2 scan tiles
+    # (800x600 and 3,000 splats: both scans have 2 scan tiles)
+    scene = pkg.workloads.plain_scene(3_000, seed=6)
+    g = render_gpu(pkg, scene, pkg.camera.look_from((0.0, 0.1, 4.0)), 800, 600)
     res = g["res"]
     res.set_scan_wait(spin_limit=1000, withheld_tile=1)
     pkg.encode_full_compute_compositor_pipeline(None, res)
