@@ -510,14 +510,15 @@ def run_serve(pkg, args, dev) -> dict:
     # requests' keys
     key_served = {}
     for key, (t_plain, cams) in key_plain.items():
-        tickets = []
-        t1 = time.perf_counter()
-        for j, u in enumerate(cams):
-            color, gb = outs[(key[1], key[2])][j]
-            tickets.append(server.submit(key[0], u, color, gb))
-        for t in tickets:
-            server.wait(t)
-        key_served[key] = (time.perf_counter() - t1) / len(cams)
+        for rep in range(2):  # the first round sizes the key's extra slots; the second is timed
+            tickets = []
+            t1 = time.perf_counter()
+            for j, u in enumerate(cams):
+                color, gb = outs[(key[1], key[2])][j]
+                tickets.append(server.submit(key[0], u, color, gb))
+            for t in tickets:
+                server.wait(t)
+            key_served[key] = (time.perf_counter() - t1) / len(cams)
     ceil_plain = sum(key_plain[q[:3]][0] for q in reqs)
     ceil_served = sum(key_served[q[:3]] for q in reqs)
     log("serving: saturated run")
@@ -651,6 +652,11 @@ def run_ours(args, rank, world, local):
                     "frac": round(ach / peak, 4), "traffic": traffic,
                     "algorithmic_bytes": int(b), "launch_ms": round(mean_pass[dom], 4),
                     "peak_source": "measured" if peaks else "fallback"}
+    clock_summary = clocks.summary(t_begin, t_end)
+    roofline_raster = None
+    if args.workload == "hot760k":  # the committed instruction count is of that workload
+        roofline_raster = raster_issue_roofline(mean_pass.get("raster"), clock_summary.get("sm_mhz"),
+                                                torch.cuda.get_device_properties(dev).multi_processor_count)
     out = {
         "metric": metric_name(wl), "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -661,7 +667,7 @@ def run_ours(args, rank, world, local):
         "e2e": e2e, "gpu_launches": int(launches),
         "passes_ms": {k: round(v, 4) for k, v in mean_pass.items()},
         "pass_share": {k: round(v / frame_ms, 4) for k, v in mean_pass.items()},
-        "roofline": roofline, "clocks": clocks.summary(t_begin, t_end),
+        "roofline": roofline, "roofline_raster": roofline_raster, "clocks": clock_summary,
         "gpu_back_to_front_sort_ms": round(sort_ms, 4),
         "composite_only_ms": round(composite_only_ms, 4),
     }
@@ -754,6 +760,26 @@ def run_deferred(pkg, F, wl, args, dev, cpu: bool) -> dict:
         out["matches_oracle"] = bool(np.array_equal(ref, lit.cpu().numpy().view(np.uint16)))
     post.destroy()
     return out
+
+
+def raster_issue_roofline(raster_ms: float, sm_mhz, sms: int):
+    """Issue roofline of the rasteriser: its warp instructions per launch
+    (ncu smsp__inst_executed.sum of one warm launch on the same workload,
+    committed in profiles/raster_issue.json) over the live CUDA-event time,
+    against every SM scheduler issuing one warp instruction per cycle (4 per
+    SM) at the SM clock sampled during the timed frames."""
+    f = ROOT / "profiles" / "raster_issue.json"
+    if not f.exists() or not raster_ms:
+        return None
+    d = json.loads(f.read_text())
+    inst = float(d["inst_executed_per_launch"])
+    mhz = float(sm_mhz or 2070.0)
+    achieved = inst / (raster_ms / 1000.0) / 1e9  # warp instructions per ns = G/s
+    peak = sms * 4 * mhz * 1e6 / 1e9
+    return {"bound": "issue", "kernel": "raster", "achieved": round(achieved, 1), "peak": round(peak, 1),
+            "unit": "G warp-instructions/s", "frac": round(achieved / peak, 4),
+            "inst_per_launch": int(inst), "launch_ms": round(raster_ms, 4), "sm_mhz": mhz,
+            "inst_source": f"profiles/raster_issue.json ({d.get('workload')}, {d.get('build', '')})".strip()}
 
 
 def load_traffic(kernel: str):

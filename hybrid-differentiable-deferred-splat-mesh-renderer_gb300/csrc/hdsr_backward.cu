@@ -98,23 +98,6 @@ __device__ __forceinline__ uint32_t warp_sum9(const float (&g)[9], uint32_t lane
   return ((lane >> 1) & 1u) | (((lane >> 2) & 1u) << 1) | (((lane >> 3) & 1u) << 2) | (((lane >> 4) & 1u) << 3);
 }
 
-// Colour sums of the adjoint raster as two floats (1) or one (0); see pass A.
-#ifndef HDSR_BWD_COMPENSATED
-#define HDSR_BWD_COMPENSATED 1
-#endif
-
-// c + v, its rounding error added to e (kept only with HDSR_BWD_COMPENSATED)
-__device__ __forceinline__ float comp_add(float c, float v, float& e) {
-#if HDSR_BWD_COMPENSATED
-  float r;
-  const float s = two_sum(c, v, r);
-  e += r;
-  return s;
-#else
-  return c + v;
-#endif
-}
-
 __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
   __shared__ float4 s_pay[kBwdWarps][32][kBRows];
   __shared__ uint32_t s_queue[kBwdWarps][kWalkQueue];
@@ -139,18 +122,10 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       dxv[k] = p00x + (float)(k & 1);
       dyv[k] = p00y + (float)(k >> 1);
     }
-    // pass A: forward recompute. The colour sums are kept as two floats (a
-    // sum and its rounding errors, Knuth's TwoSum): pass B needs the light
-    // behind each entry, the output minus the sum so far, and in one float
-    // that difference loses its digits to the ulp of the output once the
-    // light behind is small (deep entries of dense pixels)
-    float T[4], C[4][3], Ce[4][3];
+    // pass A: forward recompute
+    float T[4], C[4][3];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      T[k] = 1.0f;
-      C[k][0] = C[k][1] = C[k][2] = 0.0f;
-      Ce[k][0] = Ce[k][1] = Ce[k][2] = 0.0f;
-    }
+    for (int k = 0; k < 4; ++k) { T[k] = 1.0f; C[k][0] = C[k][1] = C[k][2] = 0.0f; }
     bool done = false;
     uint32_t n_end = 0;
     const float rx0 = (float)(tx * 16u) + 0.5f, ry0 = (float)(ty * 16u + 8u * half) + 0.5f;
@@ -178,9 +153,9 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
           const bool valid = (pw > -4.0f) && (al > (1.0f / 255.0f)) && (T[k] >= 0.001f);
           if (valid) {
             const float w = al * T[k];
-            const float cw[3] = {r1.z * w, r1.w * w, s[i][2].x * w};
-#pragma unroll
-            for (int c = 0; c < 3; ++c) C[k][c] = comp_add(C[k][c], cw[c], Ce[k][c]);
+            C[k][0] = fmaf(r1.z, w, C[k][0]);
+            C[k][1] = fmaf(r1.w, w, C[k][1]);
+            C[k][2] = fmaf(s[i][2].x, w, C[k][2]);
             T[k] = T[k] * (1.0f - al);
           }
         }
@@ -191,25 +166,21 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
       if (__all_sync(0xFFFFFFFFu, done)) break;
       nb = nb2;
     }
-    // outputs and their incoming gradients (pixels outside the image: none);
-    // R = the light still to come, output minus the colour taken so far, as
-    // two floats, starting at the whole output
-    float R[4][3], Re[4][3], Tf[4], gO[4][3], gA[4];
+    // outputs and their incoming gradients (pixels outside the image: none)
+    float O[4][3], Tf[4], gO[4][3], gA[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       Tf[k] = T[k];
-      const float bgc[3] = {kBgR, kBgG, kBgB};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Re[k][c] = Ce[k][c];
-        R[k][c] = comp_add(C[k][c], T[k] * bgc[c], Re[k][c]);
-      }
+      O[k][0] = fmaf(T[k], kBgR, C[k][0]);
+      O[k][1] = fmaf(T[k], kBgG, C[k][1]);
+      O[k][2] = fmaf(T[k], kBgB, C[k][2]);
       const uint32_t px = bx + (uint32_t)(k & 1), py = by + (uint32_t)(k >> 1);
       float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (px < a.W && py < a.H)
         g = reinterpret_cast<const float4*>(reinterpret_cast<const char*>(b.d_color) + (size_t)py * b.d_color_pitch)[px];
       gO[k][0] = g.x; gO[k][1] = g.y; gO[k][2] = g.z; gA[k] = g.w;
       T[k] = 1.0f;
+      C[k][0] = C[k][1] = C[k][2] = 0.0f;
     }
     // pass B: gradients, the same n_end entries in the same order
     walk.start(a, tx, ty, s_queue[warp]);
@@ -240,17 +211,13 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
           if (!valid) continue;
           any = true;
           const float w = al * T[k];
-          // the light behind this entry: R minus this entry's colour, in two floats
-          const float cw[3] = {cr * w, cg * w, cb * w};
-          float behind[3];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            R[k][c] = comp_add(R[k][c], -cw[c], Re[k][c]);
-            behind[c] = R[k][c] + Re[k][c];
-          }
+          C[k][0] = fmaf(cr, w, C[k][0]);
+          C[k][1] = fmaf(cg, w, C[k][1]);
+          C[k][2] = fmaf(cb, w, C[k][2]);
           const float inv1m = 1.0f / (1.0f - al);
-          float dal = gO[k][0] * (cr * T[k] - behind[0] * inv1m) + gO[k][1] * (cg * T[k] - behind[1] * inv1m) +
-                      gO[k][2] * (cb * T[k] - behind[2] * inv1m) + gA[k] * Tf[k] * inv1m;
+          float dal = gO[k][0] * (cr * T[k] - (O[k][0] - C[k][0]) * inv1m) +
+                      gO[k][1] * (cg * T[k] - (O[k][1] - C[k][1]) * inv1m) +
+                      gO[k][2] * (cb * T[k] - (O[k][2] - C[k][2]) * inv1m) + gA[k] * Tf[k] * inv1m;
           g[6] += gO[k][0] * w;
           g[7] += gO[k][1] * w;
           g[8] += gO[k][2] * w;
