@@ -173,10 +173,11 @@ def setup_frame(pkg, wl, device_index=0):
     return dict(packed=packed, plan=plan, u=u, order=order, bufs=bufs, color=color, gb=gb, res=res, stats=st)
 
 
-def pass_bytes(name: str, N: int, P: int, Q: int, S: int, sh_floats: int) -> float | None:
+def pass_bytes(name: str, N: int, P: int, Q: int, S: int, sh_floats: int, depth_passes: int = 4) -> float | None:
     """Algorithmic HBM bytes of one pass of the frame (None: not HBM-bound).
 
-    N splats, P (tile, splat) pairs, Q superblock list entries, S segments."""
+    N splats, P (tile, splat) pairs, Q superblock list entries, S segments,
+    depth_passes the 9-bit passes the depth sort ran this frame."""
     if name == "project":
         # indices, position, scale, rotation, opacity, material, SH in; geo,
         # app, gb, aux, depth, ntiles, nsb, depth key out
@@ -184,7 +185,9 @@ def pass_bytes(name: str, N: int, P: int, Q: int, S: int, sh_floats: int) -> flo
     if name == "tile_counts":
         return N * 8  # tile boxes
     if name == "depth_sort":
-        return 4 * (N * 8 + N * 16)  # 4 passes: upsweep read + downsweep read/write
+        # the first histogram reads the keys; every pass reads them, the last
+        # writes the 4-byte order words, the others the 8-byte keys
+        return N * 8 + depth_passes * N * 8 + (depth_passes - 1) * N * 8 + N * 4
     if name == "superblock_lists":
         # scan: depth-order words (counts ride in them) and gathered tile boxes
         # in, offsets and Q keys out; one radix pass: Q keys read twice, written once
@@ -637,14 +640,14 @@ def run_ours(args, rank, world, local):
     sh_floats = 6 + 3 * ((wl.scene.sh_degree + 1) ** 2 - 1)
     mean_pass = {k: statistics.mean(v) for k, v in passes.items()}
     frame_ms = statistics.mean(times)
-    Q, S = int(st["superblock_entries"]), int(st["segments"])
-    hbm_passes = {k: v for k, v in mean_pass.items() if pass_bytes(k, N, P, Q, S, sh_floats)}
+    Q, S, DP = int(st["superblock_entries"]), int(st["segments"]), int(st["depth_sort_passes"])
+    hbm_passes = {k: v for k, v in mean_pass.items() if pass_bytes(k, N, P, Q, S, sh_floats, DP)}
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     dom = max(hbm_passes, key=hbm_passes.get) if hbm_passes else None
     roofline = None
     if dom:
-        b = pass_bytes(dom, N, P, Q, S, sh_floats)
+        b = pass_bytes(dom, N, P, Q, S, sh_floats, DP)
         ach = b / (mean_pass[dom] / 1000.0) / 1e9
         # the committed ncu table is of the default workload only
         traffic = load_traffic(dom) if args.workload == "hot760k" else None
@@ -662,6 +665,7 @@ def run_ours(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {**wl.describe(), "pairs": P, "hot_tiles": int(st["hot_tiles"]), "chunks": int(st["chunks"]),
+                   "depth_sort_passes": DP,
                    "l2": "256 MiB flush between timed steps",
                    "parallelism": f"replicas{world}"},
         "e2e": e2e, "gpu_launches": int(launches),

@@ -147,7 +147,8 @@ POST_PASSES = ("ss_normals", "bilateral", "gtao_prefilter", "gtao_main", "gtao_d
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_pairs", c_uint64), ("pair_capacity", c_uint64), ("visible_splats", c_uint32),
                 ("superblock_entries", c_uint32), ("hot_tiles", c_uint32), ("chunks", c_uint32),
-                ("device_flags", c_uint32), ("segments", c_uint32)]
+                ("device_flags", c_uint32), ("segments", c_uint32), ("depth_sort_passes", c_uint32),
+                ("reserved", c_uint32)]
 
 
 class HdsrError(RuntimeError):

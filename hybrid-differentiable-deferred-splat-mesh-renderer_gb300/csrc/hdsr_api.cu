@@ -685,6 +685,8 @@ hdsr_status hdsr_query_status(hdsr_compositor* h, hdsr_frame_stats* st) {
     st->device_flags = ctl[kCtlFlags];
     st->superblock_entries = ctl[kCtlSbPairs];
     st->segments = ctl[kCtlSegments];
+    st->depth_sort_passes = ctl[kCtlDepthPasses];
+    st->reserved = 0u;
   }
   if (ctl[kCtlFlags] & HDSR_DEV_OVERFLOW) {
     h->sorted_valid = false;

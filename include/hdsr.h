@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define HDSR_ABI_VERSION 1
+#define HDSR_ABI_VERSION 2
 
 typedef enum hdsr_status {
   HDSR_OK = 0,
@@ -125,6 +125,8 @@ typedef struct hdsr_frame_stats {
   uint32_t chunks;                /* 4096-entry chunks of hot tiles */
   uint32_t device_flags;          /* HDSR_DEV_* */
   uint32_t segments;              /* 256-entry segments of the superblock lists */
+  uint32_t depth_sort_passes;     /* 9-bit passes the depth sort ran (1-4: the frame's depth range) */
+  uint32_t reserved;
 } hdsr_frame_stats;
 
 typedef struct hdsr_compositor hdsr_compositor;

@@ -338,11 +338,15 @@ def _morton(x: int, y: int) -> int:
 
 
 def threshold_adjacent_ranks(U, par, frame, rel=1e-4) -> set:
-    """sortRanks with a (pixel, entry) within `rel` of a composite threshold
-    (power -4, alpha 1/255, the 0.99 cap, T 0.001) or whose opacity or
-    colour sits at a clamp, traced in FP64 over the frame's entry lists; par
-    is orc_project_f64's (N, 10) array. There fp32 and FP64 may decide a
-    comparison differently, so those splats are left out of exact checks."""
+    """sortRanks left out of exact gradient checks, traced in FP64 over the
+    frame's entry lists (par: orc_project_f64's (N, 10) array): those whose
+    opacity or colour sits at a clamp, and, for every pixel where some entry
+    lies within `rel` of a composite threshold (power -4, alpha 1/255, the
+    0.99 cap, T 0.001), every entry taken in that pixel. There fp32 and FP64
+    may decide the comparison differently, and a decision that differs
+    changes the transmittance of every entry behind it and the light behind
+    every entry in front of it, i.e. the gradients of all of the pixel's
+    entries, not only its own."""
     U = np.asarray(U, np.float32)
     Uu = U.view(np.uint32)
     cols, rows = int(Uu[20]), int(Uu[21])
@@ -378,6 +382,9 @@ def threshold_adjacent_ranks(U, par, frame, rel=1e-4) -> set:
             # an entry after the saturation point changes nothing; a T near
             # the cutoff still matters at the entry that meets it
             sat = np.maximum.accumulate(G < 0.001 * (1 - rel), axis=0)
-            hit = (near & ~np.vstack([np.zeros((1, sat.shape[1]), bool), sat[:-1]])).any(1)
+            near = near & ~np.vstack([np.zeros((1, sat.shape[1]), bool), sat[:-1]])
+            valid = cond & (G >= 0.001)
+            pix = near.any(0)
+            hit = near.any(1) | (valid[:, pix].any(1) if pix.any() else np.zeros(K, bool))
             flagged.update(int(x) for x in e[hit])
     return flagged
