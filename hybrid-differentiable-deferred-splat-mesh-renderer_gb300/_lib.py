@@ -54,6 +54,7 @@ BUFFER_IDS = {
     "sorted_keys": 8,
     "pair_offsets": 9,
     "depth_order": 10,
+    "backward_params": 11,
 }
 
 

@@ -727,6 +727,9 @@ hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, u
       *ptr = a.sorted_keys; *bytes = cap * 8; break;
     case HDSR_BUF_PAIR_OFFSETS: *ptr = a.sb_off; *bytes = N * 4; break;
     case HDSR_BUF_DEPTH_ORDER: *ptr = a.order; *bytes = N * 4; break;
+    case HDSR_BUF_BACKWARD_PARAMS:
+      if (!h->bwd_par) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_BACKWARD");
+      *ptr = h->bwd_par; *bytes = N * 48; break;
     default: return fail(h, HDSR_ERR_INVALID_ARG, "unknown buffer id");
   }
   return HDSR_OK;

@@ -199,8 +199,11 @@ typedef enum hdsr_buffer_id {
                                  handle's last stream and synchronizes that stream. */
   HDSR_BUF_SORTED_KEYS = 8,   /* u64[P] per final entry: tile<<(20+R) | k20<<R | sortRank */
   HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat superblock counts, depth order */
-  HDSR_BUF_DEPTH_ORDER = 10   /* u32[N] ascending (depth bits, sortRank): sortRank in bits 0-23,
+  HDSR_BUF_DEPTH_ORDER = 10,  /* u32[N] ascending (depth bits, sortRank): sortRank in bits 0-23,
                                  the splat's superblock count in bits 24-31 */
+  HDSR_BUF_BACKWARD_PARAMS = 11 /* float4[N][3] per sortRank, written by hdsr_encode_backward: the
+                                 adjoint's screen-space parameters (cx, cy, ia, ib | ic, opacity,
+                                 r, g | b, 0, 0, 0); HDSR_CFG_BACKWARD handles only */
 } hdsr_buffer_id;
 
 /* Device address and byte size of an internal buffer (valid until destroy).
