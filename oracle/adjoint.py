@@ -214,12 +214,53 @@ def project_dual(U, packed, order):
     return screen, visible, lay
 
 
-def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray, with_abs: bool = False):
+def _f32_trajectory(p, px, py):
+    """The canonical f32 composite of one tile's entries over its pixels (the
+    oracle's composite arithmetic, hdsr_oracle.c: fused power, its own exp,
+    f32 alpha and transmittance products), at the f32 values of the screen
+    parameters p (K, 9): per entry and pixel the alpha, the exp factor, the
+    capped flag, the validity and the transmittance before the entry."""
+    from . import composite_expf  # the oracle's composite exp
+
+    f32 = np.float32
+    fma32 = lambda a, b, c: (np.asarray(a, np.float64) * b + c).astype(f32)  # noqa: E731
+    K, n = p.shape[0], px.size
+    px32, py32 = px.astype(f32), py.astype(f32)
+    al, ex, cap, val, tin = (np.zeros((K, n)), np.zeros((K, n)), np.zeros((K, n), bool), np.zeros((K, n), bool),
+                             np.zeros((K, n)))
+    T = np.ones(n, f32)
+    for k in range(K):
+        cx, cy, ia, ib, ic, op = (f32(v) for v in p[k, :6])
+        ka, kb, kc = f32(ia * f32(-0.5)), f32(-ib), f32(ic * f32(-0.5))
+        dx, dy = (px32 - cx).astype(f32), (py32 - cy).astype(f32)
+        pw = fma32((kc * dy).astype(f32), dy, fma32((kb * dx).astype(f32), dy, ((ka * dx).astype(f32) * dx).astype(f32)))
+        g = composite_expf(pw).reshape(n)
+        raw = (op * g).astype(f32)
+        a = np.minimum(f32(0.99), raw)
+        v = (pw > f32(-4.0)) & (a > f32(1.0) / f32(255.0)) & (T >= f32(0.001))
+        # entries a pixel does not take contribute nothing (far entries may
+        # even overflow the power to inf or nan there)
+        al[k], ex[k], cap[k], val[k], tin[k] = np.where(v, a, 0), np.where(v, g, 0), v & (raw > f32(0.99)), v, T
+        T = np.where(v, (T * (f32(1.0) - a).astype(f32)).astype(f32), T)
+    return al, ex, cap, val, tin, T.astype(np.float64)
+
+
+def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray, with_abs: bool = False,
+                      trajectory: str = "f64"):
     """dL/d(cx, cy, ia, ib, ic, op, r, g, b) per sortRank for dL/d(output
     rgba) = d_out (H, W, 4), over the frame's entry lists; FP64 values of
     the screen parameters come from `screen`. With `with_abs`, also the sums
     of the absolute per-pixel terms (the magnitude an fp32 sum of those terms
-    is rounded against)."""
+    is rounded against).
+
+    `trajectory` "f64": the composite's alphas and transmittances are FP64.
+    "f32": they are those of the canonical f32 composite (_f32_trajectory),
+    the reverse sweep staying FP64: the exact gradient of the frame as fp32
+    renders it. An fp32 transmittance drifts from the FP64 one (each
+    1 - alpha carries the rounding of alpha, relatively larger as alpha
+    nears 1: measured up to 7e-4 after ~100 entries of a dense pixel), and a
+    gradient that sums many opposing pixel terms magnifies that drift; this
+    mode takes the drift out of the comparison with an fp32 adjoint."""
     U = np.asarray(U, np.float32)
     Uu = U.view(np.uint32)
     cols, rows = int(Uu[20]), int(Uu[21])
@@ -246,18 +287,21 @@ def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray, with_abs:
             dx = px[None, :] - p[:, 0:1]
             dy = py[None, :] - p[:, 1:2]
             ia, ib, ic, op = p[:, 2:3], p[:, 3:4], p[:, 4:5], p[:, 5:6]
-            pw = -0.5 * ia * dx * dx - 0.5 * ic * dy * dy - ib * dx * dy
-            ex = np.exp(pw)
-            raw = op * ex
-            capped = raw > 0.99
-            a = np.where(capped, 0.99, raw)
-            cond = (pw > -4.0) & (a > 1.0 / 255.0)
-            fac = np.where(cond, 1.0 - a, 1.0)
-            G = np.vstack([np.ones((1, fac.shape[1])), np.cumprod(fac, axis=0)[:-1]])   # exclusive products
-            valid = cond & (G >= 0.001)
-            fac_v = np.where(valid, 1.0 - a, 1.0)
-            Tin = np.vstack([np.ones((1, fac.shape[1])), np.cumprod(fac_v, axis=0)[:-1]])  # T before entry k
-            Tf = Tin[-1] * fac_v[-1]
+            if trajectory == "f32":
+                a, ex, capped, valid, Tin, Tf = _f32_trajectory(p, px, py)
+            else:
+                pw = -0.5 * ia * dx * dx - 0.5 * ic * dy * dy - ib * dx * dy
+                ex = np.exp(pw)
+                raw = op * ex
+                capped = raw > 0.99
+                a = np.where(capped, 0.99, raw)
+                cond = (pw > -4.0) & (a > 1.0 / 255.0)
+                fac = np.where(cond, 1.0 - a, 1.0)
+                G = np.vstack([np.ones((1, fac.shape[1])), np.cumprod(fac, axis=0)[:-1]])   # exclusive products
+                valid = cond & (G >= 0.001)
+                fac_v = np.where(valid, 1.0 - a, 1.0)
+                Tin = np.vstack([np.ones((1, fac.shape[1])), np.cumprod(fac_v, axis=0)[:-1]])  # T before entry k
+                Tf = Tin[-1] * fac_v[-1]
             wgt = np.where(valid, a * Tin, 0.0)                      # colour weight of entry k
             dC = d_out[Y, X, :3]                                     # (px, 3)
             dA = d_out[Y, X, 3]
@@ -287,7 +331,7 @@ def composite_adjoint(U, screen: dict, frame: dict, d_out: np.ndarray, with_abs:
 
 
 def reference_gradient(U, packed, order, frame: dict, d_out: np.ndarray, with_scale: bool = False,
-                       screen_f32: bool = False):
+                       screen_f32: bool = False, trajectory: str = "f64"):
     """dL/d(parameters) per splat id in the layouts of hdsr_scene_views, for
     dL/d(output rgba) = d_out, in FP64. With `with_scale`, also (second
     value) per parameter the sum over pixels of the absolute value of each
@@ -302,11 +346,12 @@ def reference_gradient(U, packed, order, frame: dict, d_out: np.ndarray, with_sc
     cache defines it. Splat centres lie hundreds to thousands of pixels from
     the origin, where an f32 centre is good to ~1e-4 px, which alone moves
     some gradients by up to ~1e-2 relative (where a gradient sums many
-    opposing pixel terms)."""
+    opposing pixel terms). `trajectory`: see composite_adjoint."""
     screen, visible, lay = project_dual(U, packed, order)
     if screen_f32:
         screen = {k: Dual(v.v.astype(np.float32).astype(np.float64), v.d) for k, v in screen.items()}
-    res = composite_adjoint(U, screen, frame, np.asarray(d_out, np.float64), with_abs=with_scale)
+    res = composite_adjoint(U, screen, frame, np.asarray(d_out, np.float64), with_abs=with_scale,
+                            trajectory=trajectory)
     g2d, gabs = res if with_scale else (res, None)
     keys = ("cx", "cy", "ia", "ib", "ic", "op", "r", "g", "b")
     n = int(packed.count)
