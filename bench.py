@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -635,6 +636,7 @@ def run_ours(args, rank, world, local):
     # end to end through the C ABI with host buffers
     log(f"frames timed: {value:.1f} frames/s")
     e2e = None if args.no_e2e else run_e2e(pkg, F, args, stream, world, dev)
+    moving = run_moving_camera(pkg, F, wl, args, stream)
 
     # roofline of the dominant HBM-bound pass
     sh_floats = 6 + 3 * ((wl.scene.sh_degree + 1) ** 2 - 1)
@@ -683,6 +685,7 @@ def run_ours(args, rank, world, local):
         "clocks": clock_summary,
         "gpu_back_to_front_sort_ms": round(sort_ms, 4),
         "composite_only_ms": round(composite_only_ms, 4),
+        "moving_camera": moving,
     }
     if rank == 0 and not args.no_deferred:
         log("deferred tail leg")
@@ -703,6 +706,71 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         print(json.dumps(out))
     res.destroy()
+
+
+def run_moving_camera(pkg, F, wl, args, stream) -> dict:
+    """The timed workload under a camera that orbits by a fixed azimuth step
+    per frame, as in an interactive viewer: every frame sorts the splats back
+    to front on the device into the bound sortedIndices, uploads its uniform
+    block and renders a full frame (one stream, CUDA events over a run of
+    frames). The raster's work order comes from the previous frame's tile
+    costs, so this measures how well that order carries across camera
+    motion; the static frame (plus its sort) is the reference point. The
+    static camera's state is restored afterwards."""
+    import dataclasses
+
+    import torch
+
+    plan, bufs = F["plan"], F["bufs"]
+    cam0 = wl.cameras[0]
+    frames = max(8, min(args.steps, 60))
+    out = {"frames_per_run": frames}
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    seqs = {}
+    for deg in (0.25, 1.0, 4.0):
+        cams = [dataclasses.replace(cam0, azimuth=cam0.azimuth + math.radians(deg) * i) for i in range(frames)]
+        us = [pkg.frame_uniforms_for(plan, c, sh_degree=wl.scene.sh_degree)[0] for c in cams]
+        views = [np.asarray(c.frame(wl.width, wl.height)["view"], np.float32).reshape(-1) for c in cams]
+        seqs[deg] = (us, views)
+    # a handle of its own, its pair capacity sized on the sequences' frames
+    res = pkg.create_tile_splat_compositor(plan, pair_capacity=F["res"].pair_capacity)
+    pkg.create_tile_splat_bind_groups(res, bufs, F["color"], F["gb"])
+    need = 0
+    for us, views in seqs.values():
+        for u, v in zip(us, views):
+            pkg.sort_back_to_front(stream, res, v, bufs["sorted_indices"])
+            pkg.write_frame_uniform_buffer(res, u)
+            pkg.encode_full_compute_compositor_pipeline(stream, res)
+            need = max(need, int(res.query_status()["total_pairs"]))
+    if need > res.pair_capacity:
+        res.destroy()
+        res = pkg.create_tile_splat_compositor(plan, pair_capacity=int(need * 1.02) + 1024)
+        pkg.create_tile_splat_bind_groups(res, bufs, F["color"], F["gb"])
+    for deg, (us, views) in seqs.items():
+
+        def run():
+            for u, v in zip(us, views):
+                pkg.sort_back_to_front(stream, res, v, bufs["sorted_indices"])
+                pkg.write_frame_uniform_buffer(res, u)
+                pkg.encode_full_compute_compositor_pipeline(stream, res)
+
+        run()  # warm: sizes, graph, costs of the sequence's own frames
+        torch.cuda.synchronize()
+        s.record(stream)
+        run()
+        e.record(stream)
+        e.synchronize()
+        res.check_frame()
+        out[f"ms_per_frame_{deg:g}deg"] = round(s.elapsed_time(e) / frames, 4)
+    # back to the static camera for the legs that follow (they share the
+    # bound sortedIndices and the output images)
+    view0 = np.asarray(cam0.frame(wl.width, wl.height)["view"], np.float32).reshape(-1)
+    pkg.sort_back_to_front(stream, res, view0, bufs["sorted_indices"])
+    res.destroy()
+    F["res"].check_frame()
+    pkg.encode_full_compute_compositor_pipeline(stream, F["res"])
+    torch.cuda.synchronize()
+    return out
 
 
 def run_deferred(pkg, F, wl, args, dev, cpu: bool) -> dict:

@@ -41,6 +41,7 @@ struct hdsr_compositor {
   bool outputs_bound = false;
   bool sorted_valid = false;
   bool entries_valid = false;      // a.entries holds the last full frame's per-tile lists
+  bool cost_stale = true;          // a.tile_cost holds no raster of the bound scene: cleared by the next frame
   cudaStream_t last_stream = nullptr;
   bool has_last_stream = false;
   uint64_t launches = 0;           // kernels queued by this handle
@@ -234,6 +235,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.tile_dmax, M, "tile_dmax");
   ALLOC(a.tile_off, M, "tile_offsets");
   ALLOC(a.tile_order, (uint64_t)plan->tile_columns * plan->tile_rows, "tile_order");
+  ALLOC(a.tile_cost, 2ull * plan->tile_columns * plan->tile_rows, "tile_cost");
   ALLOC(a.tile_log, M, "tile_log");
   ALLOC(a.entries, cap, "tile_entries");
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
@@ -331,6 +333,7 @@ hdsr_status hdsr_bind_scene(hdsr_compositor* h, const hdsr_scene_views* sc) {
   a.sh_degree = sc->sh_degree;
   h->scene_bound = true;
   h->sorted_valid = false;
+  h->cost_stale = true;
   drop_graph(h);
   return HDSR_OK;
 }
@@ -510,6 +513,17 @@ static hdsr_status encode_raster(hdsr_compositor* h, cudaStream_t s, bool full) 
     // is the one control word it must start from zero
     e = cudaMemsetAsync(a.ctl + kCtlRasterTile, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return cuda_fail(h, e, "reset raster counter");
+  }
+  if (full && a.tile_count) {
+    // the work order follows the last raster's tile costs; a new scene's
+    // first frame starts from none (the tile scan's order)
+    if (h->cost_stale) {
+      e = cudaMemsetAsync(a.tile_cost, 0, 2ull * a.tile_count * sizeof(uint32_t), s);
+      if (e != cudaSuccess) return cuda_fail(h, e, "reset tile costs");
+      h->cost_stale = false;
+    }
+    if ((e = launch_work_order(a, s)) != cudaSuccess) return cuda_fail(h, e, "work_order");
+    h->launches += 1;
   }
   if ((e = launch_raster(a, s)) != cudaSuccess) return cuda_fail(h, e, "raster");
   mark(h, s, 17);

@@ -132,6 +132,7 @@ struct FrameArgs {
   uint32_t* tile_dmax;
   uint32_t* tile_off;
   uint32_t* tile_order;           // tile_count: ty << 16 | tx, the rasterisers' work order
+  uint32_t* tile_cost;            // 2 x tile_count: each half tile's cost in the last raster
   float2* tile_log;               // (logMin, keyScale)
   // entries
   unsigned long long* sorted_keys;  // optional: tile, 20-bit log-depth key, sortRank per entry
@@ -347,6 +348,9 @@ cudaError_t launch_log_depth_keys(const FrameArgs& a, cudaStream_t s);
 // back-to-front order of the bound positions for a view matrix (row 2 of the
 // view transform: view[2], view[6], view[10], view[14]) into `out`
 cudaError_t launch_sort_back_to_front(const FrameArgs& a, const double vrow[4], uint32_t* out, cudaStream_t s);
+// the rasteriser's work order from the last raster's per-tile costs, most
+// expensive first (1 launch; leaves the tile scan's order when there are none)
+cudaError_t launch_work_order(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_raster(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_backward(const BwdArgs& b, cudaStream_t s);  // 3 launches
 cudaError_t launch_bwd_prep(const BwdArgs& b, cudaStream_t s);  // hdsr_backward_prep.cu

@@ -156,8 +156,13 @@ HDSR_HD float hi16(uint32_t w) { return f16_to_f32(w >> 16); }
 // arithmetic, at most 2.6 ulp in f32 Horner steps against the true exp on
 // (-4, 0]). A pixel only takes a splat when the power is > -4, so the scale
 // 2^k, k in [-6, 0], is exact in one multiply; below that the value is unused.
+// k is the integer nearest the exact x log2(e): the fma adds 1.5 * 2^23, where
+// the float spacing is 1, so its rounding rounds the product to an integer
+// and leaves k + 2^22 in the low mantissa bits (no conversion instructions);
+// shifted into the exponent field those bits give 2^k.
 HDSR_HD float composite_expf(float x) {
-  const float k = rintf(x * 1.44269502162933349609375f);
+  const float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
+  const float k = t - 12582912.0f;
   float r = fmaf(k, -0.693145751953125f, x);
   r = fmaf(k, -1.428606765330187045e-06f, r);
   float p = 0x1.0fe5c6p-7f;
@@ -166,7 +171,7 @@ HDSR_HD float composite_expf(float x) {
   p = fmaf(p, r, 0x1.fffd1ap-2f);
   p = fmaf(p, r, 0x1.fffff6p-1f);
   p = fmaf(p, r, 0x1.000002p+0f);
-  return p * u2f((uint32_t)((int)k + 127) << 23);
+  return p * u2f((f2u(t) << 23) + 0x3F800000u);
 }
 
 // 16-bit x/y interleave, x on even bits (gpu_tile_splat_composite.wgsl:33-47).

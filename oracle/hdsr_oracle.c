@@ -99,11 +99,14 @@ float orc_logf(float x) {
 }
 
 /* exp of the composite's power, the same steps as the kernels' composite_expf:
- * Cody-Waite reduction (ln2 in two parts), degree-5 polynomial fitted for least
- * maximum relative error on |r| <= ln2/2 (own Remez fit), scale 2^k exact for
- * k in [-6, 0] (the power range a pixel uses, (-4, 0]). */
+ * k = the integer nearest the exact x log2(e) (an fma with 1.5 * 2^23, whose
+ * rounding rounds to an integer), Cody-Waite reduction (ln2 in two parts),
+ * degree-5 polynomial fitted for least maximum relative error on |r| <= ln2/2
+ * (own Remez fit), scale 2^k from the sum's low bits, exact for k in [-6, 0]
+ * (the power range a pixel uses, (-4, 0]). */
 float orc_composite_expf(float x) {
-  const float k = rintf(x * 1.44269502162933349609375f);
+  const float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
+  const float k = t - 12582912.0f;
   float r = fmaf(k, -0.693145751953125f, x);
   r = fmaf(k, -1.428606765330187045e-06f, r);
   float p = 0x1.0fe5c6p-7f;
@@ -112,7 +115,7 @@ float orc_composite_expf(float x) {
   p = fmaf(p, r, 0x1.fffd1ap-2f);
   p = fmaf(p, r, 0x1.fffff6p-1f);
   p = fmaf(p, r, 0x1.000002p+0f);
-  return p * bitsf((uint32_t)((int)k + 127) << 23);
+  return p * bitsf((fbits(t) << 23) + 0x3F800000u);
 }
 
 /* pack2x16float conversion: IEEE round-to-nearest-even, overflow -> inf,
