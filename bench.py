@@ -636,7 +636,7 @@ def run_ours(args, rank, world, local):
     # end to end through the C ABI with host buffers
     log(f"frames timed: {value:.1f} frames/s")
     e2e = None if args.no_e2e else run_e2e(pkg, F, args, stream, world, dev)
-    moving = run_moving_camera(pkg, F, wl, args, stream)
+    moving = None if args.no_moving else run_moving_camera(pkg, F, wl, args, stream)
 
     # roofline of the dominant HBM-bound pass
     sh_floats = 6 + 3 * ((wl.scene.sh_degree + 1) ** 2 - 1)
@@ -1058,6 +1058,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg (8 scenes, 2,000 requests)")
     ap.add_argument("--no-deferred", action="store_true", help="skip the deferred-tail leg")
     ap.add_argument("--no-sh3", action="store_true", help="skip the 3M-splat SH3 4K orbit leg")
+    ap.add_argument("--no-moving", action="store_true", help="skip the moving-camera leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

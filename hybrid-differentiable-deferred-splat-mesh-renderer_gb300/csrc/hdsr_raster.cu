@@ -301,6 +301,14 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
 // costs recorded (a new scene's first frame) the tile scan's order stays.
 constexpr int kOrderThreads = 1024;
 constexpr int kOrderBuckets = 128;
+constexpr int kOrderUnroll = 8;
+
+// a tile's cost: the larger of its halves' (0 past the grid)
+__device__ __forceinline__ uint32_t tile_cost_of(const FrameArgs& a, uint32_t t) {
+  if (t >= a.tile_count) return 0u;
+  const uint2 c = reinterpret_cast<const uint2*>(a.tile_cost)[t];
+  return max(c.x, c.y);
+}
 
 __device__ __forceinline__ uint32_t cost_bucket(uint32_t c) {
   const uint32_t v = c + 1u;
@@ -313,13 +321,25 @@ __global__ void __launch_bounds__(kOrderThreads) k_work_order(FrameArgs a) {
   __shared__ uint32_t hist[kOrderBuckets];
   __shared__ uint32_t any;
   if (a.ctl[kCtlFlags] & kSkipFlags) return;
+  const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
   for (uint32_t b = threadIdx.x; b < (uint32_t)kOrderBuckets; b += blockDim.x) hist[b] = 0u;
   if (threadIdx.x == 0) any = 0u;
   __syncthreads();
-  for (uint32_t t = threadIdx.x; t < a.tile_count; t += blockDim.x) {
-    const uint32_t c = max(a.tile_cost[2u * t], a.tile_cost[2u * t + 1u]);
-    if (c) any = 1u;
-    atomicAdd(&hist[cost_bucket(c)], 1u);
+  // bucket sizes: one shared-memory atomic per distinct bucket of a warp;
+  // each thread's costs are loaded kOrderUnroll at a time (one latency)
+  const uint32_t step = blockDim.x * kOrderUnroll;
+  for (uint32_t t0 = 0; t0 < a.tile_count; t0 += step) {
+    uint32_t c[kOrderUnroll];
+#pragma unroll
+    for (int u = 0; u < kOrderUnroll; ++u) c[u] = tile_cost_of(a, t0 + u * blockDim.x + threadIdx.x);
+#pragma unroll
+    for (int u = 0; u < kOrderUnroll; ++u) {
+      const uint32_t t = t0 + u * blockDim.x + threadIdx.x;
+      if (c[u]) any = 1u;
+      const uint32_t b = t < a.tile_count ? cost_bucket(c[u]) : 0xFFFFFFFFu;
+      const uint32_t same = __match_any_sync(0xFFFFFFFFu, b);
+      if (b != 0xFFFFFFFFu && (same & lt) == 0u) atomicAdd(&hist[b], (uint32_t)__popc(same));
+    }
   }
   __syncthreads();
   if (!any) return;
@@ -333,10 +353,21 @@ __global__ void __launch_bounds__(kOrderThreads) k_work_order(FrameArgs a) {
     }
   }
   __syncthreads();
-  for (uint32_t t = threadIdx.x; t < a.tile_count; t += blockDim.x) {
-    const uint32_t c = max(a.tile_cost[2u * t], a.tile_cost[2u * t + 1u]);
-    const uint32_t pos = atomicAdd(&hist[cost_bucket(c)], 1u);
-    a.tile_order[pos] = (t / a.cols) << 16 | (t % a.cols);
+  for (uint32_t t0 = 0; t0 < a.tile_count; t0 += step) {
+    uint32_t c[kOrderUnroll];
+#pragma unroll
+    for (int u = 0; u < kOrderUnroll; ++u) c[u] = tile_cost_of(a, t0 + u * blockDim.x + threadIdx.x);
+#pragma unroll
+    for (int u = 0; u < kOrderUnroll; ++u) {
+      const uint32_t t = t0 + u * blockDim.x + threadIdx.x;
+      const uint32_t b = t < a.tile_count ? cost_bucket(c[u]) : 0xFFFFFFFFu;
+      const uint32_t same = __match_any_sync(0xFFFFFFFFu, b);
+      const uint32_t leader = (uint32_t)__ffs(same) - 1u;
+      uint32_t base = 0;
+      if (b != 0xFFFFFFFFu && lane == leader) base = atomicAdd(&hist[b], (uint32_t)__popc(same));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (b != 0xFFFFFFFFu) a.tile_order[base + __popc(same & lt)] = (t / a.cols) << 16 | (t % a.cols);
+    }
   }
 }
 
