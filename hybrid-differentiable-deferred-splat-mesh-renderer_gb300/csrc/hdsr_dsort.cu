@@ -73,6 +73,8 @@ __global__ void __launch_bounds__(kRadixThreads) k_dsort_upsweep0(FrameArgs a) {
   __shared__ uint32_t s_hist[kDBins];
   __shared__ uint32_t s_min[kRadixThreads / 32], s_max[kRadixThreads / 32];
   __shared__ uint32_t s_flag;
+  pdl_wait();
+  pdl_trigger();
   if (dsort_skipped(a, &s_flag)) return;
   const uint32_t N = a.N, tiles = (N + kRadixTile - 1u) / kRadixTile;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -119,6 +121,8 @@ __global__ void __launch_bounds__(256) k_dsort_colscan(FrameArgs a, uint32_t p) 
   __shared__ uint32_t s_w[8];
   __shared__ uint32_t s_carry;
   __shared__ uint32_t s_flag;
+  pdl_wait();
+  pdl_trigger();
   if (dsort_skipped(a, &s_flag)) return;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
   if (p == 0u) {
@@ -213,6 +217,8 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_dsort_downsweep(FrameArgs 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DSweepSmem& S = *reinterpret_cast<DSweepSmem*>(smem_raw);
   __shared__ uint32_t s_flag;
+  pdl_wait();
+  pdl_trigger();
   if (dsort_skipped(a, &s_flag)) return;
   const uint32_t L = a.ctl[kCtlDepthPasses];
   if (p >= L) return;
@@ -356,12 +362,14 @@ cudaError_t launch_depth_sort(const FrameArgs& a, cudaStream_t s) {
   const uint32_t tiles = (a.N + kRadixTile - 1u) / kRadixTile;
   const uint32_t up_grid = tiles < (uint32_t)a.num_sms * 8u ? tiles : (uint32_t)a.num_sms * 8u;
   const uint32_t down_grid = tiles < (uint32_t)grid ? tiles : (uint32_t)grid;
-  k_dsort_upsweep0<<<up_grid, kRadixThreads, 0, s>>>(a);
-  for (uint32_t p = 0; p < 4u; ++p) {
-    k_dsort_colscan<<<kDBins, 256, 0, s>>>(a, p);
-    k_dsort_downsweep<<<down_grid, kRadixThreads, smem, s>>>(a, p);
+  // programmatic dependent launches: each kernel of the chain is scheduled
+  // while its predecessor runs and waits for it in pdl_wait()
+  cudaError_t e = launch_pdl(k_dsort_upsweep0, dim3(up_grid), dim3(kRadixThreads), 0, s, a);
+  for (uint32_t p = 0; p < 4u && e == cudaSuccess; ++p) {
+    e = launch_pdl(k_dsort_colscan, dim3(kDBins), dim3(256), 0, s, a, p);
+    if (e == cudaSuccess) e = launch_pdl(k_dsort_downsweep, dim3(down_grid), dim3(kRadixThreads), smem, s, a, p);
   }
-  return cudaGetLastError();
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace hdsr

@@ -330,6 +330,32 @@ HDSR_HD unsigned long long make_status(uint32_t epoch, unsigned long long flag, 
   return ((unsigned long long)(epoch & 0x3FFFFFFFu) << 34) | (flag << 32) | v;
 }
 
+// Programmatic dependent launch (sm_90 and later). A kernel launched with
+// launch_pdl may be scheduled while the previous kernel of its stream is
+// still running; it calls pdl_wait() before touching any memory, which
+// returns once that kernel has completed and its writes are visible, so the
+// order of effects is that of a plain launch and only the launch latency
+// overlaps. pdl_trigger() lets the next such kernel be scheduled early (it
+// then waits in its own pdl_wait). Without the launch attribute both are
+// no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // launchers (each returns cudaGetLastError() of its launches)
 cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_project(const FrameArgs& a, cudaStream_t s);
