@@ -55,6 +55,8 @@ BUFFER_IDS = {
     "pair_offsets": 9,
     "depth_order": 10,
     "backward_params": 11,
+    "work_order": 12,
+    "tile_costs": 13,
 }
 
 

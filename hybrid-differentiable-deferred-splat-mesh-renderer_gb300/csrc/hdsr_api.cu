@@ -744,6 +744,8 @@ hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, u
     case HDSR_BUF_BACKWARD_PARAMS:
       if (!h->bwd_par) return fail(h, HDSR_ERR_UNSUPPORTED, "create with HDSR_CFG_BACKWARD");
       *ptr = h->bwd_par; *bytes = N * 48; break;
+    case HDSR_BUF_WORK_ORDER: *ptr = a.tile_order; *bytes = (uint64_t)a.tile_count * 4; break;
+    case HDSR_BUF_TILE_COSTS: *ptr = a.tile_cost; *bytes = (uint64_t)a.tile_count * 8; break;
     default: return fail(h, HDSR_ERR_INVALID_ARG, "unknown buffer id");
   }
   return HDSR_OK;

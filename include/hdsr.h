@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define HDSR_ABI_VERSION 2
+#define HDSR_ABI_VERSION 3
 
 typedef enum hdsr_status {
   HDSR_OK = 0,
@@ -201,9 +201,14 @@ typedef enum hdsr_buffer_id {
   HDSR_BUF_PAIR_OFFSETS = 9,  /* u32[N] exclusive prefix of per-splat superblock counts, depth order */
   HDSR_BUF_DEPTH_ORDER = 10,  /* u32[N] ascending (depth bits, sortRank): sortRank in bits 0-23,
                                  the splat's superblock count in bits 24-31 */
-  HDSR_BUF_BACKWARD_PARAMS = 11 /* float4[N][3] per sortRank, written by hdsr_encode_backward: the
+  HDSR_BUF_BACKWARD_PARAMS = 11, /* float4[N][3] per sortRank, written by hdsr_encode_backward: the
                                  adjoint's screen-space parameters (cx, cy, ia, ib | ic, opacity,
                                  r, g | b, 0, 0, 0); HDSR_CFG_BACKWARD handles only */
+  HDSR_BUF_WORK_ORDER = 12,   /* u32[tile_count] ty << 16 | tx: the order in which the last full
+                                 frame's rasteriser took its tiles (a permutation of the tiles) */
+  HDSR_BUF_TILE_COSTS = 13    /* u32[2 * tile_count] per half tile (index 2 * (ty * cols + tx) +
+                                 half): the last raster's cost, from which the next full frame
+                                 orders its tiles (most expensive first); 0 before any raster */
 } hdsr_buffer_id;
 
 /* Device address and byte size of an internal buffer (valid until destroy).
