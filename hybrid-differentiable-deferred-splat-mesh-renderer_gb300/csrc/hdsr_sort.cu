@@ -44,6 +44,8 @@ __device__ __forceinline__ bool skipped(const RadixJob& j) { return (*j.flags & 
 // Upsweep: per block-tile digit counts, bin-major (tile_digits[bin*cap+tile]).
 __global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
   __shared__ uint32_t s_hist[kRadixBins];
+  pdl_wait();
+  pdl_trigger();
   if (skipped(j)) return;
   const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
@@ -75,6 +77,8 @@ __global__ void __launch_bounds__(256) k_radix_colscan(RadixJob j) {
   constexpr uint32_t IT = 16;
   __shared__ uint32_t s_w[8];
   __shared__ uint32_t s_carry;
+  pdl_wait();
+  pdl_trigger();
   if (skipped(j)) return;
   const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
@@ -129,6 +133,8 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
   constexpr uint32_t W = kRadixThreads / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SweepSmem& S = *reinterpret_cast<SweepSmem*>(smem_raw);
+  pdl_wait();
+  pdl_trigger();
   if (skipped(j)) return;
   const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
@@ -474,11 +480,14 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
     grid_mid = resident_blocks(k_radix_downsweep<false>, kRadixThreads, num_sms, smem);
     grid_last = resident_blocks(k_radix_downsweep<true>, kRadixThreads, num_sms, smem);
   }
-  k_radix_upsweep<<<num_sms * 8, kRadixThreads, 0, s>>>(j);
-  k_radix_colscan<<<1u << j.bits, 256, 0, s>>>(j);
-  if (last) k_radix_downsweep<true><<<grid_last, kRadixThreads, smem, s>>>(j);
-  else k_radix_downsweep<false><<<grid_mid, kRadixThreads, smem, s>>>(j);
-  return cudaGetLastError();
+  // programmatic dependent launches (pdl_wait at the top of each kernel)
+  cudaError_t e = launch_pdl(k_radix_upsweep, dim3(num_sms * 8), dim3(kRadixThreads), 0, s, j);
+  if (e == cudaSuccess) e = launch_pdl(k_radix_colscan, dim3(1u << j.bits), dim3(256), 0, s, j);
+  if (e == cudaSuccess) {
+    if (last) e = launch_pdl(k_radix_downsweep<true>, dim3(grid_last), dim3(kRadixThreads), smem, s, j);
+    else e = launch_pdl(k_radix_downsweep<false>, dim3(grid_mid), dim3(kRadixThreads), smem, s, j);
+  }
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // Chunk masks: for every 32-entry chunk of the sorted superblock lists, the
@@ -526,6 +535,8 @@ namespace {
 __global__ void __launch_bounds__(256) k_view_keys(const float* pos, uint32_t N, double v2, double v6, double v10,
                                                    double v14, unsigned long long* keys, uint32_t* ctl) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  pdl_wait();
+  pdl_trigger();
   if (i == 0) {
     ctl[kCtlSortCount] = N;
     ctl[kCtlSortFlags] = 0u;
@@ -545,7 +556,9 @@ __global__ void __launch_bounds__(256) k_view_keys(const float* pos, uint32_t N,
 
 cudaError_t launch_sort_back_to_front(const FrameArgs& a, const double vrow[4], uint32_t* out, cudaStream_t s) {
   if (!a.N) return cudaSuccess;
-  k_view_keys<<<(a.N + 255) / 256, 256, 0, s>>>(a.pos, a.N, vrow[0], vrow[1], vrow[2], vrow[3], a.dkeys_a, a.ctl);
+  cudaError_t ek = launch_pdl(k_view_keys, dim3((a.N + 255) / 256), dim3(256), 0, s, a.pos, a.N, vrow[0], vrow[1],
+                              vrow[2], vrow[3], a.dkeys_a, a.ctl);
+  if (ek != cudaSuccess) return ek;
   RadixJob j{};
   j.count = a.ctl + kCtlSortCount;
   j.flags = a.ctl + kCtlSortFlags;
