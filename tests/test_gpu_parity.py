@@ -365,6 +365,33 @@ def test_bad_sorted_index_is_flagged(cuda, pkg, orc):
     assert_frame_parity(orc, g)
 
 
+def test_repeated_sorted_index_projects_each_position(cuda, pkg, orc):
+    # sortedIndices that is not a permutation (a repeated id, another never
+    # named): every position projects the id it names, as the reference does
+    # (the repeated splat is drawn twice), and the frame is the oracle's;
+    # then the same handle with the permutation again matches too
+    import torch
+
+    scene = pkg.workloads.plain_scene(3000, seed=11)
+    cam = pkg.camera.look_from((0.2, 0.1, 5.0))
+    packed = pkg.splats.pack_splat_attributes(scene)
+    plan = pkg.plan_tile_splat_compositor(96, 80, 16, 3000)
+    _, fr = pkg.frame_uniforms_for(plan, cam)
+    order = pkg.splats.back_to_front_order(packed.positions, fr["view"]).copy()
+    repeated = order.copy()
+    repeated[17] = repeated[1234]
+    g = render_gpu(pkg, scene, cam, 96, 80, order=repeated)
+    st = g["res"].query_status()
+    assert not st["device_flags"] & pkg._lib.DEV_BAD_INDEX
+    assert_frame_parity(orc, g)
+    g["bufs"]["sorted_indices"].copy_(torch.from_numpy(order.view(np.int32)))
+    g["order"] = order
+    pkg.encode_full_compute_compositor_pipeline(None, g["res"])
+    torch.cuda.synchronize()
+    assert_frame_parity(orc, g)
+    g["res"].destroy()
+
+
 def test_bind_validation(cuda, pkg):
     wl = pkg.workloads.plain50k()
     plan = pkg.plan_tile_splat_compositor(64, 64, 16, 10)
