@@ -42,6 +42,41 @@ def test_device_order_equals_host_order(cuda, pkg, seed):
     res.destroy()
 
 
+@pytest.mark.parametrize("case", ["inside", "flat", "nan"])
+def test_device_order_over_every_depth_range(cuda, pkg, case):
+    # Depths of both signs (camera inside the cloud), a nearly flat cloud
+    # (keys a few ulps apart, many ties), and non-finite positions (keys that
+    # sort last, by id).
+    import torch
+
+    scene = pkg.workloads.plain_scene(40_000, 7)
+    if case == "inside":
+        cam = pkg.camera.OrbitCamera(azimuth=0.7, elevation=0.1, distance=0.05)
+    else:
+        cam = pkg.camera.OrbitCamera(azimuth=0.0, elevation=0.0, distance=4.0)
+    fr = cam.frame(320, 240)
+    view = np.asarray(fr["view"], np.float32).reshape(-1)
+    if case == "flat":
+        # every point on one plane facing the camera, a hair apart in depth
+        v = view.astype(np.float64)
+        fwd = np.array([v[2], v[6], v[10]])
+        p = scene.positions.astype(np.float64)
+        p -= np.outer(p @ fwd, fwd) / (fwd @ fwd)
+        p += np.outer(np.random.default_rng(3).uniform(0, 1e-4, len(p)), fwd)
+        scene.positions[:] = p.astype(np.float32)
+    if case == "nan":
+        scene.positions[[5, 77, 31000]] = np.nan
+    packed, plan, res, bufs, color, gb = _handle(pkg, scene)
+    out = torch.empty(scene.count, dtype=torch.int32, device="cuda")
+    pkg.sort_back_to_front(None, res, view, out)
+    torch.cuda.synchronize()
+    want = pkg.splats.back_to_front_order(packed.positions, view)
+    assert np.array_equal(u32(out), want)
+    if case == "nan":
+        assert sorted(u32(out)[-3:].tolist()) == [5, 77, 31000]
+    res.destroy()
+
+
 def test_device_sorted_frame_matches_the_host_sorted_frame(cuda, pkg, orc):
     import torch
 
