@@ -87,7 +87,14 @@ __device__ __forceinline__ void write_invisible(const FrameArgs& a, uint32_t r) 
   a.dkeys_a[r] = ((unsigned long long)kSentinel << 32) | r;
 }
 
-__global__ void __launch_bounds__(256) k_project(FrameArgs a) {
+// MINB: resident 256-thread blocks per SM the register budget is fitted to.
+// The gathers are latency-bound, so more threads in flight help while the
+// registers suffice: 6 blocks (40 registers) for scenes of SH degree 0-1
+// (hot760k: 0.058 -> 0.054 ms); degrees 2-3 keep the unconstrained budget
+// (at 6 blocks the degree-3 terms spill: sh3_3m 0.474 -> 0.527 ms). Both
+// instantiations compute the same frame; the bound scene's degree picks one.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_project(FrameArgs a) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= a.N) return;
   const float* U = a.U;
@@ -479,7 +486,10 @@ cudaError_t launch_frame_init(const FrameArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_project(const FrameArgs& a, cudaStream_t s) {
-  if (a.N) k_project<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  if (a.N) {
+    if (a.sh_degree <= 1u) k_project<6><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+    else k_project<1><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
