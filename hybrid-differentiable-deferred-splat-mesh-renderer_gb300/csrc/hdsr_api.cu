@@ -239,8 +239,8 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
   ALLOC(a.tile_log, M, "tile_log");
   ALLOC(a.entries, cap, "tile_entries");
   if (h->cfg.flags & HDSR_CFG_KEEP_SORTED_KEYS) { ALLOC(a.sorted_keys, cap, "sorted_keys"); }
-  ALLOC(a.tile_digits, (uint64_t)a.radix_tiles_cap * kRadixBins, "tile_digits");
-  ALLOC(a.bin_base, (uint64_t)kRadixBins, "bin_base");
+  ALLOC(a.tile_digits, (uint64_t)a.radix_tiles_cap * kRadixWideBins, "tile_digits");
+  ALLOC(a.bin_base, (uint64_t)kRadixWideBins, "bin_base");
   a.dsort_tiles_cap = depth_sort_tiles(N);
   ALLOC(a.dsort_hist0, (uint64_t)depth_sort_bins() * a.dsort_tiles_cap, "depth_sort_counts_0");
   ALLOC(a.dsort_hist1, (uint64_t)depth_sort_bins() * a.dsort_tiles_cap, "depth_sort_counts_1");
@@ -255,7 +255,7 @@ hdsr_status hdsr_create_tile_splat_compositor(const hdsr_plan* plan, const hdsr_
 #undef ALLOC
   if (s != HDSR_OK) { free_all(h); delete h; return s; }
   a.U = U;
-  a.sbk_sorted = a.sb_bits > kRadixBits ? a.sbk_a : a.sbk_b;  // where the last superblock pass writes
+  a.sbk_sorted = a.sb_bits > kRadixWideBits ? a.sbk_a : a.sbk_b;  // where the last superblock pass writes
   // status words start at epoch 0, which no frame uses. The clears run on the
   // legacy stream and are complete when create returns: the caller's stream
   // may be a non-blocking one, which does not wait for the legacy stream.
@@ -478,13 +478,14 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   RadixJob sj = dj;
   sj.count = a.ctl + kCtlSbPairs;
   sj.out_low = nullptr;
-  const uint32_t sb_passes = a.sb_bits > kRadixBits ? 2u : 1u;
+  // 9-bit digits: one pass up to 512 superblocks (a 4K viewport has 510)
+  const uint32_t sb_passes = a.sb_bits > kRadixWideBits ? 2u : 1u;
   for (uint32_t p = 0; p < sb_passes; ++p) {
     sj.in = (p & 1u) ? a.sbk_b : a.sbk_a;
     sj.out = (p & 1u) ? nullptr : a.sbk_b;
     sj.out_keys = (p & 1u) ? a.sbk_a : a.sbk_b;
-    sj.shift = kSbKeyShift + kRadixBits * p;
-    sj.bits = p == 0 ? (a.sb_bits < kRadixBits ? a.sb_bits : kRadixBits) : a.sb_bits - kRadixBits;
+    sj.shift = kSbKeyShift + kRadixWideBits * p;
+    sj.bits = p == 0 ? (a.sb_bits < kRadixWideBits ? a.sb_bits : kRadixWideBits) : a.sb_bits - kRadixWideBits;
     if ((e = launch_radix_pass(sj, p + 1 == sb_passes, a.num_sms, s)) != cudaSuccess)
       return cuda_fail(h, e, "superblock_sort");
   }
@@ -501,7 +502,7 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
     h->launches += 2;
   }
   h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 9 * n_splat_launch + 1 +
-                 3 * (a.sb_bits > kRadixBits ? 2 : 1) + (a.tile_count ? 1 : 0);
+                 3 * (a.sb_bits > kRadixWideBits ? 2 : 1) + (a.tile_count ? 1 : 0);
   return HDSR_OK;
 }
 

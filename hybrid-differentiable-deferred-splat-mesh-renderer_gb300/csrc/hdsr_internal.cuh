@@ -38,6 +38,9 @@ enum Ctl : int {
 
 constexpr uint32_t kRadixBits = 8;               // widest digit
 constexpr uint32_t kRadixBins = 1u << kRadixBits;
+// wide digits: the superblock passes (up to 512 superblocks in one pass)
+constexpr uint32_t kRadixWideBits = 9;
+constexpr uint32_t kRadixWideBins = 1u << kRadixWideBits;
 constexpr uint32_t kDepthPasses = 4;             // 32 depth bits
 
 // Superblocks: squares of 8x8 tiles. A superblock list entry is
@@ -72,8 +75,8 @@ struct RadixJob {
   unsigned long long low_mask;
   const uint32_t* count;            // number of keys (device)
   const uint32_t* flags;            // frame flags: skip the pass on overflow
-  uint32_t* tile_digits;            // kRadixBins * tiles_cap counts -> offsets
-  uint32_t* bin_base;               // kRadixBins totals -> bases
+  uint32_t* tile_digits;            // kRadixWideBins * tiles_cap counts -> offsets
+  uint32_t* bin_base;               // kRadixWideBins totals -> bases
   uint32_t tiles_cap;
   uint32_t shift;
   uint32_t bits;
@@ -365,7 +368,8 @@ cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s);
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s);  // 3 launches
 cudaError_t launch_chunk_masks(const FrameArgs& a, cudaStream_t s);   // 1 launch
-cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);  // 3 launches
+// one stable pass over j.bits digit bits (8: 256 bins; 9: 512 bins), 3 launches
+cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s);
 // the frame's depth sort (hdsr_dsort.cu): a.dkeys_a -> a.order, 9 launches
 cudaError_t launch_depth_sort(const FrameArgs& a, cudaStream_t s);
 uint32_t depth_sort_tiles(uint32_t N);  // blocks of its tables (dsort_tiles_cap)

@@ -13,7 +13,7 @@
 //      bits over u64 keys depth << 32 | sortRank; the pairs are then emitted
 //      in that depth order (hdsr_scan.cu);
 //   2. the tile: the pairs are listed per superblock of 8x8 tiles by one
-//      (two above 256 superblocks) stable 8-bit pass over the superblock
+//      (two above 512 superblocks) stable 9-bit pass over the superblock
 //      index. A tile's entries are then its superblock list filtered by the
 //      entries' local rects: the rasterisers walk the lists (k_chunk_masks
 //      marks which 32-entry chunks hold which tiles), and only on demand is
@@ -42,8 +42,10 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 __device__ __forceinline__ bool skipped(const RadixJob& j) { return (*j.flags & kSkipFlags) != 0u; }
 
 // Upsweep: per block-tile digit counts, bin-major (tile_digits[bin*cap+tile]).
+// BINS: the widest digit the instantiation handles (256 or 512 bins).
+template <uint32_t BINS>
 __global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
-  __shared__ uint32_t s_hist[kRadixBins];
+  __shared__ uint32_t s_hist[BINS];
   pdl_wait();
   pdl_trigger();
   if (skipped(j)) return;
@@ -51,18 +53,18 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
   const uint32_t dmask = (1u << j.bits) - 1u;
   for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
-    for (uint32_t i = threadIdx.x; i < kRadixBins; i += blockDim.x) s_hist[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < BINS; i += blockDim.x) s_hist[i] = 0u;
     __syncthreads();
     const uint32_t base = tile * kRadixTile;
     uint32_t dig[kRadixItems];
 #pragma unroll
     for (uint32_t i = 0; i < kRadixItems; ++i) {
       const uint32_t g = base + i * kRadixThreads + threadIdx.x;
-      dig[i] = g < P ? (uint32_t)(j.in[g] >> j.shift) & dmask : kRadixBins;
+      dig[i] = g < P ? (uint32_t)(j.in[g] >> j.shift) & dmask : BINS;
     }
 #pragma unroll
     for (uint32_t i = 0; i < kRadixItems; ++i)
-      if (dig[i] < kRadixBins) atomicAdd(&s_hist[dig[i]], 1u);
+      if (dig[i] < BINS) atomicAdd(&s_hist[dig[i]], 1u);
     __syncthreads();
     for (uint32_t b = threadIdx.x; b <= dmask; b += blockDim.x)
       j.tile_digits[(size_t)b * j.tiles_cap + tile] = s_hist[b];
@@ -119,20 +121,40 @@ __global__ void __launch_bounds__(256) k_radix_colscan(RadixJob j) {
 }
 
 // Shared memory of one downsweep block (dynamic).
+template <uint32_t BINS>
 struct SweepSmem {
   unsigned long long keys[kRadixTile];
-  uint32_t whist[kRadixThreads / 32][kRadixBins];
-  uint32_t excl[kRadixBins];  // per digit: global offset minus tile-local bucket start
+  uint32_t whist[kRadixThreads / 32][BINS];
+  uint32_t excl[BINS];  // per digit: global offset minus tile-local bucket start
   uint32_t wsum[kRadixThreads / 32];
 };
 
+// Block-wide exclusive scan of one value per thread (kRadixThreads threads).
+__device__ __forceinline__ uint32_t radix_excl_scan(uint32_t v, uint32_t* wsum, uint32_t lane, uint32_t warp) {
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= (uint32_t)o) inc += t;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t off = 0;
+  for (uint32_t w = 0; w < warp; ++w) off += wsum[w];
+  __syncthreads();
+  return off + inc - v;
+}
+
 // Downsweep: rank (warp match, leader atomic + shuffle), fold per-warp
 // offsets into one table, scatter to shared memory in digit order, write out.
-template <bool LAST>
+// BINS / kRadixThreads digits per thread in the bookkeeping.
+template <uint32_t BINS, bool LAST>
 __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j) {
   constexpr uint32_t W = kRadixThreads / 32;
+  constexpr uint32_t DPT = BINS / kRadixThreads;
+  static_assert(DPT * kRadixThreads == BINS, "digits split evenly over the threads");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SweepSmem& S = *reinterpret_cast<SweepSmem*>(smem_raw);
+  SweepSmem<BINS>& S = *reinterpret_cast<SweepSmem<BINS>*>(smem_raw);
   pdl_wait();
   pdl_trigger();
   if (skipped(j)) return;
@@ -142,28 +164,26 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
   const uint32_t dmask = (1u << j.bits) - 1u;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t lt = lanemask_lt();
-  static_assert(kRadixBins == kRadixThreads, "one digit per thread in the bookkeeping");
-  // global base of digit `tid`: exclusive scan of the bin totals (each block
-  // computes it; 256 values)
-  uint32_t digit_base;
+  // global bases of this thread's digits: exclusive scan of the bin totals
+  // (each block computes it)
+  uint32_t digit_base[DPT];
   {
-    const uint32_t tot = tid <= dmask ? j.bin_base[tid] : 0u;
-    uint32_t inc = tot;
+    uint32_t tot[DPT], sum = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-      if (lane >= (uint32_t)o) inc += t;
+    for (uint32_t k = 0; k < DPT; ++k) {
+      const uint32_t d = tid * DPT + k;
+      tot[k] = d <= dmask ? j.bin_base[d] : 0u;
+      sum += tot[k];
     }
-    if (lane == 31) S.wsum[warp] = inc;
-    __syncthreads();
-    uint32_t off = 0;
-    for (uint32_t w = 0; w < warp; ++w) off += S.wsum[w];
-    digit_base = off + inc - tot;
-    __syncthreads();
+    uint32_t run = radix_excl_scan(sum, S.wsum, lane, warp);
+#pragma unroll
+    for (uint32_t k = 0; k < DPT; ++k) {
+      digit_base[k] = run;
+      run += tot[k];
+    }
   }
   for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
-    for (uint32_t i = tid; i < W * kRadixBins; i += kRadixThreads) (&S.whist[0][0])[i] = 0u;
-    const uint32_t d = tid;
+    for (uint32_t i = tid; i < W * BINS; i += kRadixThreads) (&S.whist[0][0])[i] = 0u;
     __syncthreads();
     const uint32_t base = tile * kRadixTile;
     {
@@ -177,37 +197,41 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
 #pragma unroll
       for (uint32_t i = 0; i < kRadixItems; ++i) {
         const uint32_t g = base + warp * (32u * kRadixItems) + i * 32u + lane;
-        const uint32_t dig = g < P ? (uint32_t)(key[i] >> shift) & dmask : kRadixBins;
+        const uint32_t dig = g < P ? (uint32_t)(key[i] >> shift) & dmask : BINS;
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig);
         const uint32_t lower = __popc(peers & lt);
         const uint32_t leader = __ffs(peers) - 1u;
         uint32_t prior = 0u;
-        if (lower == 0u && dig < kRadixBins) prior = atomicAdd(&S.whist[warp][dig], (uint32_t)__popc(peers));
+        if (lower == 0u && dig < BINS) prior = atomicAdd(&S.whist[warp][dig], (uint32_t)__popc(peers));
         prior = __shfl_sync(0xFFFFFFFFu, prior, leader);  // every lane reads its group's leader
         rank[i] = prior + lower;
       }
       __syncthreads();
-      // digit d: count over warps, tile-local bucket start, per-warp offsets
-      uint32_t run = 0;
+      // this thread's digits: count over warps, tile-local bucket start,
+      // per-warp offsets
+      uint32_t cnt[DPT], sum = 0;
 #pragma unroll
-      for (uint32_t w = 0; w < W; ++w) run += S.whist[w][d];
-      uint32_t inc = run;
+      for (uint32_t k = 0; k < DPT; ++k) {
+        const uint32_t d = tid * DPT + k;
+        uint32_t c = 0;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-        if (lane >= (uint32_t)o) inc += t;
+        for (uint32_t w = 0; w < W; ++w) c += S.whist[w][d];
+        cnt[k] = c;
+        sum += c;
       }
-      if (lane == 31) S.wsum[warp] = inc;
-      __syncthreads();
-      uint32_t woff = 0;
-      for (uint32_t w = 0; w < warp; ++w) woff += S.wsum[w];
-      uint32_t e = woff + inc - run;
-      if (d <= dmask) S.excl[d] = digit_base + j.tile_digits[(size_t)d * j.tiles_cap + tile] - e;
+      uint32_t e = radix_excl_scan(sum, S.wsum, lane, warp);
 #pragma unroll
-      for (uint32_t w = 0; w < W; ++w) {
-        const uint32_t c = S.whist[w][d];
-        S.whist[w][d] = e;
-        e += c;
+      for (uint32_t k = 0; k < DPT; ++k) {
+        const uint32_t d = tid * DPT + k;
+        if (d <= dmask) S.excl[d] = digit_base[k] + j.tile_digits[(size_t)d * j.tiles_cap + tile] - e;
+        uint32_t r = e;
+#pragma unroll
+        for (uint32_t w = 0; w < W; ++w) {
+          const uint32_t c = S.whist[w][d];
+          S.whist[w][d] = r;
+          r += c;
+        }
+        e += cnt[k];
       }
       __syncthreads();
 #pragma unroll
@@ -468,26 +492,32 @@ int resident_blocks(K kernel, int threads, int sms, size_t smem) {
 
 }  // namespace
 
-cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s) {
+template <uint32_t BINS>
+static cudaError_t radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s) {
   static int grid_mid = 0, grid_last = 0;
-  const size_t smem = sizeof(SweepSmem);
+  const size_t smem = sizeof(SweepSmem<BINS>);
   if (!grid_mid) {
-    cudaError_t e = cudaFuncSetAttribute(k_radix_downsweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_radix_downsweep<BINS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_radix_downsweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e = cudaFuncSetAttribute(k_radix_downsweep<BINS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    grid_mid = resident_blocks(k_radix_downsweep<false>, kRadixThreads, num_sms, smem);
-    grid_last = resident_blocks(k_radix_downsweep<true>, kRadixThreads, num_sms, smem);
+    grid_mid = resident_blocks(k_radix_downsweep<BINS, false>, kRadixThreads, num_sms, smem);
+    grid_last = resident_blocks(k_radix_downsweep<BINS, true>, kRadixThreads, num_sms, smem);
   }
   // programmatic dependent launches (pdl_wait at the top of each kernel)
-  cudaError_t e = launch_pdl(k_radix_upsweep, dim3(num_sms * 8), dim3(kRadixThreads), 0, s, j);
+  cudaError_t e = launch_pdl(k_radix_upsweep<BINS>, dim3(num_sms * 8), dim3(kRadixThreads), 0, s, j);
   if (e == cudaSuccess) e = launch_pdl(k_radix_colscan, dim3(1u << j.bits), dim3(256), 0, s, j);
   if (e == cudaSuccess) {
-    if (last) e = launch_pdl(k_radix_downsweep<true>, dim3(grid_last), dim3(kRadixThreads), smem, s, j);
-    else e = launch_pdl(k_radix_downsweep<false>, dim3(grid_mid), dim3(kRadixThreads), smem, s, j);
+    if (last) e = launch_pdl(k_radix_downsweep<BINS, true>, dim3(grid_last), dim3(kRadixThreads), smem, s, j);
+    else e = launch_pdl(k_radix_downsweep<BINS, false>, dim3(grid_mid), dim3(kRadixThreads), smem, s, j);
   }
   return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStream_t s) {
+  return j.bits > kRadixBits ? radix_pass<kRadixWideBins>(j, last, num_sms, s)
+                             : radix_pass<kRadixBins>(j, last, num_sms, s);
 }
 
 // Chunk masks: for every 32-entry chunk of the sorted superblock lists, the
