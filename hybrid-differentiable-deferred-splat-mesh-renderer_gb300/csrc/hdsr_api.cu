@@ -42,6 +42,8 @@ struct hdsr_compositor {
   bool sorted_valid = false;
   bool entries_valid = false;      // a.entries holds the last full frame's per-tile lists
   bool cost_stale = true;          // a.tile_cost holds no raster of the bound scene: cleared by the next frame
+  float cost_view[3] = {0.0f, 0.0f, 0.0f};  // view direction of the frame whose costs a.tile_cost holds
+  bool cost_view_valid = false;
   cudaStream_t last_stream = nullptr;
   bool has_last_stream = false;
   uint64_t launches = 0;           // kernels queued by this handle
@@ -584,6 +586,11 @@ static void capture_frame(hdsr_compositor* h, cudaStream_t s) {
   cudaGetLastError();  // a failed capture leaves no sticky error: clear its record
 }
 
+// Camera turn (degrees) up to which the last frame's tile costs still order
+// the raster's tiles.
+constexpr double kCostKeepDegrees = 10.0;
+const double kCostKeepCos = std::cos(kCostKeepDegrees * 3.14159265358979323846 / 180.0);
+
 static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
   hdsr_status st = encode_checks(h, full);
   if (st != HDSR_OK) return st;
@@ -607,6 +614,28 @@ static hdsr_status encode(hdsr_compositor* h, void* stream, bool full) {
     h->device_u_valid = true;
   }
   mark(h, s, 0);
+  if (full && a.tile_count) {
+    // The raster's work order follows the last frame's tile costs. After a
+    // camera turn of more than kCostKeepDegrees they describe other tiles
+    // (an orbit's 45-degree steps made the raster 4% slower than the tile
+    // scan's order), so they are cleared and this frame takes the scan's
+    // order. The view direction is the view matrix's third row.
+    const float* u = h->uniforms;
+    const double f[3] = {u[34], u[38], u[42]};
+    if (h->cost_view_valid) {
+      const double dot = f[0] * h->cost_view[0] + f[1] * h->cost_view[1] + f[2] * h->cost_view[2];
+      const double nn = std::sqrt((f[0] * f[0] + f[1] * f[1] + f[2] * f[2]) *
+                                  ((double)h->cost_view[0] * h->cost_view[0] +
+                                   (double)h->cost_view[1] * h->cost_view[1] +
+                                   (double)h->cost_view[2] * h->cost_view[2]));
+      if (!(dot >= kCostKeepCos * nn)) {
+        cudaError_t e = cudaMemsetAsync(a.tile_cost, 0, 2ull * a.tile_count * sizeof(uint32_t), s);
+        if (e != cudaSuccess) return cuda_fail(h, e, "reset tile costs");
+      }
+    }
+    for (int k = 0; k < 3; ++k) h->cost_view[k] = (float)f[k];
+    h->cost_view_valid = true;
+  }
   if (full && use_graph(h, s)) {
     if (!h->frame_graph && !h->graph_failed && h->direct_frames > 0) capture_frame(h, s);
     if (h->frame_graph) {

@@ -79,4 +79,29 @@ def test_cost_order_is_a_sorted_permutation_and_changes_no_pixel(cuda, pkg, orc)
     third = read_gpu(g)
     for k in ("color", "out_depth", "normal", "material"):
         assert np.array_equal(third[k].view(np.uint8), first[k].view(np.uint8)), k
+
+    # a camera turn of more than 10 degrees clears the costs as well: the
+    # costs of the previous view describe other tiles
+    import dataclasses
+
+    cam = dataclasses.replace(wl.cameras[0], azimuth=wl.cameras[0].azimuth + 0.8)
+    u2, _ = pkg.frame_uniforms_for(plan, cam, sh_degree=wl.scene.sh_degree)
+    pkg.write_frame_uniform_buffer(res, u2)
+    pkg.encode_full_compute_compositor_pipeline(None, res)
+    torch.cuda.synchronize()
+    t4 = _tiles(_u32(res.buffer("work_order")), cols)
+    assert np.array_equal(np.sort(t4), np.arange(T))
+    counts4 = _u32(res.buffer("tile_counts"))
+    heavy4 = counts4[orc.morton(t4 % cols, t4 // cols)] >= 1024
+    assert heavy4.any() and not (np.diff(heavy4.astype(np.int8)) > 0).any()
+    # a turn of a few degrees keeps them: the next frame orders by cost
+    cam = dataclasses.replace(cam, azimuth=cam.azimuth + 0.02)
+    u3, _ = pkg.frame_uniforms_for(plan, cam, sh_degree=wl.scene.sh_degree)
+    costs4 = _u32(res.buffer("tile_costs"))
+    pkg.write_frame_uniform_buffer(res, u3)
+    pkg.encode_full_compute_compositor_pipeline(None, res)
+    torch.cuda.synchronize()
+    t5 = _tiles(_u32(res.buffer("work_order")), cols)
+    b5 = cost_bucket(np.maximum(costs4[0::2], costs4[1::2])[t5])
+    assert (np.diff(b5) <= 0).all()
     res.destroy()
