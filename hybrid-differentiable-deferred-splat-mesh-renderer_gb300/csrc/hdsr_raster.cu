@@ -8,7 +8,11 @@
 // gated at weight > 0.01; a quad stops once all four T < 0.001.
 //
 // GB300 layout: a warp owns half a tile (16x8 pixels, one 2x2 quad per
-// lane), taken from an atomic counter, so that each half stops on its own. It
+// lane), taken from an atomic counter in the work order, so that each half
+// stops on its own. The work order starts the most expensive tiles first:
+// every raster records each half tile's cost, and the next frame's
+// k_work_order sorts the tiles by it (a tile's list length does not predict
+// how far its pixels go before they saturate, its last cost does). It
 // reads the tile's entries straight from its superblock's depth-ordered list
 // (no per-tile list is written on the frame path; see k_raster), culls them
 // against the half tile, gathers the kept ones from the SoA projection cache
