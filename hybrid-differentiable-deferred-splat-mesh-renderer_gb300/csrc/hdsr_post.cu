@@ -140,8 +140,8 @@ __device__ __forceinline__ void bilateral_tap(float4 c, F3 cn, float dden, float
                                               float4 s, F3& acc, float& total) {
   F3 sn = f3(s.x, s.y, s.z);
   float depthDiff = fabsf(c.w - s.w) / dden;
-  float depthW = hx_expf(-depthDiff * depthDiff / sd2);
-  float normalW = px_pow(mx(dot(cn, sn), 0.0f), ne);
+  float depthW = weight_expf(-depthDiff * depthDiff / sd2);
+  float normalW = weight_pow(mx(dot(cn, sn), 0.0f), ne);
   float w = spatialW * depthW * normalW;
   acc = add(acc, muls(sn, w));
   total = total + w;

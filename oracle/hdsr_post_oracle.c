@@ -153,6 +153,18 @@ float orp_pow(float x, float y) {
   return orc_expf(y * orc_logf(x));
 }
 
+/* The bilateral filter's weights (exponents <= 0, or a hair above): the
+ * composite's exp, 0 below -86 (a denormal weight); pow through it. The
+ * kernels' weight_expf / weight_pow, the same steps. */
+float orp_weight_expf(float x) { return x > -86.0f ? orc_composite_expf(x) : 0.0f; }
+float orp_weight_pow(float x, float y) {
+  if (x == 1.0f || y == 0.0f) return 1.0f;
+  if (!(x == x) || !(y == y)) return bf(0x7FC00000u);
+  if (x == 0.0f) return y > 0.0f ? 0.0f : bf(0x7F800000u);
+  if (x < 0.0f) return bf(0x7FC00000u);
+  return orp_weight_expf(y * orc_logf(x));
+}
+
 /* octEncode / octDecode / faceForwardNormal (gpu_screen_space_normals.wgsl:36-59) */
 static inline void oct_xy(f3 n, float* ox, float* oy) {
   float sum = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
@@ -244,8 +256,8 @@ void orp_bilateral(const orp_inputs* in, const orp_params* q, const uint32_t* ss
           float dist2 = (float)(dx * dx + dy * dy);
           float spatialW = orc_expf(-dist2 / (2.0f * ss * ss));
           float depthDiff = fabsf(cd - sd) / fmx(cd, 0.001f);
-          float depthW = orc_expf(-depthDiff * depthDiff / (2.0f * sdv * sdv));
-          float normalW = orp_pow(fmx(dot(cn, sn), 0.0f), 1.0f / fmx(q->bilateral_normal_sigma, 0.01f));
+          float depthW = orp_weight_expf(-depthDiff * depthDiff / (2.0f * sdv * sdv));
+          float normalW = orp_weight_pow(fmx(dot(cn, sn), 0.0f), 1.0f / fmx(q->bilateral_normal_sigma, 0.01f));
           float w = spatialW * depthW * normalW;
           acc = add(acc, muls(sn, w));
           total = total + w;

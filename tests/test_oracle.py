@@ -207,6 +207,17 @@ def test_composite_exp_accuracy(orc):
     assert orc.composite_expf(np.float32(0.0))[0] == np.float32(1.0) + np.float32(2.0 ** -23)
 
 
+def test_composite_exp_accuracy_over_the_weight_range(orc):
+    # the deferred bilateral filter's weights use the same exp down to -86
+    # (2^k exact for k >= -126), and 0 below
+    x = np.concatenate([np.linspace(-86.0, 0.001, 400001),
+                        -np.random.default_rng(6).uniform(0, 86, 200000)]).astype(np.float32)
+    got = orc.composite_expf(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    ulp = np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert np.max(np.abs(got - ref) / ulp) <= 3.0
+
+
 def test_log_accuracy(orc):
     x = np.concatenate([np.geomspace(1e-30, 1e30, 200001), np.linspace(0.5, 2.0, 100001),
                         np.array([1e-6, 1.0, 2.0, 0.5], np.float64)]).astype(np.float32)
