@@ -136,11 +136,14 @@ __global__ void __launch_bounds__(256) k_ss_normals(PostArgs a) {
 // ---------------------------------------------------------------------------
 // bilateral normal filter
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void bilateral_tap(float4 c, F3 cn, float dden, float sd2, float ne, float spatialW,
-                                              float4 s, F3& acc, float& total) {
+// The two divisions of a tap by per-pixel constants (the centre's depth and
+// 2 sigma^2) are multiplications by their reciprocals, taken once per pixel
+// (within the 2.5 ulp WGSL allows a division; the oracle does the same).
+__device__ __forceinline__ void bilateral_tap(float4 c, F3 cn, float inv_dden, float neg_inv_sd2, float ne,
+                                              float spatialW, float4 s, F3& acc, float& total) {
   F3 sn = f3(s.x, s.y, s.z);
-  float depthDiff = fabsf(c.w - s.w) / dden;
-  float depthW = weight_expf(-depthDiff * depthDiff / sd2);
+  float depthDiff = fabsf(c.w - s.w) * inv_dden;
+  float depthW = weight_expf((depthDiff * depthDiff) * neg_inv_sd2);
   float normalW = weight_pow(mx(dot(cn, sn), 0.0f), ne);
   float w = spatialW * depthW * normalW;
   acc = add(acc, muls(sn, w));
@@ -175,7 +178,8 @@ __global__ void __launch_bounds__(256) k_bilateral(PostArgs a) {
   F3 cn = f3(c.x, c.y, c.z);
   const float sd2 = 2.0f * a.p.bilateral_depth_sigma * a.p.bilateral_depth_sigma;
   const float ne = 1.0f / mx(a.p.bilateral_normal_sigma, 0.01f);
-  const float dden = mx(c.w, 0.001f);
+  const float inv_dden = 1.0f / mx(c.w, 0.001f);
+  const float neg_inv_sd2 = -(1.0f / sd2);
   F3 acc = f3(0.0f, 0.0f, 0.0f);
   float total = 0.0f;
 #pragma unroll 1
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(256) k_bilateral(PostArgs a) {
     const float4* row = s_nd + (threadIdx.y + R + dy) * T + threadIdx.x + R;
 #pragma unroll
     for (int dx = -R; dx <= R; ++dx)
-      bilateral_tap(c, cn, dden, sd2, ne, s_spatial[(dy + R) * (2 * R + 1) + dx + R], row[dx], acc, total);
+      bilateral_tap(c, cn, inv_dden, neg_inv_sd2, ne, s_spatial[(dy + R) * (2 * R + 1) + dx + R], row[dx], acc, total);
   }
   a.nrm[idx] = oct_word(normalize(divs(acc, mx(total, 0.0001f))));
 }

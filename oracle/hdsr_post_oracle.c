@@ -255,8 +255,12 @@ void orp_bilateral(const orp_inputs* in, const orp_params* q, const uint32_t* ss
           float sd = DEPTH(sx, sy);
           float dist2 = (float)(dx * dx + dy * dy);
           float spatialW = orc_expf(-dist2 / (2.0f * ss * ss));
-          float depthDiff = fabsf(cd - sd) / fmx(cd, 0.001f);
-          float depthW = orp_weight_expf(-depthDiff * depthDiff / (2.0f * sdv * sdv));
+          /* divisions by per-pixel constants as multiplications by their
+           * reciprocals (within WGSL's 2.5 ulp division), as the kernel */
+          float inv_dden = 1.0f / fmx(cd, 0.001f);
+          float neg_inv_sd2 = -(1.0f / (2.0f * sdv * sdv));
+          float depthDiff = fabsf(cd - sd) * inv_dden;
+          float depthW = orp_weight_expf((depthDiff * depthDiff) * neg_inv_sd2);
           float normalW = orp_weight_pow(fmx(dot(cn, sn), 0.0f), 1.0f / fmx(q->bilateral_normal_sigma, 0.01f));
           float w = spatialW * depthW * normalW;
           acc = add(acc, muls(sn, w));
