@@ -248,17 +248,20 @@ __device__ __forceinline__ F3 view_pos(const PostArgs& a, const float pi[4], flo
   return f3((u * pi[0] + pi[2]) * depth, (v * pi[1] + pi[3]) * depth, -depth);
 }
 
+// Divisions by frame constants (thickness, falloff end, viewport size) are
+// multiplications by reciprocals taken once (within the 2.5 ulp WGSL allows a
+// division; the oracle does the same); dot / dist stays a division.
 __device__ __forceinline__ void horizon_sample(const PostArgs& a, const float pi[4], float u, float v, int mip,
-                                               F3 viewPos, F3 vn, float& best) {
+                                               F3 viewPos, F3 vn, float inv_thick, float inv_falloff, float& best) {
   if (u >= 0.0f && u <= 1.0f && v >= 0.0f && v <= 1.0f) {
     float sd = sample_depth_mip(a, u, v, mip);
     F3 diff = sub(view_pos(a, pi, u, v, sd), viewPos);
     float dist = length(diff);
     if (dist > 0.001f) {
-      float zr = fabsf(diff.z) / a.p.ao_thickness;
+      float zr = fabsf(diff.z) * inv_thick;
       float tw = sat(1.0f - zr * zr);
       float hz = dot(diff, vn) / dist;
-      float fo = sat(1.0f - dist / a.p.ao_falloff_end);
+      float fo = sat(1.0f - dist * inv_falloff);
       best = mx(best, hz * fo * tw);
     }
   }
@@ -299,6 +302,8 @@ __global__ void __launch_bounds__(256) k_gtao_main(PostArgs a, float4 projInfo) 
       tm[st - 1] = to_i32(clampf(px_log2(pixelRadius * t / 4.0f), 0.0f, 2.0f));
     }
   }
+  const float inv_vw = 1.0f / a.vw, inv_vh = 1.0f / a.vh;
+  const float inv_thick = 1.0f / a.p.ao_thickness, inv_falloff = 1.0f / a.p.ao_falloff_end;
   float totalAO = 0.0f;
   F3 bent = f3(0.0f, 0.0f, 0.0f);
   for (uint32_t sl = 0; sl < S; ++sl) {
@@ -310,17 +315,17 @@ __global__ void __launch_bounds__(256) k_gtao_main(PostArgs a, float4 projInfo) 
     if (TC > 0) {
 #pragma unroll
       for (int k = 0; k < (TC > 0 ? TC : 1); ++k) {
-        float ox = dcp * tt[k] / a.vw, oy = dsp * tt[k] / a.vh;
-        horizon_sample(a, pi, u + ox, v + oy, tm[k], viewPos, vn, bestP);
-        horizon_sample(a, pi, u - ox, v - oy, tm[k], viewPos, vn, bestN);
+        float ox = dcp * tt[k] * inv_vw, oy = dsp * tt[k] * inv_vh;
+        horizon_sample(a, pi, u + ox, v + oy, tm[k], viewPos, vn, inv_thick, inv_falloff, bestP);
+        horizon_sample(a, pi, u - ox, v - oy, tm[k], viewPos, vn, inv_thick, inv_falloff, bestN);
       }
     } else {
       for (uint32_t st = 1; st <= T; ++st) {
         float t = ((float)st + soy * 0.5f) / (float)T;
-        float ox = dcp * t / a.vw, oy = dsp * t / a.vh;
+        float ox = dcp * t * inv_vw, oy = dsp * t * inv_vh;
         int mip = to_i32(clampf(px_log2(pixelRadius * t / 4.0f), 0.0f, 2.0f));
-        horizon_sample(a, pi, u + ox, v + oy, mip, viewPos, vn, bestP);
-        horizon_sample(a, pi, u - ox, v - oy, mip, viewPos, vn, bestN);
+        horizon_sample(a, pi, u + ox, v + oy, mip, viewPos, vn, inv_thick, inv_falloff, bestP);
+        horizon_sample(a, pi, u - ox, v - oy, mip, viewPos, vn, inv_thick, inv_falloff, bestN);
       }
     }
     float nds = vn.x * dc + vn.y * ds + vn.z * 0.0f;

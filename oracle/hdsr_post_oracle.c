@@ -329,15 +329,18 @@ static inline float mip_sample(const gtao_ctx* c, float u, float v, int level) {
 static inline f3 vpos(const gtao_ctx* c, float u, float v, float d) {
   return F3((u * c->pi[0] + c->pi[2]) * d, (v * c->pi[1] + c->pi[3]) * d, -d);
 }
-static inline float horizon(const gtao_ctx* c, float u, float v, int mip, f3 vp, f3 vn, float best) {
+/* divisions by frame constants as multiplications by reciprocals taken
+ * once, as the kernel (within WGSL's 2.5 ulp division); dot / dist stays */
+static inline float horizon(const gtao_ctx* c, float u, float v, int mip, f3 vp, f3 vn, float inv_thick,
+                            float inv_falloff, float best) {
   if (u >= 0.0f && u <= 1.0f && v >= 0.0f && v <= 1.0f) {
     f3 diff = sub(vpos(c, u, v, mip_sample(c, u, v, mip)), vp);
     float dist = len(diff);
     if (dist > 0.001f) {
-      float zr = fabsf(diff.z) / c->q->ao_thickness;
+      float zr = fabsf(diff.z) * inv_thick;
       float tw = sat(1.0f - zr * zr);
       float hz = dot(diff, vn) / dist;
-      float fo = sat(1.0f - dist / c->q->ao_falloff_end);
+      float fo = sat(1.0f - dist * inv_falloff);
       best = fmx(best, hz * fo * tw);
     }
   }
@@ -376,6 +379,8 @@ void orp_gtao_main(const orp_inputs* in, const orp_params* q, const float* mip0,
       float sox = (float)ridx * a1 + 0.5f, soy = (float)ridx * a2 + 0.5f;
       sox = sox - floorf(sox);
       soy = soy - floorf(soy);
+      const float inv_vw = 1.0f / vw, inv_vh = 1.0f / vh;
+      const float inv_thick = 1.0f / q->ao_thickness, inv_falloff = 1.0f / q->ao_falloff_end;
       float total = 0.0f;
       f3 bent = F3(0.0f, 0.0f, 0.0f);
       for (uint32_t sl = 0; sl < q->ao_slices; ++sl) {
@@ -385,10 +390,10 @@ void orp_gtao_main(const orp_inputs* in, const orp_params* q, const float* mip0,
         float bp = -1.0f, bn = -1.0f;
         for (uint32_t st = 1; st <= q->ao_steps; ++st) {
           float t = ((float)st + soy * 0.5f) / (float)q->ao_steps;
-          float ox = dc * pr * t / vw, oy = ds * pr * t / vh;
+          float ox = dc * pr * t * inv_vw, oy = ds * pr * t * inv_vh;
           int mip = i32_of(clampf(orp_log2(pr * t / 4.0f), 0.0f, 2.0f));
-          bp = horizon(&c, u + ox, v + oy, mip, vp, vn, bp);
-          bn = horizon(&c, u - ox, v - oy, mip, vp, vn, bn);
+          bp = horizon(&c, u + ox, v + oy, mip, vp, vn, inv_thick, inv_falloff, bp);
+          bn = horizon(&c, u - ox, v - oy, mip, vp, vn, inv_thick, inv_falloff, bn);
         }
         float nds = vn.x * dc + vn.y * ds + vn.z * 0.0f;
         float cp = fmx(bp, nds * 0.08f), cn = fmx(bn, -nds * 0.08f);

@@ -486,9 +486,11 @@ def _np_oct_word(n, orc):
 
 
 def test_bilateral_filter_matches_an_independent_numpy_restatement(pkg, orc):
-    # bilateral_normal_filter.wgsl:39-86 with numpy f32 steps, the oracle's
-    # exp and log (pow = exp(y log x) with its special cases), clamped taps;
-    # bit for bit against the oracle
+    # bilateral_normal_filter.wgsl:39-86 with numpy f32 steps, clamped taps;
+    # the oracle's exp for the spatial weights, the composite's exp (0 below
+    # -86) for the depth and normal weights (pow = exp(y log x) with its
+    # special cases), the divisions by the centre's depth and 2 sigma^2 as
+    # multiplications by reciprocals; bit for bit against the oracle
     D = pkg.deferred
     f32 = np.float32
     rng = np.random.default_rng(12)
@@ -507,6 +509,11 @@ def test_bilateral_filter_matches_an_independent_numpy_restatement(pkg, orc):
     R, ss, sdv = int(q.bilateral_radius), f32(q.bilateral_spatial_sigma), f32(q.bilateral_depth_sigma)
     ne = f32(1.0) / np.maximum(f32(q.bilateral_normal_sigma), f32(0.01))
     cn = _np_oct_decode(ssn, orc)
+
+    def weight_exp(a):
+        a = np.asarray(a, np.float32)
+        return np.where(a > f32(-86.0), orc.composite_expf(a.reshape(-1)).reshape(a.shape), f32(0.0))
+
     acc = [np.zeros((H, W), np.float32) for _ in range(3)]
     total = np.zeros((H, W), np.float32)
     with np.errstate(divide="ignore", invalid="ignore"):
@@ -517,10 +524,12 @@ def test_bilateral_filter_matches_an_independent_numpy_restatement(pkg, orc):
                 sd = depth[sy, sx]
                 dist2 = f32(dx * dx + dy * dy)
                 spatial = orc.expf(np.full((H, W), -dist2 / ((f32(2.0) * ss) * ss), np.float32)).reshape(H, W)
-                dd = np.abs(depth - sd) / np.maximum(depth, f32(0.001))
-                dw = orc.expf(((-dd) * dd) / ((f32(2.0) * sdv) * sdv)).reshape(H, W)
+                inv_dden = f32(1.0) / np.maximum(depth, f32(0.001))
+                neg_inv_sd2 = -(f32(1.0) / ((f32(2.0) * sdv) * sdv))
+                dd = np.abs(depth - sd) * inv_dden
+                dw = weight_exp((dd * dd) * neg_inv_sd2)
                 x = np.maximum((cn[0] * sn[0] + cn[1] * sn[1]) + cn[2] * sn[2], f32(0.0))
-                pw = orc.expf(ne * orc.logf(np.maximum(x, f32(1e-30)).reshape(-1)).reshape(H, W)).reshape(H, W)
+                pw = weight_exp(ne * orc.logf(np.maximum(x, f32(1e-30)).reshape(-1)).reshape(H, W))
                 pw = np.where(x == f32(1.0), f32(1.0), np.where(x == f32(0.0), f32(0.0), pw))
                 w = (spatial * dw) * pw
                 acc = [(acc[i] + sn[i] * w).astype(np.float32) for i in range(3)]
@@ -659,10 +668,10 @@ def test_gtao_main_matches_an_independent_numpy_restatement(pkg, orc, frame_coun
         sp = vpos(su, sv, sd)
         diff = tuple(sp[k] - vp[k] for k in range(3))
         dist = np.sqrt(dot3(diff, diff))
-        zr = np.abs(diff[2]) / thick
+        zr = np.abs(diff[2]) * (f32(1.0) / thick)
         tw = sat(f32(1.0) - zr * zr)
         hz = dot3(diff, vn) / dist
-        fo = sat(f32(1.0) - dist / fall)
+        fo = sat(f32(1.0) - dist * (f32(1.0) / fall))
         cand = np.maximum(best, (hz * fo) * tw)
         return np.where(ok & (dist > f32(0.001)), cand, best)
 
@@ -675,8 +684,8 @@ def test_gtao_main_matches_an_independent_numpy_restatement(pkg, orc, frame_coun
             bn = np.full((H, W), f32(-1.0))
             for st in range(1, T + 1):
                 t = (f32(st) + soy * f32(0.5)) / f32(T)
-                ox = dc * pr * t / res_x
-                oy = ds * pr * t / res_y
+                ox = dc * pr * t * (f32(1.0) / res_x)
+                oy = ds * pr * t * (f32(1.0) / res_y)
                 lg = orc.logf((pr * t / f32(4.0)).reshape(-1)).reshape(H, W) * f32(1.44269502162933349609)
                 mip = np.trunc(np.clip(lg, f32(0.0), f32(2.0))).astype(np.int64)
                 bp = horizon(u + ox, v + oy, mip, bp)
