@@ -480,11 +480,11 @@ __device__ __forceinline__ float curve(const PostArgs& a, int lut, float x) {
 }
 
 __device__ __forceinline__ F3 srgb_to_linear(F3 c) {
-  return f3(px_pow(mx(c.x, 0.0f), 2.2f), px_pow(mx(c.y, 0.0f), 2.2f), px_pow(mx(c.z, 0.0f), 2.2f));
+  return f3(weight_pow(mx(c.x, 0.0f), 2.2f), weight_pow(mx(c.y, 0.0f), 2.2f), weight_pow(mx(c.z, 0.0f), 2.2f));
 }
 __device__ __forceinline__ F3 linear_to_srgb(F3 c) {
   const float e = 0.454545468091964721680f;   // f32(1 / 2.2)
-  return f3(px_pow(mx(c.x, 0.0f), e), px_pow(mx(c.y, 0.0f), e), px_pow(mx(c.z, 0.0f), e));
+  return f3(weight_pow(mx(c.x, 0.0f), e), weight_pow(mx(c.y, 0.0f), e), weight_pow(mx(c.z, 0.0f), e));
 }
 __device__ __forceinline__ F3 tonemap(F3 c, float exposure) {
   F3 e = muls(c, exposure);
@@ -497,6 +497,14 @@ __device__ __forceinline__ float geom_direct(float ndv, float r) {
 }
 
 __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
+  // the environment's rotation (sin, cos) and its top mip level are the same
+  // for every pixel: computed once per block (same functions, same bits)
+  __shared__ float s_env[3];
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    px_sincos(a.p.env_rotation, &s_env[0], &s_env[1]);
+    s_env[2] = px_log2((float)a.env_w);
+  }
+  __syncthreads();
   int x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
   if (x >= a.W || y >= a.H) return;
   uint64_t idx = (uint64_t)y * a.W + x;
@@ -514,8 +522,7 @@ __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
       mat4_mul(a.p.view_proj_inverse, nx, ny, 1.0f, 1.0f, wf);
       F3 vd = normalize(sub(f3(wf[0] / wf[3], wf[1] / wf[3], wf[2] / wf[3]),
                             f3(wn[0] / wn[3], wn[1] / wn[3], wn[2] / wn[3])));
-      float rs, rc;
-      px_sincos(a.p.env_rotation, &rs, &rc);
+      const float rs = s_env[0], rc = s_env[1];
       float4 e = sample_env(a, rs, rc, vd, 0.0f);
       F3 m = linear_to_srgb(tonemap(f3(e.x, e.y, e.z), a.p.exposure));
       *out = pack_h4(m.x, m.y, m.z, 0.0f);
@@ -551,7 +558,7 @@ __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
   float dd = NdotH * NdotH * (ra2 - 1.0f) + 1.0f;
   float D = ra2 / (kPI * dd * dd);
   float G = geom_direct(NdotV, roughness) * geom_direct(NdotL, roughness);
-  float fp = px_pow(sat(1.0f - HdotV), 5.0f);
+  float fp = weight_pow(sat(1.0f - HdotV), 5.0f);
   F3 F = f3(F0.x + (1.0f - F0.x) * fp, F0.y + (1.0f - F0.y) * fp, F0.z + (1.0f - F0.z) * fp);
   float den = 4.0f * NdotV * NdotL + 0.0001f;
   F3 spec = f3(D * G * F.x / den, D * G * F.y / den, D * G * F.z / den);
@@ -580,10 +587,9 @@ __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
     if (hasEnv) {
       F3 bentN = oct_dec(aoS.y, aoS.z);
       F3 diffDir = normalize(mix3(N, bentN, 0.5f));
-      float maxLod = px_log2((float)a.env_w);
+      const float maxLod = s_env[2];
       float diffLod = mx(maxLod - 2.0f, 3.0f);
-      float rs, rc;
-      px_sincos(a.p.env_rotation, &rs, &rc);
+      const float rs = s_env[0], rc = s_env[1];
       float4 irr = sample_env(a, rs, rc, diffDir, diffLod);
       F3 diffIBL = f3(kD.x * albedo.x * irr.x, kD.y * albedo.y * irr.y, kD.z * albedo.z * irr.z);
       F3 I = neg(V);
@@ -595,7 +601,7 @@ __global__ void __launch_bounds__(256) k_lighting(PostArgs a) {
       uint32_t bw = a.brdf[byi * kBrdfSize + bxi];
       float bA = lo16(bw), bB = hi16(bw);
       float om = 1.0f - roughness;
-      float fr = px_pow(sat(1.0f - NdotV), 5.0f);
+      float fr = weight_pow(sat(1.0f - NdotV), 5.0f);
       F3 Fi = f3(F0.x + (mx(om, F0.x) - F0.x) * fr, F0.y + (mx(om, F0.y) - F0.y) * fr,
                  F0.z + (mx(om, F0.z) - F0.z) * fr);
       float graze = smoothstepf(0.0f, 0.02f, NdotV);

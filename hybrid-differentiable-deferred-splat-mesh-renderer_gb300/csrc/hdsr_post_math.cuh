@@ -117,11 +117,11 @@ HDSR_HD float px_asin(float x) { return px_atan2(x, sqrtf((1.0f - x) * (1.0f + x
 
 HDSR_HD float px_log2(float x) { return hx_logf(x) * 1.44269502162933349609f; }
 
-// Weights of the bilateral filter, whose exponents are <= 0 (or a hair
-// above, for a rounded dot product of two unit normals): exp as the
-// composite's (fma-rounded k, Cody-Waite, degree-5 fit; the 2^k scale is
-// exact for the k >= -126 that x > -86 gives), 0 below -86, where the weight
-// would be denormal: far below what the filter's f32 sums resolve.
+// exp and pow where the exponent stays below a few units (the bilateral
+// filter's weights; the lighting's sRGB transfer of values in [0, ~1] and
+// Schlick's (1 - cos)^5): exp as the composite's (fma-rounded k, Cody-Waite,
+// degree-5 fit; the 2^k scale is exact for the k >= -126 that x > -86
+// gives), 0 below -86, where the value would be denormal.
 HDSR_HD float weight_expf(float x) { return x > -86.0f ? composite_expf(x) : 0.0f; }
 HDSR_HD float weight_pow(float x, float y) {
   if (x == 1.0f || y == 0.0f) return 1.0f;

@@ -387,7 +387,7 @@ def _post_lib():
         for nm in ("orp_asin", "orp_sin", "orp_cos", "orp_log2"):
             getattr(L, nm).argtypes = [c_float]
             getattr(L, nm).restype = c_float
-        for nm in ("orp_atan2", "orp_pow"):
+        for nm in ("orp_atan2", "orp_pow", "orp_weight_pow"):
             getattr(L, nm).argtypes = [c_float, c_float]
             getattr(L, nm).restype = c_float
         _post_ready = True

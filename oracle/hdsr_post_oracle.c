@@ -153,8 +153,9 @@ float orp_pow(float x, float y) {
   return orc_expf(y * orc_logf(x));
 }
 
-/* The bilateral filter's weights (exponents <= 0, or a hair above): the
- * composite's exp, 0 below -86 (a denormal weight); pow through it. The
+/* exp and pow where the exponent stays below a few units (the bilateral
+ * filter's weights, the lighting's sRGB transfer and Schlick's (1 - cos)^5):
+ * the composite's exp, 0 below -86 (a denormal value); pow through it. The
  * kernels' weight_expf / weight_pow, the same steps. */
 float orp_weight_expf(float x) { return x > -86.0f ? orc_composite_expf(x) : 0.0f; }
 float orp_weight_pow(float x, float y) {
@@ -521,11 +522,11 @@ static inline float lut(const uint16_t* curves, int which, float x) {
   return orc_f16_to_f32(curves[which * 256 + clampi(i32_of(x * 255.0f), 0, 255)]);
 }
 static inline f3 to_lin(f3 c) {
-  return F3(orp_pow(fmx(c.x, 0.0f), 2.2f), orp_pow(fmx(c.y, 0.0f), 2.2f), orp_pow(fmx(c.z, 0.0f), 2.2f));
+  return F3(orp_weight_pow(fmx(c.x, 0.0f), 2.2f), orp_weight_pow(fmx(c.y, 0.0f), 2.2f), orp_weight_pow(fmx(c.z, 0.0f), 2.2f));
 }
 static inline f3 to_srgb(f3 c) {
   const float e = 0.454545468091964721680f;
-  return F3(orp_pow(fmx(c.x, 0.0f), e), orp_pow(fmx(c.y, 0.0f), e), orp_pow(fmx(c.z, 0.0f), e));
+  return F3(orp_weight_pow(fmx(c.x, 0.0f), e), orp_weight_pow(fmx(c.y, 0.0f), e), orp_weight_pow(fmx(c.z, 0.0f), e));
 }
 static inline f3 reinhard(f3 c, float exposure) {
   f3 e = muls(c, exposure);
@@ -586,7 +587,7 @@ void orp_lighting(const orp_inputs* in, const orp_params* q, const uint32_t* nrm
       float dd = NdotH * NdotH * (ra2 - 1.0f) + 1.0f;
       float D = ra2 / (PI_F * dd * dd);
       float G = g_direct(NdotV, rough) * g_direct(NdotL, rough);
-      float fp = orp_pow(sat(1.0f - HdotV), 5.0f);
+      float fp = orp_weight_pow(sat(1.0f - HdotV), 5.0f);
       f3 F = F3(F0.x + (1.0f - F0.x) * fp, F0.y + (1.0f - F0.y) * fp, F0.z + (1.0f - F0.z) * fp);
       float den = 4.0f * NdotV * NdotL + 0.0001f;
       f3 spec = F3(D * G * F.x / den, D * G * F.y / den, D * G * F.z / den);
@@ -621,7 +622,7 @@ void orp_lighting(const orp_inputs* in, const orp_params* q, const uint32_t* nrm
           int bxi = i32_of(clampf(NdotV * 255.0f, 0.0f, 255.0f)), byi = i32_of(clampf(rough * 255.0f, 0.0f, 255.0f));
           uint32_t bw = brdf[byi * 256 + bxi];
           float bA = lo(bw), bB = hi(bw);
-          float om = 1.0f - rough, fr = orp_pow(sat(1.0f - NdotV), 5.0f);
+          float om = 1.0f - rough, fr = orp_weight_pow(sat(1.0f - NdotV), 5.0f);
           f3 Fi = F3(F0.x + (fmx(om, F0.x) - F0.x) * fr, F0.y + (fmx(om, F0.y) - F0.y) * fr,
                      F0.z + (fmx(om, F0.z) - F0.z) * fr);
           float gz = smoothstep_(0.0f, 0.02f, NdotV);
