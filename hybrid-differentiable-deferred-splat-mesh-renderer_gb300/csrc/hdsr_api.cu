@@ -461,6 +461,17 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   if (a.log_keys && (e = launch_depth_range(a, ts)) != cudaSuccess) return cuda_fail(h, e, "depth_range");
   mark(h, s, 3);
   if ((e = launch_scan_tiles(a, ts)) != cudaSuccess) return cuda_fail(h, e, "scan_tiles");
+  if (a.tile_count) {
+    // the raster's work order from the last frame's tile costs, on the side
+    // stream after the tile scan's own order (off the frame's critical
+    // path); a new scene's first frame starts from none (the scan's order)
+    if (h->cost_stale) {
+      e = cudaMemsetAsync(a.tile_cost, 0, 2ull * a.tile_count * sizeof(uint32_t), ts);
+      if (e != cudaSuccess) return cuda_fail(h, e, "reset tile costs");
+      h->cost_stale = false;
+    }
+    if ((e = launch_work_order(a, ts)) != cudaSuccess) return cuda_fail(h, e, "work_order");
+  }
   mark(h, s, 5);
   if (fork && (e = cudaEventRecord(h->join_ev, ts)) != cudaSuccess) return cuda_fail(h, e, "fork");
   // splats: as many 9-bit passes as the frame's depth range needs -> order
@@ -504,7 +515,7 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
     h->launches += 2;
   }
   h->launches += 1 + n_splat_launch + (n_splat_launch + 1) + 1 + 9 * n_splat_launch + 1 +
-                 3 * (a.sb_bits > kRadixWideBits ? 2 : 1) + (a.tile_count ? 1 : 0);
+                 3 * (a.sb_bits > kRadixWideBits ? 2 : 1) + (a.tile_count ? 2 : 0);
   return HDSR_OK;
 }
 
@@ -516,17 +527,6 @@ static hdsr_status encode_raster(hdsr_compositor* h, cudaStream_t s, bool full) 
     // is the one control word it must start from zero
     e = cudaMemsetAsync(a.ctl + kCtlRasterTile, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return cuda_fail(h, e, "reset raster counter");
-  }
-  if (full && a.tile_count) {
-    // the work order follows the last raster's tile costs; a new scene's
-    // first frame starts from none (the tile scan's order)
-    if (h->cost_stale) {
-      e = cudaMemsetAsync(a.tile_cost, 0, 2ull * a.tile_count * sizeof(uint32_t), s);
-      if (e != cudaSuccess) return cuda_fail(h, e, "reset tile costs");
-      h->cost_stale = false;
-    }
-    if ((e = launch_work_order(a, s)) != cudaSuccess) return cuda_fail(h, e, "work_order");
-    h->launches += 1;
   }
   if ((e = launch_raster(a, s)) != cudaSuccess) return cuda_fail(h, e, "raster");
   mark(h, s, 17);

@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
 // only which warp takes a tile when; the images do not depend on it. With no
 // costs recorded (a new scene's first frame) the tile scan's order stays.
 constexpr int kOrderThreads = 1024;
-constexpr int kOrderBuckets = 128;
+constexpr int kOrderBuckets = 128;  // 4 per lane of one warp in the bucket scan
 constexpr int kOrderUnroll = 8;
 
 // a tile's cost: the larger of its halves' (0 past the grid)
@@ -347,13 +347,27 @@ __global__ void __launch_bounds__(kOrderThreads) k_work_order(FrameArgs a) {
   }
   __syncthreads();
   if (!any) return;
-  if (threadIdx.x == 0) {
-    // most expensive bucket first: each bucket's first position
-    uint32_t run = 0;
-    for (int b = kOrderBuckets - 1; b >= 0; --b) {
-      const uint32_t n = hist[b];
-      hist[b] = run;
-      run += n;
+  if (threadIdx.x < 32u) {
+    // most expensive bucket first: each bucket's first position (a warp
+    // scan over the buckets in descending order, 4 per lane)
+    constexpr int kPer = kOrderBuckets / 32;
+    uint32_t v[kPer], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      v[k] = hist[kOrderBuckets - 1 - (int)(lane * kPer) - k];
+      sum += v[k];
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += t;
+    }
+    uint32_t run = inc - sum;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      hist[kOrderBuckets - 1 - (int)(lane * kPer) - k] = run;
+      run += v[k];
     }
   }
   __syncthreads();
