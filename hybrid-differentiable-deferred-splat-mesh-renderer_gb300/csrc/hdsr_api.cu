@@ -59,9 +59,10 @@ struct hdsr_compositor {
   uint32_t next_u = 0;
   float device_u[64] = {};
   bool device_u_valid = false;
-  // second stream of a frame: tile counts and the tile scan run there,
-  // forked after projection and joined before the superblock lists, beside
-  // the depth sort (none when profiling: per-pass times need one stream)
+  // second stream of a frame: tile counts, the tile scan and the work order
+  // run there, forked after projection and joined before the rasteriser,
+  // beside the depth sort and the superblock lists (none when profiling:
+  // per-pass times need one stream)
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   uint32_t ev_used = 0;
@@ -450,8 +451,10 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   mark(h, s, 1);
   if ((e = launch_project(a, s)) != cudaSuccess) return cuda_fail(h, e, "project");
   mark(h, s, 2);
-  // tile counts and the tile scan: beside the depth sort on the side stream
-  // (they share no buffer with it), or in line when profiling
+  // tile counts, the tile scan and the work order: on the side stream beside
+  // the depth sort and the superblock lists (they share no buffer with them;
+  // the main stream's kernels read the overflow flag the tile scan may set
+  // once per block), or in line when profiling
   const bool fork = !h->profiling && h->side;
   cudaStream_t ts = fork ? h->side : s;
   if (fork && ((e = cudaEventRecord(h->fork_ev, s)) != cudaSuccess ||
@@ -484,8 +487,6 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   dj.bin_base = a.bin_base;
   dj.tiles_cap = a.radix_tiles_cap;
   dj.low_mask = 0xFFFFFFFFull;
-  // the superblock lists need the tile scan's totals and overflow flag
-  if (fork && (e = cudaStreamWaitEvent(s, h->join_ev, 0)) != cudaSuccess) return cuda_fail(h, e, "join");
   // superblock lists in depth order, sorted by superblock (stable)
   if ((e = launch_scan_sb(a, s)) != cudaSuccess) return cuda_fail(h, e, "scan_superblocks");
   RadixJob sj = dj;
@@ -505,6 +506,9 @@ static hdsr_status encode_pre_raster(hdsr_compositor* h, cudaStream_t s) {
   mark(h, s, 7);
   if ((e = launch_chunk_masks(a, s)) != cudaSuccess) return cuda_fail(h, e, "chunk_masks");
   mark(h, s, 9);
+  // the rasteriser needs the superblock starts and the work order, the
+  // per-tile lists the tile offsets, and all of them the final overflow flag
+  if (fork && (e = cudaStreamWaitEvent(s, h->join_ev, 0)) != cudaSuccess) return cuda_fail(h, e, "join");
   if (entries_each_frame(h)) {
     if ((e = launch_tile_entries(a, s)) != cudaSuccess) return cuda_fail(h, e, "tile_entries");
     mark(h, s, 8);

@@ -54,16 +54,6 @@ __device__ __forceinline__ uint32_t lane_lt() {
   return m;
 }
 
-// Does the frame skip its remaining kernels? Read once per block and shared,
-// so that every thread of the block takes the same branch even when another
-// stream's kernel (the tile scan runs beside the depth sort) sets a flag
-// meanwhile.
-__device__ __forceinline__ bool dsort_skipped(const FrameArgs& a, uint32_t* s_flag) {
-  if (threadIdx.x == 0) *s_flag = *reinterpret_cast<volatile const uint32_t*>(a.ctl + kCtlFlags) & kSkipFlags;
-  __syncthreads();
-  return *s_flag != 0u;
-}
-
 __device__ __forceinline__ uint32_t dsort_t(unsigned long long key, uint32_t base) {
   const uint32_t bits = (uint32_t)(key >> 32);
   return bits == kSentinel ? bits : bits - base;
@@ -75,7 +65,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_dsort_upsweep0(FrameArgs a) {
   __shared__ uint32_t s_flag;
   pdl_wait();
   pdl_trigger();
-  if (dsort_skipped(a, &s_flag)) return;
+  if (block_skipped(a.ctl + kCtlFlags, &s_flag)) return;
   const uint32_t N = a.N, tiles = (N + kRadixTile - 1u) / kRadixTile;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   uint32_t lo = kSentinel, hi = 0u;
@@ -123,7 +113,7 @@ __global__ void __launch_bounds__(256) k_dsort_colscan(FrameArgs a, uint32_t p) 
   __shared__ uint32_t s_flag;
   pdl_wait();
   pdl_trigger();
-  if (dsort_skipped(a, &s_flag)) return;
+  if (block_skipped(a.ctl + kCtlFlags, &s_flag)) return;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
   if (p == 0u) {
     if (blockIdx.x == 0 && tid == 0) {
@@ -219,7 +209,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_dsort_downsweep(FrameArgs 
   __shared__ uint32_t s_flag;
   pdl_wait();
   pdl_trigger();
-  if (dsort_skipped(a, &s_flag)) return;
+  if (block_skipped(a.ctl + kCtlFlags, &s_flag)) return;
   const uint32_t L = a.ctl[kCtlDepthPasses];
   if (p >= L) return;
   const bool last = p + 1u == L;

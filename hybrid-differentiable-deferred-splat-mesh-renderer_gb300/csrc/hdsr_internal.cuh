@@ -326,6 +326,18 @@ constexpr uint32_t kNoWithheldTile = 0xFFFFFFFFu;
 // and its offsets are not trustworthy).
 constexpr uint32_t kSkipFlags = 0x3u;
 
+// Does the frame skip its remaining kernels (a kSkipFlags bit in *flags)?
+// Read once per block and shared, so that every thread of the block takes the
+// same branch even when a kernel of the other stream (tile counts and the
+// tile scan run beside the depth sort and the superblock lists) sets a flag
+// meanwhile. A flag one kernel has seen, every later kernel of its stream
+// sees, so a kernel that runs reads only what earlier kernels wrote in full.
+__device__ __forceinline__ bool block_skipped(const uint32_t* flags, uint32_t* s_flag) {
+  if (threadIdx.x == 0) *s_flag = *reinterpret_cast<volatile const uint32_t*>(flags) & kSkipFlags;
+  __syncthreads();
+  return *s_flag != 0u;
+}
+
 // Lookback status word: epoch (30 bits) | flag (2 bits) | value (32 bits).
 constexpr unsigned long long kFlagAgg = 1ull;
 constexpr unsigned long long kFlagInc = 2ull;

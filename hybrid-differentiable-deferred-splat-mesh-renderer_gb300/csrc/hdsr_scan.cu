@@ -84,8 +84,9 @@ __device__ __forceinline__ void emit_superblock_entries(const FrameArgs& a, uint
 // Scan of the superblock counts in depth order (read from bits 24-31 of the
 // depth-order words), emitting every splat's list entries at its offset.
 struct SbScan {
-  // an overflowed frame skipped the depth sort: order holds no permutation
-  static __device__ bool skip(const FrameArgs& a) { return (a.ctl[kCtlFlags] & kSkipFlags) != 0u; }
+  // an overflowed frame may have skipped the depth sort: order then holds no
+  // permutation
+  static constexpr bool kMaySkip = true;
   static __device__ uint32_t size(const FrameArgs& a) { return a.N; }
   static __device__ uint32_t counter() { return kCtlScanNTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_n; }
@@ -102,11 +103,16 @@ struct SbScan {
     a.sb_off[i] = excl;
     emit_superblock_entries(a, p.r, p.box, excl);
   }
-  static __device__ void finish(const FrameArgs& a, uint32_t total) { a.ctl[kCtlSbPairs] = total; }
+  // the lists' own capacity check (tile counts, on the other stream, make the
+  // same one): the radix pass reads no entry past the buffers
+  static __device__ void finish(const FrameArgs& a, uint32_t total) {
+    if (total > a.sb_cap) atomicOr(a.ctl + kCtlFlags, 0x1u);
+    a.ctl[kCtlSbPairs] = total < a.sb_cap ? total : (uint32_t)a.sb_cap;
+  }
 };
 
 struct TileScan {
-  static __device__ bool skip(const FrameArgs&) { return false; }  // it decides the overflow
+  static constexpr bool kMaySkip = false;  // it decides the overflow
   static __device__ uint32_t size(const FrameArgs& a) { return a.M; }
   static __device__ uint32_t counter() { return kCtlScanMTile; }
   static __device__ unsigned long long* status(const FrameArgs& a) { return a.scan_status_m; }
@@ -156,7 +162,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(FrameArgs a) {
   __shared__ uint32_t s_warp[kScanThreads / 32];
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_prefix;
-  if (Policy::skip(a)) return;
+  __shared__ uint32_t s_skip;
+  // the superblock scan is a programmatic dependent launch after the depth
+  // sort (a no-op for the tile scan's plain launch)
+  pdl_wait();
+  pdl_trigger();
+  if (Policy::kMaySkip && block_skipped(a.ctl + kCtlFlags, &s_skip)) return;
   const uint32_t n = Policy::size(a);
   const uint32_t num_tiles = (n + kScanTile - 1) / kScanTile;
   const uint32_t epoch = a.ctl[kCtlEpoch];
@@ -253,8 +264,8 @@ int scan_grid(const FrameArgs& a, uint32_t n) {
 }  // namespace
 
 cudaError_t launch_scan_sb(const FrameArgs& a, cudaStream_t s) {
-  k_scan<SbScan><<<scan_grid(a, a.N), kScanThreads, 0, s>>>(a);
-  return cudaGetLastError();
+  const cudaError_t e = launch_pdl(k_scan<SbScan>, dim3(scan_grid(a, a.N)), dim3(kScanThreads), 0, s, a);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_scan_tiles(const FrameArgs& a, cudaStream_t s) {

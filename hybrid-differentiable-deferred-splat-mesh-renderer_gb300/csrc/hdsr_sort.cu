@@ -39,16 +39,15 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-__device__ __forceinline__ bool skipped(const RadixJob& j) { return (*j.flags & kSkipFlags) != 0u; }
-
 // Upsweep: per block-tile digit counts, bin-major (tile_digits[bin*cap+tile]).
 // BINS: the widest digit the instantiation handles (256 or 512 bins).
 template <uint32_t BINS>
 __global__ void __launch_bounds__(kRadixThreads) k_radix_upsweep(RadixJob j) {
   __shared__ uint32_t s_hist[BINS];
+  __shared__ uint32_t s_skip;
   pdl_wait();
   pdl_trigger();
-  if (skipped(j)) return;
+  if (block_skipped(j.flags, &s_skip)) return;
   const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
   const uint32_t dmask = (1u << j.bits) - 1u;
@@ -79,9 +78,10 @@ __global__ void __launch_bounds__(256) k_radix_colscan(RadixJob j) {
   constexpr uint32_t IT = 16;
   __shared__ uint32_t s_w[8];
   __shared__ uint32_t s_carry;
+  __shared__ uint32_t s_skip;
   pdl_wait();
   pdl_trigger();
-  if (skipped(j)) return;
+  if (block_skipped(j.flags, &s_skip)) return;
   const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
   const uint32_t bin = blockIdx.x, tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
@@ -155,9 +155,10 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_downsweep(RadixJob j
   static_assert(DPT * kRadixThreads == BINS, "digits split evenly over the threads");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SweepSmem<BINS>& S = *reinterpret_cast<SweepSmem<BINS>*>(smem_raw);
+  __shared__ uint32_t s_skip;
   pdl_wait();
   pdl_trigger();
-  if (skipped(j)) return;
+  if (block_skipped(j.flags, &s_skip)) return;
   const uint32_t P = *j.count;
   const uint32_t num_tiles = (P + kRadixTile - 1) / kRadixTile;
   const uint32_t shift = j.shift;
@@ -527,7 +528,9 @@ cudaError_t launch_radix_pass(const RadixJob& j, bool last, int num_sms, cudaStr
 // the union over both: a reader then visits a chunk that may hold none of its
 // tile's entries, which costs time only.
 __global__ void __launch_bounds__(256) k_chunk_masks(FrameArgs a) {
-  if (a.ctl[kCtlFlags] & kSkipFlags) return;
+  __shared__ uint32_t s_skip;
+  pdl_wait();  // a programmatic dependent launch after the superblock pass
+  if (block_skipped(a.ctl + kCtlFlags, &s_skip)) return;
   const uint32_t Q = a.ctl[kCtlSbPairs];
   const uint32_t chunks = (Q + kChunkEntries - 1u) / kChunkEntries;
   const uint32_t lane = threadIdx.x & 31u;
@@ -543,8 +546,8 @@ __global__ void __launch_bounds__(256) k_chunk_masks(FrameArgs a) {
 
 cudaError_t launch_chunk_masks(const FrameArgs& a, cudaStream_t s) {
   if (!a.tile_count) return cudaSuccess;
-  k_chunk_masks<<<a.num_sms * 8, 256, 0, s>>>(a);
-  return cudaGetLastError();
+  const cudaError_t e = launch_pdl(k_chunk_masks, dim3(a.num_sms * 8), dim3(256), 0, s, a);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_tile_entries(const FrameArgs& a, cudaStream_t s) {
