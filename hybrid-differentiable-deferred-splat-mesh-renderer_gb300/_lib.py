@@ -57,6 +57,8 @@ BUFFER_IDS = {
     "backward_params": 11,
     "work_order": 12,
     "tile_costs": 13,
+    "superblock_lists": 14,
+    "chunk_masks": 15,
 }
 
 

@@ -115,7 +115,7 @@ class TileSplatCompositorResources:
         import torch
 
         ptr, size = self.buffer_address(name)
-        dtype = dtype or (torch.int64 if name == "sorted_keys" else torch.int32)
+        dtype = dtype or (torch.int64 if name in ("sorted_keys", "superblock_lists", "chunk_masks") else torch.int32)
         itemsize = torch.empty((), dtype=dtype).element_size()
         n = size // itemsize if count is None else count
         return _DeviceView(ptr, n, dtype).tensor()

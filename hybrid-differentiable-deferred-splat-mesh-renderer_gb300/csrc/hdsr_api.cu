@@ -780,6 +780,9 @@ hdsr_status hdsr_get_buffer(hdsr_compositor* h, hdsr_buffer_id id, void** ptr, u
       *ptr = h->bwd_par; *bytes = N * 48; break;
     case HDSR_BUF_WORK_ORDER: *ptr = a.tile_order; *bytes = (uint64_t)a.tile_count * 4; break;
     case HDSR_BUF_TILE_COSTS: *ptr = a.tile_cost; *bytes = (uint64_t)a.tile_count * 8; break;
+    case HDSR_BUF_SUPERBLOCK_LISTS:
+      *ptr = const_cast<unsigned long long*>(a.sbk_sorted); *bytes = a.sb_cap * 8; break;
+    case HDSR_BUF_CHUNK_MASKS: *ptr = a.chunk_mask; *bytes = (a.sb_cap / kChunkEntries + 1u) * 8; break;
     default: return fail(h, HDSR_ERR_INVALID_ARG, "unknown buffer id");
   }
   return HDSR_OK;

@@ -9,9 +9,10 @@
 // depth — also the cascade's order when a bucket keeps (depth, sortRank)
 // order. So the frame's sort is one stable LSD radix over the composite key
 // (Morton tile, depth bits, sortRank), done in two stages:
-//   1. the depth digits on the N splats (depth is per splat): 4 passes of 8
-//      bits over u64 keys depth << 32 | sortRank; the pairs are then emitted
-//      in that depth order (hdsr_scan.cu);
+//   1. the depth digits on the N splats (depth is per splat): as many 9-bit
+//      passes over u64 keys depth << 32 | sortRank as the frame's depth
+//      range needs (hdsr_dsort.cu); the pairs are then emitted in that depth
+//      order (hdsr_scan.cu);
 //   2. the tile: the pairs are listed per superblock of 8x8 tiles by one
 //      (two above 512 superblocks) stable 9-bit pass over the superblock
 //      index. A tile's entries are then its superblock list filtered by the

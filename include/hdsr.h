@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define HDSR_ABI_VERSION 3
+#define HDSR_ABI_VERSION 4
 
 typedef enum hdsr_status {
   HDSR_OK = 0,
@@ -206,9 +206,16 @@ typedef enum hdsr_buffer_id {
                                  r, g | b, 0, 0, 0); HDSR_CFG_BACKWARD handles only */
   HDSR_BUF_WORK_ORDER = 12,   /* u32[tile_count] ty << 16 | tx: the order in which the last full
                                  frame's rasteriser took its tiles (a permutation of the tiles) */
-  HDSR_BUF_TILE_COSTS = 13    /* u32[2 * tile_count] per half tile (index 2 * (ty * cols + tx) +
+  HDSR_BUF_TILE_COSTS = 13,   /* u32[2 * tile_count] per half tile (index 2 * (ty * cols + tx) +
                                  half): the last raster's cost, from which the next full frame
                                  orders its tiles (most expensive first); 0 before any raster */
+  HDSR_BUF_SUPERBLOCK_LISTS = 14, /* u64[Q] (Q: hdsr_frame_status.superblock_entries) the lists the
+                                 rasterisers walk: superblock << 36 | local rect << 24 | sortRank,
+                                 grouped by superblock (8x8 tiles, row-major), each list in
+                                 ascending (depth bits, sortRank); the local rect is x0 | x1 << 3 |
+                                 y0 << 6 | y1 << 9, the splat's tile box clipped to the superblock */
+  HDSR_BUF_CHUNK_MASKS = 15   /* u64[(Q + 31) / 32] per 32 list entries: the union of their local
+                                 rects as tile bits (bit y * 8 + x of the superblock) */
 } hdsr_buffer_id;
 
 /* Device address and byte size of an internal buffer (valid until destroy).

@@ -46,7 +46,7 @@ def test_python_mirror_constants_match_the_header(pkg):
 
 
 def test_abi_version(hdsr_lib):
-    assert hdsr_lib.hdsr_abi_version() == 3
+    assert hdsr_lib.hdsr_abi_version() == 4
 
 
 @pytest.mark.parametrize("W,H,N", [(800, 600, 50_000), (1920, 1080, 760_000), (3840, 2160, 3_000_000),
