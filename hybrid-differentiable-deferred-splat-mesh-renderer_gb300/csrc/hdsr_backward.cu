@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
         for (int k = 0; k < 4; ++k) {
           const float dx = dxv[k] - cx, dy = dyv[k] - cy;
           const float pw = fmaf(kc * dy, dy, fmaf(kb * dx, dy, (ka * dx) * dx));
-          const float al = mn(0.99f, op * composite_expf(pw));
+          const float al = mn(0.99f, op * splat_expf(pw));
           const bool valid = (pw > -4.0f) && (al > (1.0f / 255.0f)) && (T[k] >= 0.001f);
           if (valid) {
             const float w = al * T[k];
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
         for (int k = 0; k < 4; ++k) {
           const float dx = dxv[k] - cx, dy = dyv[k] - cy;
           const float pw = fmaf(kc * dy, dy, fmaf(kb * dx, dy, (ka * dx) * dx));
-          const float ge = composite_expf(pw);
+          const float ge = splat_expf(pw);
           const float raw = op * ge;
           const float al = mn(0.99f, raw);
           const bool valid = (pw > -4.0f) && (al > (1.0f / 255.0f)) && (T[k] >= 0.001f);

@@ -174,6 +174,36 @@ HDSR_HD float composite_expf(float x) {
   return p * u2f((f2u(t) << 23) + 0x3F800000u);
 }
 
+// The rasterisers' exp of a splat's power, whose value is used only for a
+// power in (-4, 0] (k in [-6, 0]): the steps of composite_expf with one
+// reduction constant, ln 2 rounded to f32 (1.9e-9 above ln 2, so k * ln2f is
+// off by at most 1.2e-8 for |k| <= 6, below the polynomial's own error).
+// exp(x) = p * 2^k, returned as p and kb = k << 23 (mod 2^32), the bits that
+// put 2^k into a float's exponent field: the rasterisers scale the opacity by
+// 2^k with one integer add instead of forming 2^k and multiplying by it
+// (exact for a normal or zero opacity with a normal product, so the alpha
+// keeps the bits of opacity * splat_expf(x)).
+struct SplatExp {
+  float p;
+  uint32_t kb;
+};
+HDSR_HD SplatExp splat_exp_parts(float x) {
+  const float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
+  const float k = t - 12582912.0f;
+  const float r = fmaf(k, -0.693147182464599609375f, x);
+  float p = 0x1.0fe5c6p-7f;
+  p = fmaf(p, r, 0x1.575eeep-5f);
+  p = fmaf(p, r, 0x1.555a18p-3f);
+  p = fmaf(p, r, 0x1.fffd1ap-2f);
+  p = fmaf(p, r, 0x1.fffff6p-1f);
+  p = fmaf(p, r, 0x1.000002p+0f);
+  return SplatExp{p, f2u(t) << 23};
+}
+HDSR_HD float splat_expf(float x) {
+  const SplatExp e = splat_exp_parts(x);
+  return e.p * u2f(e.kb + 0x3F800000u);
+}
+
 // 16-bit x/y interleave, x on even bits (gpu_tile_splat_composite.wgsl:33-47).
 HDSR_HD uint32_t morton(uint32_t x, uint32_t y) {
   uint32_t a = x & 0xFFFFu;

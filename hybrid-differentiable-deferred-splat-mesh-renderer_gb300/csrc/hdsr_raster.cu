@@ -19,7 +19,8 @@
 // (one entry per lane, 16-byte loads) into the warp's shared-memory slab and
 // reads them as broadcasts. FP32 transmittance.
 // Arithmetic is the canonical form: power = fma(c' dy, dy, fma(b' dx, dy,
-// (a' dx) dx)) and every "acc += v * w" is fma(v, w, acc).
+// (a' dx) dx)), the Gaussian splat_expf(power) (hdsr_math.cuh) and every
+// "acc += v * w" is fma(v, w, acc).
 #include "hdsr_internal.cuh"
 
 namespace hdsr {
@@ -128,8 +129,13 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
   const bool emits = er != 0.0f || eg != 0.0f || eb != 0.0f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const float g = composite_expf(pw[k]);
-    const float al = mn(0.99f, op * g);
+    // alpha = min(0.99, op * splat_expf(power)), with 2^k added into op's
+    // exponent bits (op is 0 or a normal f16 value <= 0.99, op * 2^k stays
+    // normal for k >= -6; for op = 0 and k < 0 the sum is negative or -inf,
+    // an alpha the validity test rejects as it rejects 0; at a power <= -4 the
+    // alpha is unused)
+    const SplatExp ex = splat_exp_parts(pw[k]);
+    const float al = mn(0.99f, u2f(f2u(op) + ex.kb) * ex.p);
     float w;
     if (F16) {
       const __half a16 = __float2half_rn(al), T16 = __float2half_rn(q.T[k]);

@@ -86,9 +86,10 @@ def lib() -> ctypes.CDLL:
         L.orc_gpu_sort_prototype_order.restype = c_int
         L.orc_gpu_sort_prototype_order.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p]
         for nm in ("orc_expf_n", "orc_logf_n", "orc_f16_rne_n", "orc_f16_trunc_n", "orc_f16_to_f32_n", "orc_f64_to_f16_n",
-                   "orc_composite_expf_n"):
+                   "orc_composite_expf_n", "orc_splat_expf_n"):
             getattr(L, nm).argtypes = [c_void_p, c_void_p, c_uint64]
         L.orc_morton_n.argtypes = [c_void_p, c_void_p, c_void_p, c_uint64]
+        L.orc_splat_exp_parts_n.argtypes = [c_void_p, c_void_p, c_void_p, c_uint64]
         L.orc_bucket_key20_n.argtypes = [c_void_p, c_uint64, c_uint32, c_uint32, c_void_p, c_void_p]
         _lib = L
     return _lib
@@ -264,6 +265,19 @@ def expf(x):
 
 def composite_expf(x):
     return _map("orc_composite_expf_n", x, np.float32)
+
+
+def splat_expf(x):
+    return _map("orc_splat_expf_n", x, np.float32)
+
+
+def splat_exp_parts(x):
+    """(p, kb) with splat_expf(x) = p * 2^k and kb = k << 23 (mod 2^32)."""
+    a = np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1))
+    p = np.empty(a.size, np.float32)
+    kb = np.empty(a.size, np.uint32)
+    lib().orc_splat_exp_parts_n(a.ctypes.data, p.ctypes.data, kb.ctypes.data, a.size)
+    return p, kb
 
 
 def logf(x):

@@ -220,7 +220,7 @@ def _f32_trajectory(p, px, py):
     f32 alpha and transmittance products), at the f32 values of the screen
     parameters p (K, 9): per entry and pixel the alpha, the exp factor, the
     capped flag, the validity and the transmittance before the entry."""
-    from . import composite_expf  # the oracle's composite exp
+    from . import splat_expf  # the oracle's composite exp
 
     f32 = np.float32
     fma32 = lambda a, b, c: (np.asarray(a, np.float64) * b + c).astype(f32)  # noqa: E731
@@ -234,7 +234,7 @@ def _f32_trajectory(p, px, py):
         ka, kb, kc = f32(ia * f32(-0.5)), f32(-ib), f32(ic * f32(-0.5))
         dx, dy = (px32 - cx).astype(f32), (py32 - cy).astype(f32)
         pw = fma32((kc * dy).astype(f32), dy, fma32((kb * dx).astype(f32), dy, ((ka * dx).astype(f32) * dx).astype(f32)))
-        g = composite_expf(pw).reshape(n)
+        g = splat_expf(pw).reshape(n)
         raw = (op * g).astype(f32)
         a = np.minimum(f32(0.99), raw)
         v = (pw > f32(-4.0)) & (a > f32(1.0) / f32(255.0)) & (T >= f32(0.001))

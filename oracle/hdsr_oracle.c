@@ -98,12 +98,12 @@ float orc_logf(float x) {
   return fmaf(fe, LN2_HI, fmaf(fe, LN2_LO, lm));
 }
 
-/* exp of the composite's power, the same steps as the kernels' composite_expf:
+/* exp of the deferred passes' weights, the same steps as the kernels' composite_expf:
  * k = the integer nearest the exact x log2(e) (an fma with 1.5 * 2^23, whose
  * rounding rounds to an integer), Cody-Waite reduction (ln2 in two parts),
  * degree-5 polynomial fitted for least maximum relative error on |r| <= ln2/2
- * (own Remez fit), scale 2^k from the sum's low bits, exact for k in [-6, 0]
- * (the power range a pixel uses, (-4, 0]). */
+ * (own Remez fit), scale 2^k from the sum's low bits (a normal float for
+ * k >= -126: the weights call it for x > -86). */
 float orc_composite_expf(float x) {
   const float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
   const float k = t - 12582912.0f;
@@ -116,6 +116,30 @@ float orc_composite_expf(float x) {
   p = fmaf(p, r, 0x1.fffff6p-1f);
   p = fmaf(p, r, 0x1.000002p+0f);
   return p * bitsf((fbits(t) << 23) + 0x3F800000u);
+}
+
+/* exp of a splat's power in the composites (the kernels' splat_expf): the
+ * steps above with one reduction constant, ln 2 rounded to f32, which is
+ * accurate for the powers whose exp is used (k in [-6, 0]). exp(x) = p * 2^k;
+ * *kb = k << 23 (mod 2^32), the exponent-field bits of 2^k. */
+float orc_splat_exp_parts(float x, uint32_t* kb) {
+  const float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
+  const float k = t - 12582912.0f;
+  const float r = fmaf(k, -0.693147182464599609375f, x);
+  float p = 0x1.0fe5c6p-7f;
+  p = fmaf(p, r, 0x1.575eeep-5f);
+  p = fmaf(p, r, 0x1.555a18p-3f);
+  p = fmaf(p, r, 0x1.fffd1ap-2f);
+  p = fmaf(p, r, 0x1.fffff6p-1f);
+  p = fmaf(p, r, 0x1.000002p+0f);
+  *kb = fbits(t) << 23;
+  return p;
+}
+
+float orc_splat_expf(float x) {
+  uint32_t kb;
+  const float p = orc_splat_exp_parts(x, &kb);
+  return p * bitsf(kb + 0x3F800000u);
 }
 
 /* pack2x16float conversion: IEEE round-to-nearest-even, overflow -> inf,
@@ -837,7 +861,7 @@ static void composite_tile(const float* U, const uint32_t* pc, const uint32_t* d
         float sc = unpack_lo(c[13]);
         float er = unpack_lo(c[11]), eg = unpack_hi(c[11]), eb = unpack_lo(c[12]);
         for (int i = 0; i < 4; ++i) {
-          float g = orc_composite_expf(pw[i]);
+          float g = orc_splat_expf(pw[i]);
           float a = fmin_(0.99f, op * g);
           float nT = T[i] * (1.0f - a);
           int valid = (pw[i] > -4.0f) && (a > (1.0f / 255.0f)) && (T[i] >= 0.001f);
@@ -931,7 +955,7 @@ static void composite_tile_f16(const float* U, const uint32_t* pc, const uint32_
         float sc = unpack_lo(c[13]);
         float er = unpack_lo(c[11]), eg = unpack_hi(c[11]), eb = unpack_lo(c[12]);
         for (int i = 0; i < 4; ++i) {
-          float g = orc_composite_expf(pw[i]);
+          float g = orc_splat_expf(pw[i]);
           float a32 = fmin_(0.99f, op * g);
           float a16 = orc_f16_to_f32(orc_f32_to_f16_rne(a32));
           float nT = h16((double)T[i] * (double)h16(1.0 - (double)a16));
@@ -1229,6 +1253,10 @@ void orc_f16_trunc_n(const float* in, uint16_t* out, uint64_t n) { for (uint64_t
 void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f16_to_f32(in[i]); }
 void orc_f64_to_f16_n(const double* in, uint16_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_f64_to_f16_rne(in[i]); }
 void orc_composite_expf_n(const float* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_composite_expf(in[i]); }
+void orc_splat_expf_n(const float* in, float* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_splat_expf(in[i]); }
+void orc_splat_exp_parts_n(const float* in, float* p, uint32_t* kb, uint64_t n) {
+  for (uint64_t i = 0; i < n; ++i) p[i] = orc_splat_exp_parts(in[i], kb + i);
+}
 void orc_morton_n(const uint32_t* x, const uint32_t* y, uint32_t* out, uint64_t n) { for (uint64_t i = 0; i < n; ++i) out[i] = orc_morton(x[i], y[i]); }
 /* bucket (gpu_tile_bucket_sort.wgsl:85) and k20 of depths against one
  * tile's (min, max) depth bits; used to check bucket == k20 >> 13. */

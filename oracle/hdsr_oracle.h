@@ -117,7 +117,9 @@ typedef struct {
 
 /* --- arithmetic ---------------------------------------------------------- */
 float orc_expf(float x);
-float orc_composite_expf(float x);       /* the composite's exp (power in (-4, 0]) */
+float orc_composite_expf(float x);       /* the deferred passes' weight exp */
+float orc_splat_expf(float x);           /* the composites' exp (power in (-4, 0]) */
+float orc_splat_exp_parts(float x, uint32_t* kb); /* its p and k << 23 */
 float orc_logf(float x);
 uint16_t orc_f32_to_f16_rne(float f);     /* pack2x16float rounding */
 uint16_t orc_f64_to_f16_rne(double x);    /* binary16 round-to-nearest-even of a double */
@@ -175,6 +177,8 @@ void orc_f16_trunc_n(const float* in, uint16_t* out, uint64_t n);
 void orc_f16_to_f32_n(const uint16_t* in, float* out, uint64_t n);
 void orc_f64_to_f16_n(const double* in, uint16_t* out, uint64_t n);
 void orc_composite_expf_n(const float* in, float* out, uint64_t n);
+void orc_splat_expf_n(const float* in, float* out, uint64_t n);
+void orc_splat_exp_parts_n(const float* in, float* p, uint32_t* kb, uint64_t n);
 
 /* ---- deferred frame tail (hdsr_post_oracle.c) ---- */
 typedef struct orp_inputs {

@@ -207,6 +207,38 @@ def test_composite_exp_accuracy(orc):
     assert orc.composite_expf(np.float32(0.0))[0] == np.float32(1.0) + np.float32(2.0 ** -23)
 
 
+def test_splat_exp_accuracy(orc):
+    # the composites' exp (one reduction constant) on the power range whose
+    # value is used
+    x = np.concatenate([np.linspace(-4.0, 0.0, 400001), -np.random.default_rng(7).uniform(0, 4, 200000),
+                        np.float32([-4.0, -3.999999, -1e-30, 0.0, 1e-7])]).astype(np.float32)
+    got = orc.splat_expf(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    ulp = np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert np.max(np.abs(got - ref) / ulp) <= 3.0
+    assert orc.splat_expf(np.float32(0.0))[0] == np.float32(1.0) + np.float32(2.0 ** -23)
+
+
+def test_opacity_scaled_by_the_exponent_bits_equals_the_product(orc):
+    # the rasterisers form alpha's product as (op with k added to its
+    # exponent bits) * p; for every f16 opacity the projection can produce
+    # (0 and (0, 0.99]) and powers in (-4, 0] that is op * splat_expf(x) bit
+    # for bit, and op = 0 gives a product the validity test rejects
+    x = np.concatenate([np.linspace(-4.0, 0.0, 4001)[1:], -np.random.default_rng(8).uniform(0, 4, 2000),
+                        np.float32([-1e-30, 1e-7])]).astype(np.float32)
+    h = np.arange(0x0001, 0x3C00, dtype=np.uint16)  # positive f16 values below 1
+    op = orc.f16_to_f32(h)
+    op = op[op <= np.float32(0.99)]
+    p, kb = orc.splat_exp_parts(x)
+    g = orc.splat_expf(x)
+    for i in range(0, op.size, 1024):
+        o = op[i:i + 1024, None]
+        folded = (o.view(np.uint32) + kb[None, :]).view(np.float32) * p[None, :]
+        assert np.array_equal(folded.view(np.uint32), (o * g[None, :]).view(np.uint32))
+    zero = (np.uint32(0) + kb).view(np.float32) * p
+    assert np.all((zero == 0) | (zero < 0))
+
+
 def test_composite_exp_accuracy_over_the_weight_range(orc):
     # the deferred bilateral filter's weights use the same exp down to -86
     # (2^k exact for k >= -126), and 0 below
@@ -474,7 +506,7 @@ def _f16_tiles_match(orc, f, pc, got, h16, fma32, th, cut, bg, W, H):
                 dx, dy = (px - cx).astype(np.float32), (py - cy).astype(np.float32)
                 pw = fma32((kc * dy).astype(np.float32), dy, fma32((kb * dx).astype(np.float32), dy,
                                                                    ((ka * dx).astype(np.float32) * dx).astype(np.float32)))
-                g = orc.composite_expf(pw).reshape(16, 16)
+                g = orc.splat_expf(pw).reshape(16, 16)
                 a32 = np.minimum(np.float32(0.99), (op * g).astype(np.float32))
                 a16 = h16(a32)
                 valid = (pw > -4.0) & (a32 > th) & (T >= cut)
@@ -756,7 +788,7 @@ def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_l
                     dx, dy = (px - cx).astype(np.float32), (py - cy).astype(np.float32)
                     pw = fma32((kc * dy).astype(np.float32), dy, fma32((kb * dx).astype(np.float32), dy,
                                                                        ((ka * dx).astype(np.float32) * dx).astype(np.float32)))
-                    g = orc.composite_expf(pw).reshape(16, 16)
+                    g = orc.splat_expf(pw).reshape(16, 16)
                     al = np.minimum(np.float32(0.99), (op * g).astype(np.float32))
                     nT = (T * (np.float32(1.0) - al).astype(np.float32)).astype(np.float32)
                     valid = (pw > -4.0) & (al > np.float32(1.0) / np.float32(255.0)) & (T >= np.float32(0.001))
