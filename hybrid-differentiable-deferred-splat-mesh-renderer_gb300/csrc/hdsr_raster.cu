@@ -33,8 +33,10 @@ constexpr int kWarps = 4;
 // touch distinct banks within each 8-lane phase.
 //   row 0: cx, cy, -a/2, -b     row 1: -c/2, opacity, r, g
 //   row 2: b, depth, rough, met row 3: nx, ny, nz, confidence
-//   row 4: er, eg, eb, 0
+//   row 4: er, eg, eb, flags (bits, not a value: kEmits, kVotesNonFinite)
 constexpr int kRows = 5;
+constexpr uint32_t kEmits = 1u;           // some emissive channel is not zero
+constexpr uint32_t kVotesNonFinite = 2u;  // depth, material, normal, confidence or emission not finite
 
 struct Quad {
   float T[4];
@@ -126,7 +128,9 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
   const float sc = r3.w, er = r4.x, eg = r4.y, eb = r4.z;
   // a splat without emission adds exactly +0 to the emissive sums: skip it
   // (uniform across the warp, all lanes read the same splat)
-  const bool emits = er != 0.0f || eg != 0.0f || eb != 0.0f;
+  const uint32_t flags = f2u(r4.w);
+  const bool emits = (flags & kEmits) != 0u;
+  float wv[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     // alpha = min(0.99, op * splat_expf(power)), with 2^k added into op's
@@ -156,19 +160,31 @@ __device__ __forceinline__ void quad_splat(Quad& q, float p00x, float p00y, cons
       q.c[k][2] = fmaf(sb, w, q.c[k][2]);
       if (valid) q.T[k] = nT;
     }
-    const float gw = w > 0.01f ? w : 0.0f;
-    q.gd[k] = fmaf(gw, sd, q.gd[k]);
-    q.gw[k] = q.gw[k] + gw;
-    q.m[k][0] = fmaf(mr, gw, q.m[k][0]);
-    q.m[k][1] = fmaf(mm, gw, q.m[k][1]);
-    q.n[k][0] = fmaf(nx, gw, q.n[k][0]);
-    q.n[k][1] = fmaf(ny, gw, q.n[k][1]);
-    q.n[k][2] = fmaf(nz, gw, q.n[k][2]);
-    q.gc[k] = fmaf(sc, gw, q.gc[k]);
+    wv[k] = w;
     if (emits) {
       q.e[k][0] = fmaf(er, w, q.e[k][0]);
       q.e[k][1] = fmaf(eg, w, q.e[k][1]);
       q.e[k][2] = fmaf(eb, w, q.e[k][2]);
+    }
+  }
+  // G-buffer votes, weight w > 0.01 else 0 (the reference's select). A zero
+  // vote of finite attributes adds +-0 to sums that start at +0 and never
+  // become -0, so it leaves them as they are: the lane skips the votes when
+  // none of its pixels has a weight above 0.01 and the splat's attributes
+  // are finite (a non-finite one makes even a zero vote NaN, as in the
+  // reference).
+  if (wv[0] > 0.01f || wv[1] > 0.01f || wv[2] > 0.01f || wv[3] > 0.01f || (flags & kVotesNonFinite) != 0u) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float gw = wv[k] > 0.01f ? wv[k] : 0.0f;
+      q.gd[k] = fmaf(gw, sd, q.gd[k]);
+      q.gw[k] = q.gw[k] + gw;
+      q.m[k][0] = fmaf(mr, gw, q.m[k][0]);
+      q.m[k][1] = fmaf(mm, gw, q.m[k][1]);
+      q.n[k][0] = fmaf(nx, gw, q.n[k][0]);
+      q.n[k][1] = fmaf(ny, gw, q.n[k][1]);
+      q.n[k][2] = fmaf(nz, gw, q.n[k][2]);
+      q.gc[k] = fmaf(sc, gw, q.gc[k]);
     }
   }
   const float cut = F16 ? __half2float(h16_bits(kCutoff16)) : 0.001f;
@@ -226,14 +242,28 @@ __device__ __forceinline__ Row load_row(const FrameArgs& a, uint32_t r) {
   return w;
 }
 
-__device__ __forceinline__ void stage_row(float4 (*s)[kRows], const Row& w, uint32_t slot) {
+// Is any value the entry's G-buffer votes or emission multiply by a weight
+// infinite or NaN? From the stored bits: the depth (f32), the material,
+// octahedral normal, emission and confidence halves (f16, exponent all ones).
+// Finite octahedral halves decode to a finite normal (the vector they
+// normalise is never zero), so the halves decide for the normal too.
+__device__ __forceinline__ bool vote_inputs_nonfinite(const Row& w) {
+  constexpr uint32_t e2 = 0x7C007C00u;
+  const uint32_t halves = __vcmpeq2(w.gb.x & e2, e2) | __vcmpeq2(w.gb.y & e2, e2) | __vcmpeq2(w.gb.z & e2, e2) |
+                          __vcmpeq2(((w.gb.w & 0xFFFFu) | (w.conf << 16)) & e2, e2);
+  return halves != 0u || (w.depth & 0x7F800000u) == 0x7F800000u;
+}
+
+__device__ __forceinline__ void stage_row(float4 (*s)[kRows], const Row& w, bool nonfinite, uint32_t slot) {
   float nx, ny, nz;
   oct_decode(lo16(w.gb.y), hi16(w.gb.y), nx, ny, nz);
+  const float er = lo16(w.gb.z), eg = hi16(w.gb.z), eb = lo16(w.gb.w);
+  const uint32_t flags = (er != 0.0f || eg != 0.0f || eb != 0.0f ? kEmits : 0u) | (nonfinite ? kVotesNonFinite : 0u);
   s[slot][0] = make_float4(w.g.x, w.g.y, w.g.z * -0.5f, -w.g.w);
   s[slot][1] = make_float4(u2f(w.ap.x) * -0.5f, hi16(w.ap.y), lo16(w.ap.z), hi16(w.ap.z));
   s[slot][2] = make_float4(lo16(w.ap.w), u2f(w.depth), lo16(w.gb.x), hi16(w.gb.x));
   s[slot][3] = make_float4(nx, ny, nz, lo16(w.conf));
-  s[slot][4] = make_float4(lo16(w.gb.z), hi16(w.gb.z), lo16(w.gb.w), 0.0f);
+  s[slot][4] = make_float4(er, eg, eb, u2f(flags));
 }
 
 // Resident blocks per SM the register budget is fitted to.
@@ -277,11 +307,18 @@ __global__ void __launch_bounds__(kWarps * 32, HDSR_RASTER_MIN_BLOCKS) k_raster(
     Row cur;
     if (lane < n) cur = load_row(a, rank);
     while (n > 0u) {
-      // keep, in order, the batch's entries that can reach this half tile
-      const bool keep = lane < n && reaches_rect(cur.g.x, cur.g.y, cur.g.z, cur.g.w, u2f(cur.ap.x), hi16(cur.ap.y),
-                                                 rx0, rx0 + 15.0f, ry0, ry0 + 7.0f);
+      // keep, in order, the batch's entries that can reach this half tile:
+      // power > -4 and alpha > 1/255 at some pixel, or power > -4 alone for
+      // an entry with non-finite vote or emission inputs (the reference
+      // multiplies them by the zero weight of every pixel of a quad it
+      // visits, and 0 * NaN poisons the sums; the test with opacity 0.99 is
+      // power > -4 alone)
+      const bool nonfinite = lane < n && vote_inputs_nonfinite(cur);
+      const bool keep = lane < n && reaches_rect(cur.g.x, cur.g.y, cur.g.z, cur.g.w, u2f(cur.ap.x),
+                                                 nonfinite ? 0.99f : hi16(cur.ap.y), rx0, rx0 + 15.0f, ry0,
+                                                 ry0 + 7.0f);
       const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
-      if (keep) stage_row(s, cur, __popc(kept & lt));
+      if (keep) stage_row(s, cur, nonfinite, __popc(kept & lt));
       // the next batch: its rows in flight while this one is composited
       const uint32_t n2 = walk.take(a, lane, 32u, rank);
       if (lane < n2) cur = load_row(a, rank);

@@ -479,3 +479,35 @@ def test_sh3_3m_4k_orbit_parity_and_fp64_error_per_view(cuda, pkg, orc):
         assert P > 100_000_000, (i, P)
         assert psnr >= 50.0, (i, err, psnr)
     res.destroy()
+
+
+@pytest.mark.parametrize("f16", [False, True])
+def test_non_finite_vote_attributes_poison_the_votes_as_in_the_reference(cuda, pkg, orc, f16):
+    # The rasteriser drops entries that reach no pixel of a half tile with
+    # alpha > 1/255 and skips a lane's G-buffer votes when none of its pixels
+    # has a weight above 0.01; both leave the sums as they are only for
+    # finite attributes: a NaN or infinite roughness, metalness, normal or
+    # emission makes even a zero-weight vote NaN (the reference's select of
+    # weight 0 still multiplies, at every pixel of a quad it visits), so such
+    # splats are culled by power alone and always vote. Bit-exact against the
+    # oracle, which follows the reference.
+    rng = np.random.default_rng(41)
+    n = 4000
+    scene = pkg.workloads.plain_scene(n, seed=41)
+    scene.normals = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    scene.normals[2::13] = np.inf
+    scene.normals[5::17, 1] = np.nan
+    scene.roughness = rng.uniform(0, 1, n).astype(np.float32)
+    scene.roughness[::29] = np.nan
+    scene.metalness = rng.uniform(0, 1, n).astype(np.float32)
+    scene.metalness[1::31] = np.inf
+    scene.emissive = np.where(rng.uniform(0, 1, (n, 1)) < 0.3, rng.uniform(0, 2, (n, 3)), 0.0).astype(np.float32)
+    scene.emissive[7::37, 2] = np.nan
+    g = render_gpu(pkg, scene, pkg.camera.OrbitCamera(azimuth=0.3, elevation=0.2, distance=4.5), 160, 128, f16=f16)
+    gpu, ref = assert_frame_parity(orc, g)
+    # the case is live: some pixels' material or normal sums are NaN
+    # (0x7E00 halves), and most are not
+    halves = np.concatenate([gpu["material"].reshape(-1) & 0xFFFF, gpu["material"].reshape(-1) >> 16,
+                             gpu["normal"].reshape(-1) & 0xFFFF, gpu["normal"].reshape(-1) >> 16])
+    nan = (halves & 0x7FFF) > 0x7C00
+    assert 0 < nan.sum() < 0.5 * nan.size
