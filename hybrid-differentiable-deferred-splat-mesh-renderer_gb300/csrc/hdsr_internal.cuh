@@ -203,7 +203,11 @@ __device__ __forceinline__ uint32_t checked_rank(uint32_t r, uint32_t N, uint32_
 // vertices use approximate reciprocals: a vertex off by a relative d lowers
 // that edge's value by at most 0.5 ic (y d)^2 (resp. ia), about 1e-13 of the
 // terms, far inside the margin. An entry that fails the test changes no pixel
-// of the rectangle (every pixel is invalid for it), so skipping it is exact.
+// of the rectangle (every pixel is invalid for it), so skipping it is exact
+// for finite inputs; the rasteriser tests an entry whose G-buffer or emission
+// inputs are not finite with opacity 0.99, i.e. by power alone, since the
+// reference's zero-weight products of those inputs are NaN at every pixel of
+// a quad with power > -4.
 __device__ __forceinline__ bool reaches_rect(float cx, float cy, float ia, float ib, float ic, float op, float x0,
                                              float x1, float y0, float y1) {
   const float xa = x0 - cx, xb = x1 - cx, ya = y0 - cy, yb = y1 - cy;
