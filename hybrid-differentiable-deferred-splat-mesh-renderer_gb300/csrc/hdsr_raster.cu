@@ -60,6 +60,10 @@ __device__ __forceinline__ void quad_init(Quad& q) {
   q.done = false;
 }
 
+// The composites' normalisations divide by one correctly rounded reciprocal
+// (1 / |v|, 1 / (|x| + |y| + |z|), 1 / weight sum) and multiply: the canonical
+// form of WGSL's normalize and '/', which allow 2.5 ulp (the oracle's
+// composites take the same steps).
 __device__ __forceinline__ void oct_decode(float ex, float ey, float& nx, float& ny, float& nz) {
   float x = ex, y = ey, z = (1.0f - fabsf(ex)) - fabsf(ey);
   if (z < 0.0f) {
@@ -70,17 +74,17 @@ __device__ __forceinline__ void oct_decode(float ex, float ey, float& nx, float&
     x = x2;
     y = y2;
   }
-  float l = sqrtf(x * x + y * y + z * z);
-  nx = x / l;
-  ny = y / l;
-  nz = z / l;
+  const float rl = 1.0f / sqrtf(x * x + y * y + z * z);
+  nx = x * rl;
+  ny = y * rl;
+  nz = z * rl;
 }
 
 __device__ __forceinline__ uint32_t oct_pack_norm(float x, float y, float z) {
-  float l = sqrtf(x * x + y * y + z * z);
-  x = x / l; y = y / l; z = z / l;
-  float sum = fabsf(x) + fabsf(y) + fabsf(z);
-  float px = x / sum, py = y / sum;
+  const float rl = 1.0f / sqrtf(x * x + y * y + z * z);
+  x = x * rl; y = y * rl; z = z * rl;
+  const float rs = 1.0f / (fabsf(x) + fabsf(y) + fabsf(z));
+  float px = x * rs, py = y * rs;
   if (z < 0.0f) {
     float sx = px >= 0.0f ? 1.0f : -1.0f;
     float sy = py >= 0.0f ? 1.0f : -1.0f;
@@ -197,7 +201,7 @@ __device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, ui
   for (int k = 0; k < 4; ++k) {
     const uint32_t px = bx + (uint32_t)(k & 1), py = by + (uint32_t)(k >> 1);
     if (px >= a.W || py >= a.H) continue;
-    const float sw = mx(q.gw[k], 0.0001f);
+    const float rsw = 1.0f / mx(q.gw[k], 0.0001f);
     float cr, cg, cb;
     if (F16) {
       const __half T16 = __float2half_rn(q.T[k]);
@@ -216,12 +220,12 @@ __device__ __forceinline__ void quad_store(const FrameArgs& a, const Quad& q, ui
     } else {
       reinterpret_cast<uint2*>(crow)[px] = make_uint2(pack2x16(cr, cg), pack2x16(cb, ca));
     }
-    reinterpret_cast<float*>(reinterpret_cast<char*>(a.out_depth) + (size_t)py * a.depth_pitch)[px] = q.gd[k] / sw;
+    reinterpret_cast<float*>(reinterpret_cast<char*>(a.out_depth) + (size_t)py * a.depth_pitch)[px] = q.gd[k] * rsw;
     reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(a.out_normal) + (size_t)py * a.normal_pitch)[px] =
         oct_pack_norm(q.n[k][0], q.n[k][1] + 0.0001f, q.n[k][2]);
     reinterpret_cast<uint4*>(reinterpret_cast<char*>(a.out_material) + (size_t)py * a.material_pitch)[px] =
-        make_uint4(pack2x16(q.m[k][0] / sw, q.m[k][1] / sw), pack2x16(q.e[k][0], q.e[k][1]),
-                   pack2x16(q.e[k][2], 0.0f), pack2x16(q.gc[k] / sw, 0.0f));
+        make_uint4(pack2x16(q.m[k][0] * rsw, q.m[k][1] * rsw), pack2x16(q.e[k][0], q.e[k][1]),
+                   pack2x16(q.e[k][2], 0.0f), pack2x16(q.gc[k] * rsw, 0.0f));
   }
 }
 

@@ -283,6 +283,28 @@ static inline void oct_encode(v3 n, float* ox, float* oy) {
   *ox = px; *oy = py;
 }
 
+/* The composites' normalisations divide by one correctly rounded reciprocal
+ * and multiply (the kernels' canonical form of WGSL's normalize and '/',
+ * which allow 2.5 ulp); the projection's octahedral encoding keeps its
+ * divisions (oct_encode). */
+static inline v3 norm3_rcp(v3 a) { return mul3s(a, 1.0f / len3(a)); }
+
+/* octEncode(normalize(v)) of the composites' voted normals
+ * (gpu_tile_splat_composite.wgsl:134-141, 333-336), in the reciprocal form */
+static inline void oct_encode_out(v3 v, float* ox, float* oy) {
+  v3 n = norm3_rcp(v);
+  float rs = 1.0f / (fabsf(n.x) + fabsf(n.y) + fabsf(n.z));
+  float px = n.x * rs, py = n.y * rs;
+  if (n.z < 0.0f) {
+    float sx = px >= 0.0f ? 1.0f : -1.0f;
+    float sy = py >= 0.0f ? 1.0f : -1.0f;
+    float nx = (1.0f - fabsf(py)) * sx;
+    float ny = (1.0f - fabsf(px)) * sy;
+    px = nx; py = ny;
+  }
+  *ox = px; *oy = py;
+}
+
 /* gpu_tile_splat_composite.wgsl:143-149 */
 static inline v3 oct_decode(float ex, float ey) {
   v3 n = V3(ex, ey, (1.0f - fabsf(ex)) - fabsf(ey));
@@ -293,7 +315,7 @@ static inline v3 oct_decode(float ex, float ey) {
     float ny = (1.0f - fabsf(n.x)) * sy;
     n.x = nx; n.y = ny;
   }
-  return norm3(n);
+  return norm3_rcp(n);
 }
 
 /* SH constants, gpu_project_splats.wgsl:59-71 (abstract floats -> f32) */
@@ -889,19 +911,19 @@ static void composite_tile(const float* U, const uint32_t* pc, const uint32_t* d
         uint32_t px = bx + (uint32_t)(i & 1), py = by + (uint32_t)(i >> 1);
         if (px >= W || py >= H) continue;
         uint64_t o = (uint64_t)py * W + px;
-        float sw = fmax_(gbW[i], 0.0001f);
+        float rsw = 1.0f / fmax_(gbW[i], 0.0001f);
         float ox, oy;
-        oct_encode(norm3(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2])), &ox, &oy);
+        oct_encode_out(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2]), &ox, &oy);
         f->out_color[o * 4 + 0] = orc_f32_to_f16_rne(fmaf(T[i], bg[0], col[i][0]));
         f->out_color[o * 4 + 1] = orc_f32_to_f16_rne(fmaf(T[i], bg[1], col[i][1]));
         f->out_color[o * 4 + 2] = orc_f32_to_f16_rne(fmaf(T[i], bg[2], col[i][2]));
         f->out_color[o * 4 + 3] = orc_f32_to_f16_rne(1.0f - T[i]);
-        f->out_depth[o] = gbD[i] / sw;
+        f->out_depth[o] = gbD[i] * rsw;
         f->out_normal[o] = pack2x16(ox, oy);
-        f->out_material[o * 4 + 0] = pack2x16(mat[i][0] / sw, mat[i][1] / sw);
+        f->out_material[o * 4 + 0] = pack2x16(mat[i][0] * rsw, mat[i][1] * rsw);
         f->out_material[o * 4 + 1] = pack2x16(em[i][0], em[i][1]);
         f->out_material[o * 4 + 2] = pack2x16(em[i][2], 0.0f);
-        f->out_material[o * 4 + 3] = pack2x16(gbC[i] / sw, 0.0f);
+        f->out_material[o * 4 + 3] = pack2x16(gbC[i] * rsw, 0.0f);
       }
     }
 }
@@ -984,18 +1006,18 @@ static void composite_tile_f16(const float* U, const uint32_t* pc, const uint32_
         uint32_t px = bx + (uint32_t)(i & 1), py = by + (uint32_t)(i >> 1);
         if (px >= W || py >= H) continue;
         uint64_t o = (uint64_t)py * W + px;
-        float sw = fmax_(gbW[i], 0.0001f);
+        float rsw = 1.0f / fmax_(gbW[i], 0.0001f);
         float ox, oy;
-        oct_encode(norm3(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2])), &ox, &oy);
+        oct_encode_out(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2]), &ox, &oy);
         for (int ch = 0; ch < 3; ++ch)
           f->out_color[o * 4 + ch] = orc_f64_to_f16_rne((double)T[i] * bg[ch] + col[i][ch]);
         f->out_color[o * 4 + 3] = orc_f32_to_f16_rne(1.0f - T[i]);
-        f->out_depth[o] = gbD[i] / sw;
+        f->out_depth[o] = gbD[i] * rsw;
         f->out_normal[o] = pack2x16(ox, oy);
-        f->out_material[o * 4 + 0] = pack2x16(mat[i][0] / sw, mat[i][1] / sw);
+        f->out_material[o * 4 + 0] = pack2x16(mat[i][0] * rsw, mat[i][1] * rsw);
         f->out_material[o * 4 + 1] = pack2x16(em[i][0], em[i][1]);
         f->out_material[o * 4 + 2] = pack2x16(em[i][2], 0.0f);
-        f->out_material[o * 4 + 3] = pack2x16(gbC[i] / sw, 0.0f);
+        f->out_material[o * 4 + 3] = pack2x16(gbC[i] * rsw, 0.0f);
       }
     }
 }

@@ -724,26 +724,37 @@ def test_projection_sh_and_normals_match_an_independent_numpy_restatement(orc, p
 
 
 def _oct_decode_np(e):
-    """octDecode (gpu_tile_splat_composite.wgsl:143-149) on one f16 pair, f32 steps."""
+    """octDecode (gpu_tile_splat_composite.wgsl:143-149) on one f16 pair, f32 steps,
+    normalised by one correctly rounded reciprocal (the composites' canonical
+    form of normalize)."""
     f32 = np.float32
     x, y = f32(e[0]), f32(e[1])
     z = (f32(1.0) - abs(x)) - abs(y)
     if z < 0:
         x, y = (f32(1.0) - abs(y)) * (f32(1.0) if x >= 0 else f32(-1.0)), (f32(1.0) - abs(x)) * (f32(1.0) if y >= 0 else f32(-1.0))
-    ln = np.sqrt((x * x + y * y) + z * z)
-    return np.array([x / ln, y / ln, z / ln], np.float32)
+    r = f32(1.0) / np.sqrt((x * x + y * y) + z * z)
+    return np.array([x * r, y * r, z * r], np.float32)
 
 
-def _oct_encode_np(v, normalize=True):
+def _oct_encode_np(v, normalize=True, recip=False):
     """octEncode(normalize(v)) (gpu_tile_splat_composite.wgsl:134-141), or octEncode(v)
-    for an already unit v, vectorised, f32 steps."""
+    for an already unit v, vectorised, f32 steps; recip: each normalisation by one
+    correctly rounded reciprocal and products (the composites' canonical form)."""
     f32 = np.float32
     x, y, z = v[..., 0], v[..., 1], v[..., 2]
     if normalize:
-        ln = np.sqrt((x * x + y * y) + z * z)
-        x, y, z = x / ln, y / ln, z / ln
+        if recip:
+            r = f32(1.0) / np.sqrt((x * x + y * y) + z * z)
+            x, y, z = x * r, y * r, z * r
+        else:
+            ln = np.sqrt((x * x + y * y) + z * z)
+            x, y, z = x / ln, y / ln, z / ln
     s = (np.abs(x) + np.abs(y)) + np.abs(z)
-    px, py = x / s, y / s
+    if recip:
+        rs = f32(1.0) / s
+        px, py = x * rs, y * rs
+    else:
+        px, py = x / s, y / s
     sx, sy = np.where(px >= 0, f32(1.0), f32(-1.0)), np.where(py >= 0, f32(1.0), f32(-1.0))
     nx, ny = (f32(1.0) - np.abs(py)) * sx, (f32(1.0) - np.abs(px)) * sy
     neg = z < 0
@@ -811,19 +822,19 @@ def test_f32_composite_matches_an_independent_numpy_restatement(orc, pkg, hdsr_l
                 assert np.array_equal(out, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, :3]), (tx, ty)
                 alpha = (np.float32(1.0) - T).astype(np.float16).astype(np.float32)
                 assert np.array_equal(alpha, got[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16, 3]), (tx, ty)
-                sw = np.maximum(gW, np.float32(0.0001))
+                rsw = (np.float32(1.0) / np.maximum(gW, np.float32(0.0001))).astype(np.float32)
                 sl = np.s_[ty * 16:ty * 16 + 16, tx * 16:tx * 16 + 16]
-                assert np.array_equal((gd / sw).astype(np.float32), f["out_depth"][sl]), (tx, ty)
+                assert np.array_equal((gd * rsw).astype(np.float32), f["out_depth"][sl]), (tx, ty)
                 nn = nrm + np.array([0.0, 0.0001, 0.0], np.float32)
-                ox, oy = _oct_encode_np(nn)
+                ox, oy = _oct_encode_np(nn, recip=True)
                 pk = lambda a, b: orc.f16_rne(a.reshape(-1)).astype(np.uint32) | (orc.f16_rne(b.reshape(-1)).astype(np.uint32) << 16)  # noqa: E731
                 assert np.array_equal(pk(ox, oy), f["normal"][sl].reshape(-1)), (tx, ty)
                 zero = np.zeros((16, 16), np.float32)
                 m = f["material"][sl].reshape(-1, 4)
-                assert np.array_equal(pk((mat[..., 0] / sw).astype(np.float32), (mat[..., 1] / sw).astype(np.float32)), m[:, 0])
+                assert np.array_equal(pk((mat[..., 0] * rsw).astype(np.float32), (mat[..., 1] * rsw).astype(np.float32)), m[:, 0])
                 assert np.array_equal(pk(em[..., 0], em[..., 1]), m[:, 1])
                 assert np.array_equal(pk(em[..., 2], zero), m[:, 2])
-                assert np.array_equal(pk((gc / sw).astype(np.float32), zero), m[:, 3])
+                assert np.array_equal(pk((gc * rsw).astype(np.float32), zero), m[:, 3])
     finally:
         np.seterr(**prev)
 
