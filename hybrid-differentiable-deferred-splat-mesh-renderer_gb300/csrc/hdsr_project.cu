@@ -30,7 +30,13 @@ __device__ __forceinline__ V3 cross3(V3 a, V3 b) {
 __device__ __forceinline__ V3 add3(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ V3 sub3(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ V3 mul3s(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ V3 div3s(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+// Quotients that share a denominator take one correctly rounded reciprocal
+// and products (the canonical form of WGSL's '/' and normalize, which allow
+// 2.5 ulp; the oracle's projection takes the same steps).
+__device__ __forceinline__ V3 div3s(V3 a, float s) {
+  const float r = 1.0f / s;
+  return v3(a.x * r, a.y * r, a.z * r);
+}
 __device__ __forceinline__ float len3(V3 a) { return sqrtf(dot3(a, a)); }
 __device__ __forceinline__ V3 norm3(V3 a) { return div3s(a, len3(a)); }
 
@@ -38,7 +44,8 @@ __device__ __forceinline__ V3 norm3(V3 a) { return div3s(a, len3(a)); }
 __device__ __forceinline__ V3 rotate_axis(float4 q4, V3 axis) {
   float ql = sqrtf(q4.x * q4.x + q4.y * q4.y + q4.z * q4.z + q4.w * q4.w);
   float d = mx(ql, 0.000001f);
-  float qx = q4.x / d, qy = q4.y / d, qz = q4.z / d, qw = q4.w / d;
+  const float rd = 1.0f / d;
+  float qx = q4.x * rd, qy = q4.y * rd, qz = q4.z * rd, qw = q4.w * rd;
   V3 u = v3(qy, qz, qw);
   V3 inner = add3(cross3(u, axis), mul3s(axis, qx));
   V3 c = cross3(u, inner);
@@ -47,8 +54,8 @@ __device__ __forceinline__ V3 rotate_axis(float4 q4, V3 axis) {
 
 // gpu_project_splats.wgsl:82-89
 __device__ __forceinline__ uint32_t oct_pack(V3 n) {
-  float sum = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
-  float px = n.x / sum, py = n.y / sum;
+  const float rs = 1.0f / (fabsf(n.x) + fabsf(n.y) + fabsf(n.z));
+  float px = n.x * rs, py = n.y * rs;
   if (n.z < 0.0f) {
     float sx = px >= 0.0f ? 1.0f : -1.0f;
     float sy = py >= 0.0f ? 1.0f : -1.0f;
@@ -114,12 +121,12 @@ __global__ void __launch_bounds__(256, MINB) k_project(FrameArgs a) {
     clip[k] = ((ldf(U + k) * center.x + ldf(U + 4 + k) * center.y) + ldf(U + 8 + k) * center.z) +
               ldf(U + 12 + k) * 1.0f;
   if (clip[3] <= 0.0f) { write_invisible(a, r); return; }
-  float safeW = mx(clip[3], 0.0001f);
-  float ndcx = clip[0] / safeW, ndcy = clip[1] / safeW;
+  const float rW = 1.0f / mx(clip[3], 0.0001f);
+  float ndcx = clip[0] * rW, ndcy = clip[1] * rW;
   float vpW = ldf(U + 16), vpH = ldf(U + 17);
   float cpx = (ndcx * 0.5f + 0.5f) * vpW;
   float cpy = (1.0f - (ndcy * 0.5f + 0.5f)) * vpH;
-  float depthNdc = clip[2] / safeW;
+  float depthNdc = clip[2] * rW;
 
   const float* sl = a.scl + (uint64_t)splatId * 3;
   float4 q = __ldg(reinterpret_cast<const float4*>(a.rot) + splatId);
@@ -144,9 +151,10 @@ __global__ void __launch_bounds__(256, MINB) k_project(FrameArgs a) {
     vc[k] = ((ldf(U + 32 + k) * center.x + ldf(U + 36 + k) * center.y) + ldf(U + 40 + k) * center.z) +
             ldf(U + 44 + k) * 1.0f;
   float vz = mn(vc[2], -0.001f);
-  float J1x = ldf(U + 48) / vz, J1y = ldf(U + 49) / vz;
-  float J2x = (-J1x / vz) * vc[0];
-  float J2y = (-J1y / vz) * vc[1];
+  const float rvz = 1.0f / vz;
+  float J1x = ldf(U + 48) * rvz, J1y = ldf(U + 49) * rvz;
+  float J2x = (-J1x * rvz) * vc[0];
+  float J2y = (-J1y * rvz) * vc[1];
   V3 tt0 = v3(J1x * w0.x + J2x * w2.x, J1x * w0.y + J2x * w2.y, J1x * w0.z + J2x * w2.z);
   V3 tt1 = v3(J1y * w1.x + J2y * w2.x, J1y * w1.y + J2y * w2.y, J1y * w1.z + J2y * w2.z);
   V3 b0 = v3(dot3(axis0, tt0), dot3(axis1, tt0), dot3(axis2, tt0));
@@ -156,13 +164,13 @@ __global__ void __launch_bounds__(256, MINB) k_project(FrameArgs a) {
   float covXX = covXXraw + 0.3f;
   float covYY = covYYraw + 0.3f;
   float detBlur = covXX * covYY - covXY * covXY;
-  float aaFactor = sqrtf(mx(detOrig / mx(detBlur, 0.000001f), 0.0f));
+  const float detInv = 1.0f / mx(detBlur, 0.000001f);
+  float aaFactor = sqrtf(mx(detOrig * detInv, 0.0f));
   float mid = 0.5f * (covXX + covYY);
   float det = mx(detBlur, 0.1f);
   float lambda = mid + sqrtf(mx(mid * mid - det, 0.1f));
   float radius = ceilf(3.0f * sqrtf(lambda));
   if (radius <= 0.0f) { write_invisible(a, r); return; }
-  float detInv = 1.0f / mx(detBlur, 0.000001f);
   float icx = covYY * detInv, icy = -covXY * detInv, icz = covXX * detInv;
   float sourceOpacity = clampf(ldf(a.opa + splatId) * aaFactor, 0.0f, 0.99f);
 
@@ -172,10 +180,11 @@ __global__ void __launch_bounds__(256, MINB) k_project(FrameArgs a) {
   float clampedRadius = mn(radius, tileSize * 8.0f);
   float minPx = mx(cpx - clampedRadius, 0.0f), minPy = mx(cpy - clampedRadius, 0.0f);
   float maxPx = mn(cpx + clampedRadius, vpW), maxPy = mn(cpy + clampedRadius, vpH);
-  uint32_t t0x = min(sat_u32(floorf(minPx / tileSize)), maxTx);
-  uint32_t t0y = min(sat_u32(floorf(minPy / tileSize)), maxTy);
-  uint32_t t1x = min(sat_u32(floorf(mx((maxPx - 0.000000001f) / tileSize, 0.0f))), maxTx);
-  uint32_t t1y = min(sat_u32(floorf(mx((maxPy - 0.000000001f) / tileSize, 0.0f))), maxTy);
+  const float rTile = 1.0f / tileSize;
+  uint32_t t0x = min(sat_u32(floorf(minPx * rTile)), maxTx);
+  uint32_t t0y = min(sat_u32(floorf(minPy * rTile)), maxTy);
+  uint32_t t1x = min(sat_u32(floorf(mx((maxPx - 0.000000001f) * rTile, 0.0f))), maxTx);
+  uint32_t t1y = min(sat_u32(floorf(mx((maxPy - 0.000000001f) * rTile, 0.0f))), maxTy);
   uint32_t box = (t0x & 0xFFu) | ((t0y & 0xFFu) << 8) | ((t1x & 0xFFu) << 16) | ((t1y & 0xFFu) << 24);
 
   // normals (gpu_project_splats.wgsl:234-291)

@@ -254,7 +254,10 @@ static inline v3 cross3(v3 a, v3 b) {
 static inline v3 add3(v3 a, v3 b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
 static inline v3 sub3(v3 a, v3 b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
 static inline v3 mul3s(v3 a, float s) { return V3(a.x * s, a.y * s, a.z * s); }
-static inline v3 div3s(v3 a, float s) { return V3(a.x / s, a.y / s, a.z / s); }
+/* Quotients that share a denominator take one correctly rounded reciprocal
+ * and products (the kernels' canonical form of WGSL's '/' and normalize,
+ * which allow 2.5 ulp), in the projection and the composites alike. */
+static inline v3 div3s(v3 a, float s) { return mul3s(a, 1.0f / s); }
 static inline float len3(v3 a) { return sqrtf(dot3(a, a)); }
 static inline v3 norm3(v3 a) { return div3s(a, len3(a)); }
 
@@ -262,7 +265,8 @@ static inline v3 norm3(v3 a) { return div3s(a, len3(a)); }
 static inline v3 rotate_axis(const float q4[4], v3 axis) {
   float ql = sqrtf(q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
   float d = fmax_(ql, 0.000001f);
-  float qx = q4[0] / d, qy = q4[1] / d, qz = q4[2] / d, qw = q4[3] / d;
+  float rd = 1.0f / d;
+  float qx = q4[0] * rd, qy = q4[1] * rd, qz = q4[2] * rd, qw = q4[3] * rd;
   v3 u = V3(qy, qz, qw);
   v3 inner = add3(cross3(u, axis), mul3s(axis, qx));
   v3 c = cross3(u, inner);
@@ -271,28 +275,6 @@ static inline v3 rotate_axis(const float q4[4], v3 axis) {
 
 /* gpu_project_splats.wgsl:82-89 */
 static inline void oct_encode(v3 n, float* ox, float* oy) {
-  float sum = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
-  float px = n.x / sum, py = n.y / sum;
-  if (n.z < 0.0f) {
-    float sx = px >= 0.0f ? 1.0f : -1.0f;
-    float sy = py >= 0.0f ? 1.0f : -1.0f;
-    float nx = (1.0f - fabsf(py)) * sx;
-    float ny = (1.0f - fabsf(px)) * sy;
-    px = nx; py = ny;
-  }
-  *ox = px; *oy = py;
-}
-
-/* The composites' normalisations divide by one correctly rounded reciprocal
- * and multiply (the kernels' canonical form of WGSL's normalize and '/',
- * which allow 2.5 ulp); the projection's octahedral encoding keeps its
- * divisions (oct_encode). */
-static inline v3 norm3_rcp(v3 a) { return mul3s(a, 1.0f / len3(a)); }
-
-/* octEncode(normalize(v)) of the composites' voted normals
- * (gpu_tile_splat_composite.wgsl:134-141, 333-336), in the reciprocal form */
-static inline void oct_encode_out(v3 v, float* ox, float* oy) {
-  v3 n = norm3_rcp(v);
   float rs = 1.0f / (fabsf(n.x) + fabsf(n.y) + fabsf(n.z));
   float px = n.x * rs, py = n.y * rs;
   if (n.z < 0.0f) {
@@ -315,7 +297,7 @@ static inline v3 oct_decode(float ex, float ey) {
     float ny = (1.0f - fabsf(n.x)) * sy;
     n.x = nx; n.y = ny;
   }
-  return norm3_rcp(n);
+  return norm3(n);
 }
 
 /* SH constants, gpu_project_splats.wgsl:59-71 (abstract floats -> f32) */
@@ -358,12 +340,12 @@ static void project_one(const float* U, const orc_scene* s, uint32_t sortRank, u
     depth[sortRank] = SENTINEL;
     return;
   }
-  float safeW = fmax_(clip[3], 0.0001f);
-  float ndcx = clip[0] / safeW, ndcy = clip[1] / safeW;
+  float rW = 1.0f / fmax_(clip[3], 0.0001f);
+  float ndcx = clip[0] * rW, ndcy = clip[1] * rW;
   float vpW = Uf(U, 16), vpH = Uf(U, 17);
   float cpx = (ndcx * 0.5f + 0.5f) * vpW;
   float cpy = (1.0f - (ndcy * 0.5f + 0.5f)) * vpH;
-  float depthNdc = clip[2] / safeW;
+  float depthNdc = clip[2] * rW;
 
   const float* sl = s->scales + (uint64_t)splatId * 3;
   const float* q = s->rotations + (uint64_t)splatId * 4;
@@ -387,9 +369,10 @@ static void project_one(const float* U, const orc_scene* s, uint32_t sortRank, u
     vc[r] = ((U[32 + r] * center.x + U[36 + r] * center.y) + U[40 + r] * center.z) + U[44 + r] * 1.0f;
   float vz = fmin_(vc[2], -0.001f);
   float focx = U[48], focy = U[49];
-  float J1x = focx / vz, J1y = focy / vz;
-  float J2x = (-J1x / vz) * vc[0];
-  float J2y = (-J1y / vz) * vc[1];
+  float rvz = 1.0f / vz;
+  float J1x = focx * rvz, J1y = focy * rvz;
+  float J2x = (-J1x * rvz) * vc[0];
+  float J2y = (-J1y * rvz) * vc[1];
   v3 tt0 = V3(J1x * w0.x + J2x * w2.x, J1x * w0.y + J2x * w2.y, J1x * w0.z + J2x * w2.z);
   v3 tt1 = V3(J1y * w1.x + J2y * w2.x, J1y * w1.y + J2y * w2.y, J1y * w1.z + J2y * w2.z);
   v3 b0 = V3(dot3(axis0, tt0), dot3(axis1, tt0), dot3(axis2, tt0));
@@ -399,7 +382,8 @@ static void project_one(const float* U, const orc_scene* s, uint32_t sortRank, u
   float covXX = covXXraw + 0.3f;
   float covYY = covYYraw + 0.3f;
   float detBlur = covXX * covYY - covXY * covXY;
-  float aaFactor = sqrtf(fmax_(detOrig / fmax_(detBlur, 0.000001f), 0.0f));
+  float detInv = 1.0f / fmax_(detBlur, 0.000001f);
+  float aaFactor = sqrtf(fmax_(detOrig * detInv, 0.0f));
   float mid = 0.5f * (covXX + covYY);
   float det = fmax_(detBlur, 0.1f);
   float lambda = mid + sqrtf(fmax_(mid * mid - det, 0.1f));
@@ -409,7 +393,6 @@ static void project_one(const float* U, const orc_scene* s, uint32_t sortRank, u
     depth[sortRank] = SENTINEL;
     return;
   }
-  float detInv = 1.0f / fmax_(detBlur, 0.000001f);
   float icx = covYY * detInv, icy = -covXY * detInv, icz = covXX * detInv;
   float sourceOpacity = clampf_(s->opacities[splatId] * aaFactor, 0.0f, 0.99f);
 
@@ -419,10 +402,11 @@ static void project_one(const float* U, const orc_scene* s, uint32_t sortRank, u
   float clampedRadius = fmin_(radius, tileSize * 8.0f);
   float minPx = fmax_(cpx - clampedRadius, 0.0f), minPy = fmax_(cpy - clampedRadius, 0.0f);
   float maxPx = fmin_(cpx + clampedRadius, vpW), maxPy = fmin_(cpy + clampedRadius, vpH);
-  uint32_t t0x = sat_u32(floorf(minPx / tileSize)); if (t0x > maxTx) t0x = maxTx;
-  uint32_t t0y = sat_u32(floorf(minPy / tileSize)); if (t0y > maxTy) t0y = maxTy;
-  uint32_t t1x = sat_u32(floorf(fmax_((maxPx - 0.000000001f) / tileSize, 0.0f))); if (t1x > maxTx) t1x = maxTx;
-  uint32_t t1y = sat_u32(floorf(fmax_((maxPy - 0.000000001f) / tileSize, 0.0f))); if (t1y > maxTy) t1y = maxTy;
+  float rTile = 1.0f / tileSize;
+  uint32_t t0x = sat_u32(floorf(minPx * rTile)); if (t0x > maxTx) t0x = maxTx;
+  uint32_t t0y = sat_u32(floorf(minPy * rTile)); if (t0y > maxTy) t0y = maxTy;
+  uint32_t t1x = sat_u32(floorf(fmax_((maxPx - 0.000000001f) * rTile, 0.0f))); if (t1x > maxTx) t1x = maxTx;
+  uint32_t t1y = sat_u32(floorf(fmax_((maxPy - 0.000000001f) * rTile, 0.0f))); if (t1y > maxTy) t1y = maxTy;
 
   c[0] = fbits(cpx); c[1] = fbits(cpy);
   c[2] = fbits(icx); c[3] = fbits(icy); c[4] = fbits(icz);
@@ -913,7 +897,7 @@ static void composite_tile(const float* U, const uint32_t* pc, const uint32_t* d
         uint64_t o = (uint64_t)py * W + px;
         float rsw = 1.0f / fmax_(gbW[i], 0.0001f);
         float ox, oy;
-        oct_encode_out(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2]), &ox, &oy);
+        oct_encode(norm3(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2])), &ox, &oy);
         f->out_color[o * 4 + 0] = orc_f32_to_f16_rne(fmaf(T[i], bg[0], col[i][0]));
         f->out_color[o * 4 + 1] = orc_f32_to_f16_rne(fmaf(T[i], bg[1], col[i][1]));
         f->out_color[o * 4 + 2] = orc_f32_to_f16_rne(fmaf(T[i], bg[2], col[i][2]));
@@ -1008,7 +992,7 @@ static void composite_tile_f16(const float* U, const uint32_t* pc, const uint32_
         uint64_t o = (uint64_t)py * W + px;
         float rsw = 1.0f / fmax_(gbW[i], 0.0001f);
         float ox, oy;
-        oct_encode_out(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2]), &ox, &oy);
+        oct_encode(norm3(V3(nrm[i][0], nrm[i][1] + 0.0001f, nrm[i][2])), &ox, &oy);
         for (int ch = 0; ch < 3; ++ch)
           f->out_color[o * 4 + ch] = orc_f64_to_f16_rne((double)T[i] * bg[ch] + col[i][ch]);
         f->out_color[o * 4 + 3] = orc_f32_to_f16_rne(1.0f - T[i]);

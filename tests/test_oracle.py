@@ -530,8 +530,9 @@ def _np_project(orc, U, packed, n):
 def _np_project_body(orc, U, packed, n):
     """project_splats (gpu_project_splats.wgsl:112-357) restated with numpy f32
     arithmetic for splat ids 0..n-1 in order: one rounding per operation, sums
-    left to right (the canonical form), the projection's own exp. Returns the
-    expected cache words, depth and the visibility mask."""
+    left to right, quotients that share a denominator as one correctly rounded
+    reciprocal and products (the canonical form), the projection's own exp.
+    Returns the expected cache words, depth and the visibility mask."""
     f32 = np.float32
     U = np.asarray(U, np.float32)
     P = packed.positions.reshape(-1, 3).astype(f32)
@@ -544,21 +545,21 @@ def _np_project_body(orc, U, packed, n):
         return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
 
     def norm(v):
-        ln = np.sqrt(dot(v, v))
-        return tuple(c / ln for c in v)
+        r = f32(1.0) / np.sqrt(dot(v, v))
+        return tuple(c * r for c in v)
 
     clip = [((U[0 + r] * x + U[4 + r] * y) + U[8 + r] * z) + U[12 + r] * f32(1.0) for r in range(4)]
     vis = clip[3] > 0
-    safeW = np.maximum(clip[3], f32(0.0001))
-    ndcx, ndcy = clip[0] / safeW, clip[1] / safeW
+    rW = f32(1.0) / np.maximum(clip[3], f32(0.0001))
+    ndcx, ndcy = clip[0] * rW, clip[1] * rW
     cpx = (ndcx * f32(0.5) + f32(0.5)) * U[16]
     cpy = (f32(1.0) - (ndcy * f32(0.5) + f32(0.5))) * U[17]
-    depth = clip[2] / safeW
+    depth = clip[2] * rW
     sl = packed.scales.reshape(-1, 3).astype(f32)
     q = packed.rotations.reshape(-1, 4).astype(f32)
     scale = [orc.expf(sl[:, k]) * U[24] for k in range(3)]
-    qn = q / np.maximum(np.sqrt(((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]) + q[:, 2] * q[:, 2]) + q[:, 3] * q[:, 3]),
-                        f32(0.000001))[:, None]
+    qn = q * (f32(1.0) / np.maximum(np.sqrt(((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]) + q[:, 2] * q[:, 2])
+                                            + q[:, 3] * q[:, 3]), f32(0.000001)))[:, None]
     u3, qw = (qn[:, 1], qn[:, 2], qn[:, 3]), qn[:, 0]
     axes = []
     for k, e in enumerate(((1, 0, 0), (0, 1, 0), (0, 0, 1))):
@@ -568,8 +569,9 @@ def _np_project_body(orc, U, packed, n):
         axes.append(tuple((ev[i] + f32(2.0) * c2[i]) * scale[k] for i in range(3)))
     vc = [((U[32 + r] * x + U[36 + r] * y) + U[40 + r] * z) + U[44 + r] * f32(1.0) for r in range(3)]
     vz = np.minimum(vc[2], f32(-0.001))
-    J1x, J1y = U[48] / vz, U[49] / vz
-    J2x, J2y = (-J1x / vz) * vc[0], (-J1y / vz) * vc[1]
+    rvz = f32(1.0) / vz
+    J1x, J1y = U[48] * rvz, U[49] * rvz
+    J2x, J2y = (-J1x * rvz) * vc[0], (-J1y * rvz) * vc[1]
     w0, w1, w2 = (U[32], U[36], U[40]), (U[33], U[37], U[41]), (U[34], U[38], U[42])
     tt0 = tuple(J1x * w0[i] + J2x * w2[i] for i in range(3))
     tt1 = tuple(J1y * w1[i] + J2y * w2[i] for i in range(3))
@@ -578,12 +580,12 @@ def _np_project_body(orc, U, packed, n):
     detO = cxx * cyy - cxy * cxy
     cXX, cYY = cxx + f32(0.3), cyy + f32(0.3)
     detB = cXX * cYY - cxy * cxy
-    aa = np.sqrt(np.maximum(detO / np.maximum(detB, f32(0.000001)), f32(0.0)))
+    dinv = f32(1.0) / np.maximum(detB, f32(0.000001))
+    aa = np.sqrt(np.maximum(detO * dinv, f32(0.0)))
     mid = f32(0.5) * (cXX + cYY)
     lam = mid + np.sqrt(np.maximum(mid * mid - np.maximum(detB, f32(0.1)), f32(0.1)))
     radius = np.ceil(f32(3.0) * np.sqrt(lam))
     vis &= radius > 0
-    dinv = f32(1.0) / np.maximum(detB, f32(0.000001))
     ic = (cYY * dinv, -cxy * dinv, cXX * dinv)
     op = np.clip(packed.opacities.astype(f32) * aa, f32(0.0), f32(0.99))
     ts = np.maximum(U[18], f32(1.0))
@@ -592,9 +594,10 @@ def _np_project_body(orc, U, packed, n):
     lo = (np.maximum(cpx - cr, f32(0.0)), np.maximum(cpy - cr, f32(0.0)))
     hi = (np.minimum(cpx + cr, U[16]), np.minimum(cpy + cr, U[17]))
     sat = lambda v, m: np.minimum(np.clip(np.floor(v), 0, 2.0 ** 32 - 1).astype(np.uint64), m)  # noqa: E731
-    t0x, t0y = sat(lo[0] / ts, max(gx, 1) - 1), sat(lo[1] / ts, max(gy, 1) - 1)
-    t1x = sat(np.maximum((hi[0] - f32(0.000000001)) / ts, f32(0.0)), max(gx, 1) - 1)
-    t1y = sat(np.maximum((hi[1] - f32(0.000000001)) / ts, f32(0.0)), max(gy, 1) - 1)
+    rts = f32(1.0) / ts
+    t0x, t0y = sat(lo[0] * rts, max(gx, 1) - 1), sat(lo[1] * rts, max(gy, 1) - 1)
+    t1x = sat(np.maximum((hi[0] - f32(0.000000001)) * rts, f32(0.0)), max(gx, 1) - 1)
+    t1y = sat(np.maximum((hi[1] - f32(0.000000001)) * rts, f32(0.0)), max(gy, 1) - 1)
     box = (t0x & 0xFF) | ((t0y & 0xFF) << 8) | ((t1x & 0xFF) << 16) | ((t1y & 0xFF) << 24)
     # normals (:233-291)
     lens = [dot(a, a) for a in axes]
@@ -605,7 +608,8 @@ def _np_project_body(orc, U, packed, n):
     if nd.size >= 3 * n:
         bk = (nd[0:3 * n:3], nd[1:3 * n:3], nd[2:3 * n:3])
         bl = np.sqrt(dot(bk, bk))
-        sn = tuple(np.where(bl > f32(0.001), bk[i] / bl, sn[i]) for i in range(3))
+        rbl = f32(1.0) / bl
+        sn = tuple(np.where(bl > f32(0.001), bk[i] * rbl, sn[i]) for i in range(3))
     if nd.size >= 6 * n:
         dt = (nd[3 * n::3], nd[3 * n + 1::3], nd[3 * n + 2::3])
         dl = np.sqrt(dot(dt, dt))
@@ -615,9 +619,10 @@ def _np_project_body(orc, U, packed, n):
         d = dot(tc, sn)
         tp = tuple(tc[i] - sn[i] * d for i in range(3))
         tl = np.sqrt(dot(tp, tp))
-        T = tuple(tp[i] / tl for i in range(3))
+        rtl, rdl = f32(1.0) / tl, f32(1.0) / dl
+        T = tuple(tp[i] * rtl for i in range(3))
         B = cross(sn, T)
-        dn = tuple(dt[i] / dl for i in range(3))
+        dn = tuple(dt[i] * rdl for i in range(3))
         m = norm(tuple((T[i] * dn[0] + B[i] * dn[1]) + sn[i] * dn[2] for i in range(3)))
         use = (dl > f32(0.001)) & (tl > f32(0.001))
         sn = tuple(np.where(use, m[i], sn[i]) for i in range(3))
@@ -627,7 +632,7 @@ def _np_project_body(orc, U, packed, n):
     faced = tuple(np.where(flip, -c, c) for c in fn)
     conf = np.clip(dot(faced, nvd), f32(0.0), f32(1.0))
     wn = norm(tuple((U[52 + k] * faced[0] + U[56 + k] * faced[1]) + U[60 + k] * faced[2] for k in range(3)))
-    ox, oy = _oct_encode_np(np.stack(wn, -1), normalize=False)
+    ox, oy = _oct_encode_np(np.stack(wn, -1), normalize=False, recip=True)
     # SH colour (:293-351) and emissive (:353-357)
     deg = packed.sh_degree
     sh = packed.sh_data.reshape(n, -1).astype(f32)
