@@ -149,13 +149,12 @@ HDSR_HD uint32_t pack2x16(float a, float b) { return f32_to_f16(a) | (f32_to_f16
 HDSR_HD float lo16(uint32_t w) { return f16_to_f32(w & 0xFFFFu); }
 HDSR_HD float hi16(uint32_t w) { return f16_to_f32(w >> 16); }
 
-// exp of the composite's power (the rasteriser, its f16 variant and the
-// adjoint): Cody-Waite reduction r = x - k ln2 (|r| <= ln2/2, ln2 split in
-// two), then a degree-5 polynomial in r fitted for least maximum relative
-// error on that interval (this project's own Remez fit: 7.5e-8 in exact
-// arithmetic, at most 2.6 ulp in f32 Horner steps against the true exp on
-// (-4, 0]). A pixel only takes a splat when the power is > -4, so the scale
-// 2^k, k in [-6, 0], is exact in one multiply; below that the value is unused.
+// exp on a wide range (the deferred passes' weights, x > -86: weight_expf;
+// the rasterisers use splat_expf below): Cody-Waite reduction r = x - k ln2
+// (|r| <= ln2/2, ln2 split in two), then a degree-5 polynomial in r fitted
+// for least maximum relative error on that interval (this project's own Remez
+// fit: 7.5e-8 in exact arithmetic, at most 3 ulp in f32 Horner steps against
+// the true exp down to -86). The scale 2^k is a normal float for k >= -126.
 // k is the integer nearest the exact x log2(e): the fma adds 1.5 * 2^23, where
 // the float spacing is 1, so its rounding rounds the product to an integer
 // and leaves k + 2^22 in the low mantissa bits (no conversion instructions);
