@@ -198,7 +198,8 @@ def test_exp_accuracy(orc):
 
 
 def test_composite_exp_accuracy(orc):
-    # the composite's exp (degree-5 fit) on the power range a pixel uses
+    # the two-constant exp (degree-5 fit; the deferred weights' exp) on the
+    # power range a pixel uses
     x = np.concatenate([np.linspace(-4.0, 0.0, 400001), -np.random.default_rng(5).uniform(0, 4, 200000)]).astype(np.float32)
     got = orc.composite_expf(x).astype(np.float64)
     ref = np.exp(x.astype(np.float64))
