@@ -742,6 +742,29 @@ def _oct_decode_np(e):
     return np.array([x * r, y * r, z * r], np.float32)
 
 
+def test_finite_octahedral_halves_decode_to_a_finite_normal(orc):
+    # The rasteriser decides from the stored bits whether a splat's vote
+    # inputs are finite: an octahedral normal counts as finite when its two
+    # f16 halves are, which holds because the decoded vector is never zero
+    # (z = 1 - |x| - |y| is 1 where x = y = 0, and the fold leaves |x| or |y|
+    # at 1 - |.| > 0 where z < 0) and its squares stay far below f32 overflow.
+    f32 = np.float32
+    bits = np.concatenate([np.arange(0, 0x7C00, 97, dtype=np.uint16),
+                           np.array([0x0000, 0x0001, 0x03FF, 0x0400, 0x3BFF, 0x3C00, 0x3C01, 0x7BFF], np.uint16)])
+    h = orc.f16_to_f32(np.concatenate([bits, bits | 0x8000]))
+    x, y = np.meshgrid(h, h)
+    x, y = x.reshape(-1).astype(f32), y.reshape(-1).astype(f32)
+    z = (f32(1.0) - np.abs(x)) - np.abs(y)
+    fold = z < 0
+    x2 = (f32(1.0) - np.abs(y)) * np.where(x >= 0, f32(1.0), f32(-1.0))
+    y2 = (f32(1.0) - np.abs(x)) * np.where(y >= 0, f32(1.0), f32(-1.0))
+    x, y = np.where(fold, x2, x), np.where(fold, y2, y)
+    l2 = (x * x + y * y) + z * z
+    assert np.all(l2 > 0) and np.all(np.isfinite(l2))
+    r = f32(1.0) / np.sqrt(l2)
+    assert np.all(np.isfinite(x * r)) and np.all(np.isfinite(y * r)) and np.all(np.isfinite(z * r))
+
+
 def _oct_encode_np(v, normalize=True, recip=False):
     """octEncode(normalize(v)) (gpu_tile_splat_composite.wgsl:134-141), or octEncode(v)
     for an already unit v, vectorised, f32 steps; recip: each normalisation by one
