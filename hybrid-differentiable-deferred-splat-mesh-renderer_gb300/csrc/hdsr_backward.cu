@@ -214,7 +214,9 @@ __global__ void __launch_bounds__(kBwdWarps * 32) k_raster_bwd(BwdArgs b) {
           C[k][0] = fmaf(cr, w, C[k][0]);
           C[k][1] = fmaf(cg, w, C[k][1]);
           C[k][2] = fmaf(cb, w, C[k][2]);
-          const float inv1m = 1.0f / (1.0f - al);
+          // 1 - alpha is in [0.01, 1]: the approximate reciprocal (2 ulp)
+          // is far inside the gradient's tolerance
+          const float inv1m = __fdividef(1.0f, 1.0f - al);
           float dal = gO[k][0] * (cr * T[k] - (O[k][0] - C[k][0]) * inv1m) +
                       gO[k][1] * (cg * T[k] - (O[k][1] - C[k][1]) * inv1m) +
                       gO[k][2] * (cb * T[k] - (O[k][2] - C[k][2]) * inv1m) + gA[k] * Tf[k] * inv1m;
